@@ -1,0 +1,323 @@
+"""Benchmark: the fused colour chain on one 4096x4096 RGBA8 sRGB image.
+
+Workload (the metric's configuration): sRGB -> linear -> XYZ D65 -> Bradford to
+D50 -> Oklab -> L*1.1, C*0.9 -> back -> sRGB RGBA8, seeded gradient + uniform +-16
+noise, random alpha.  One step = one pass of the compiled Program over one image.
+
+  value     fused executor (one CUDA-graph-replayed kernel), inputs resident in HBM,
+            Mpix/s of source pixels; 4 input/output buffer pairs are rotated (536 MB,
+            larger than the 129 MB L2) so no step reads what the previous one left in L2
+  e2e       same metric through Executable.run_host (C-ABI zs_run_host) from pinned host
+            memory: host->device copy, kernel, device->host copy every step
+  plain     the same Program lowered as plain per-op FP32 CUDA kernels (and FP16)
+  roofline  achieved HBM GB/s of the chain kernel (8 algorithmic bytes per pixel)
+            against the measured copy bandwidth
+  cpu_baseline  the plain per-op FP32 CPU pipeline (oracle port, OpenMP) on a bounded
+            sample of the same image
+
+--impl reference times the reference's CPU path restated in C (the oracle port,
+all host threads) on the same workload, one bounded sample per step.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+W = H = 4096
+NPX = W * H
+ALGO_BYTES = NPX * 8
+METRIC = "Mpix/s fused+batched FP16-store vs plain per-op FP32 on GB300 at ≤1 LSB; %HBM peak"
+
+
+def _peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def _profiled_traffic():
+    """dram bytes per launch of the chain kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "chain_srgb8_4096.md")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("dram_bytes_per_launch:"):
+                    return int(line.split(":")[1].strip())
+    except OSError:
+        pass
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def cpu_baseline(seconds: float = 10.0, threads: int = 0):
+    """The plain per-op FP32 CPU pipeline (oracle port) on a bounded sample: 1024 rows
+    of the 4096-wide image, repeated until `seconds` have passed."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import numpy as np
+    import oracle
+    import pipelines as P
+    from zosimos_gb300.synthetic import srgb_gradient_noise
+
+    oracle.build()
+    if threads:
+        oracle.set_threads(threads)
+    cores = oracle.max_threads()
+    sample = srgb_gradient_noise(W, 1024, seed=1)
+    P.oracle_chain(sample[:64], f32=True)          # warm-up
+    n, t0 = 0, time.perf_counter()
+    while True:
+        P.oracle_chain(sample, f32=True)
+        n += 1
+        el = time.perf_counter() - t0
+        if el >= seconds:
+            break
+    mpix = n * sample.shape[0] * sample.shape[1] / el / 1e6
+    return {"value": round(mpix, 3), "unit": "Mpix/s", "cores": cores, "kind": "port",
+            "sample": f"{n} x 4096x1024 RGBA8 tiles of the 4096x4096 image, plain per-op FP32 pipeline "
+                      f"(oracle restatement, OpenMP), {el:.1f} s"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle
+    import pipelines as P
+    from zosimos_gb300.synthetic import srgb_gradient_noise
+
+    oracle.build()
+    cores = oracle.max_threads()
+    rows = 256
+    sample = srgb_gradient_noise(W, rows, seed=1)
+    for _ in range(args.warmup):
+        P.oracle_chain(sample, f32=True)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        P.oracle_chain(sample, f32=True)
+    el = time.perf_counter() - t0
+    mpix = args.steps * W * rows / el / 1e6
+    line = {"metric": METRIC, "value": round(mpix, 3), "unit": "Mpix/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(el / args.steps * 1e3, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": "fused colour chain, 4096x4096 RGBA8 sRGB (bounded sample: 4096x256 rows "
+                                   "per step)", "pipeline": "plain per-op FP32 CPU (reference restated)"},
+            "cpu_baseline": {"value": round(mpix, 3), "unit": "Mpix/s", "cores": cores, "kind": "port",
+                             "sample": f"4096x{rows} RGBA8 per step"},
+            "e2e": {"value": round(mpix, 3), "unit": "Mpix/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, rank, world, dist):
+    import ctypes
+
+    import numpy as np
+    import torch
+
+    import zosimos_gb300 as zs
+    from zosimos_gb300.synthetic import srgb_gradient_noise
+    from zosimos_gb300.workloads import color_chain, rgba_bytes
+
+    dev = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(dev)
+    stream = torch.cuda.Stream()          # a real stream: graphs cannot capture the legacy default stream
+    sh = stream.cuda_stream
+
+    img = srgb_gradient_noise(W, H, seed=1 + rank)
+    host_in = rgba_bytes(img)
+
+    def lowered(mode):
+        c, _, _ = color_chain(W, H)
+        return zs.Linker.from_included().compile(c).lower_to(zs.Capabilities(device=dev, mode=mode, use_graph=True))
+
+    fused = lowered(zs.Mode.Fused)
+    plain = lowered(zs.Mode.PerOpF32)
+    plain16 = lowered(zs.Mode.PerOpF16)
+
+    ROT = 4
+    ins = [zs.DeviceBuffer(NPX * 4) for _ in range(ROT)]
+    outs = [zs.DeviceBuffer(NPX * 4) for _ in range(ROT)]
+    for b in ins:
+        b.upload(host_in)
+
+    # correctness gate on this very workload: fused within 1 LSB of plain per-op FP32
+    fused.run_device([ins[0].ptr], [outs[0].ptr], sh)
+    plain.run_device([ins[0].ptr], [outs[1].ptr], sh)
+    torch.cuda.synchronize()
+    a = outs[0].download(np.empty((H, W * 4), np.uint8))
+    b = outs[1].download(np.empty((H, W * 4), np.uint8))
+    max_lsb = int(np.abs(a.astype(np.int16) - b.astype(np.int16)).max())
+
+    def timed(exe, steps, warmup):
+        for i in range(warmup):
+            exe.run_device([ins[i % ROT].ptr], [outs[i % ROT].ptr], sh)
+        torch.cuda.synchronize()
+        if dist:
+            dist.barrier()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        k0 = zs.kernel_launch_count()
+        e0.record(stream)
+        for i in range(steps):
+            exe.run_device([ins[i % ROT].ptr], [outs[i % ROT].ptr], sh)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        launches = zs.kernel_launch_count() - k0
+        ms = e0.elapsed_time(e1)
+        if dist:
+            t = torch.tensor([ms], device="cuda")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms / steps, launches
+
+    with ClockSampler(dev) as clocks:
+        ms_fused, launches = timed(fused, args.steps, args.warmup)
+    ms_plain, _ = timed(plain, max(3, args.steps // 4), args.warmup)
+    ms_plain16, _ = timed(plain16, max(3, args.steps // 4), args.warmup)
+
+    # end to end through the C ABI with pinned host buffers
+    lib = zs._lib()
+    hin = lib.zs_host_alloc(NPX * 4)
+    hout = lib.zs_host_alloc(NPX * 4)
+    ctypes.memmove(hin, host_in.ctypes.data, NPX * 4)
+    inp = (ctypes.c_void_p * 1)(hin)
+    outp = (ctypes.c_void_p * 1)(hout)
+    for _ in range(args.warmup):
+        zs._check(lib.zs_run_host(fused._h, inp, 1, outp, 1))
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        zs._check(lib.zs_run_host(fused._h, inp, 1, outp, 1))
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if dist:
+        t = torch.tensor([e2e_s], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    lib.zs_host_free(hin)
+    lib.zs_host_free(hout)
+
+    if rank != 0:
+        return
+    peak, peak_kind = _peaks()
+    mpix = world * NPX / (ms_fused * 1e-3) / 1e6
+    achieved = ALGO_BYTES / (ms_fused * 1e-3) / 1e9
+    traffic = _profiled_traffic()
+    line = {
+        "metric": METRIC, "value": round(mpix, 1), "unit": "Mpix/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_fused, 4), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32 (RGBA8 storage)", "data": "synthetic",
+        "config": {"workload": "fused colour chain (sRGB->XYZ D65->Bradford D50->Oklab->L*1.1,C*0.9->back->sRGB), "
+                               "4096x4096 RGBA8 sRGB per GPU, seeded gradient+noise",
+                   "l2": "4 rotating input/output buffer pairs (536 MB) > 129 MB L2",
+                   "parallelism": f"replicas x{world}", "graph": "CUDA graph replay"},
+        "plain_per_op_fp32": {"value": round(world * NPX / (ms_plain * 1e-3) / 1e6, 1), "unit": "Mpix/s",
+                              "ms_per_step": round(ms_plain, 4), "kernels": plain.kernel_count()},
+        "per_op_fp16": {"value": round(world * NPX / (ms_plain16 * 1e-3) / 1e6, 1), "unit": "Mpix/s",
+                        "ms_per_step": round(ms_plain16, 4), "kernels": plain16.kernel_count()},
+        "speedup_vs_plain_fp32": round(ms_plain / ms_fused, 2),
+        "max_lsb_vs_plain_fp32": max_lsb,
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_launch": ALGO_BYTES,
+                     "traffic": traffic},
+        "e2e": {"value": round(world * NPX / e2e_s / 1e6, 1), "unit": "Mpix/s",
+                "h2d_bytes_per_step": NPX * 4, "d2h_bytes_per_step": NPX * 4, "ms_per_step": round(e2e_s * 1e3, 3)},
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args.cpu_seconds)
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    dist = None
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as td
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        td.init_process_group("nccl")
+        dist = td
+    try:
+        run_ours(args, rank, world, dist)
+    finally:
+        if dist:
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

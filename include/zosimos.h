@@ -1,0 +1,286 @@
+/*
+ * zosimos.h -- C ABI of the GB300 executor for zosimos' compiled raster pipeline.
+ *
+ * Every entry point replaces one call of the reference's Rust API (paths inside
+ * the zosimos project, cited per function).  The wgpu backend of the reference
+ * is replaced by hand-written CUDA kernels for sm_103a; the API shape (Pool,
+ * CommandBuffer, Linker/Program, Executable, Environment, Execution, Retire)
+ * is kept so that a thin FFI crate can bind it.
+ *
+ * Conventions
+ *  - Every function returns an int status (ZS_OK = 0) unless stated otherwise;
+ *    zs_last_error() returns a thread-local description of the last failure.
+ *  - Handles are opaque; none is thread-safe, separate handles may be used from
+ *    separate threads (an Execution owns one CUDA stream).
+ *  - Registers are the SSA value ids of a command buffer (command.rs:32).
+ *  - No C++ exception crosses this boundary; no user error aborts the process.
+ */
+#ifndef ZOSIMOS_GB300_H
+#define ZOSIMOS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes: CommandError / CompileError / LaunchError / StartError /
+ *      StepError / RetireError kinds (command.rs:650-717, program.rs:374-381,
+ *      run.rs:369-448). */
+enum {
+    ZS_OK = 0,
+    ZS_ERR_TYPE = 1,            /* CommandError::TYPE_ERR, ConflictingTypes, BadDescriptor */
+    ZS_ERR_UNIMPLEMENTED = 2,   /* CommandError::UNIMPLEMENTED, CompileError::NotYetImplemented */
+    ZS_ERR_BAD_REGISTER = 3,    /* CommandError::BAD_REGISTER */
+    ZS_ERR_OTHER = 4,           /* CommandError::OTHER / INVALID_CALL */
+    ZS_ERR_LAUNCH = 5,          /* LaunchError */
+    ZS_ERR_MISMATCHED_DESCRIPTOR = 6, /* StartError::MismatchedDescriptor */
+    ZS_ERR_MISSING_KEY = 7,     /* StartError::MissingKey / unbound input */
+    ZS_ERR_DEVICE = 8,          /* a CUDA runtime error */
+    ZS_ERR_TIMEOUT = 9,         /* a bounded device wait gave up */
+    ZS_ERR_INVALID_ARG = 10,    /* null handle / pointer / size out of range */
+    ZS_ERR_OUT_OF_MEMORY = 11,
+    ZS_ERR_STEP_LIMIT = 12      /* StepLimits exhausted (run.rs:3000-3013) */
+};
+
+/* ---- descriptor vocabulary (image-canvas 0.5.1 as used by buffer.rs:1-115;
+ *      numeric codes of bits/parts/transfer follow lib/std/src/stage.frag:102-176). */
+enum { /* SampleBits */
+    ZS_BITS_UINT8 = 0, ZS_BITS_UINT332 = 1, ZS_BITS_UINT233 = 2, ZS_BITS_UINT16 = 3,
+    ZS_BITS_UINT4X4 = 4, ZS_BITS_UINT_444 = 5, ZS_BITS_UINT444_ = 6, ZS_BITS_UINT565 = 7,
+    ZS_BITS_UINT8X2 = 8, ZS_BITS_UINT8X3 = 9, ZS_BITS_UINT8X4 = 10, ZS_BITS_UINT16X2 = 11,
+    ZS_BITS_UINT16X3 = 12, ZS_BITS_UINT16X4 = 13, ZS_BITS_UINT1010102 = 14,
+    ZS_BITS_UINT2101010 = 15, ZS_BITS_UINT101010_ = 16, ZS_BITS_UINT_101010 = 17,
+    ZS_BITS_FLOAT16X4 = 18, ZS_BITS_FLOAT32X4 = 19
+};
+enum { /* SampleParts */
+    ZS_PARTS_A = 0, ZS_PARTS_R = 1, ZS_PARTS_G = 2, ZS_PARTS_B = 3, ZS_PARTS_LUMA = 4,
+    ZS_PARTS_LUMAA = 5, ZS_PARTS_RGB = 6, ZS_PARTS_BGR = 7, ZS_PARTS_RGBA = 8,
+    ZS_PARTS_RGBX = 9, ZS_PARTS_BGRA = 10, ZS_PARTS_BGRX = 11, ZS_PARTS_ARGB = 12,
+    ZS_PARTS_XRGB = 13, ZS_PARTS_ABGR = 14, ZS_PARTS_XBGR = 15, ZS_PARTS_YUV = 16,
+    ZS_PARTS_LAB = 17, ZS_PARTS_LABA = 18, ZS_PARTS_LCH = 19, ZS_PARTS_LCHA = 20
+};
+enum { /* Transfer */
+    ZS_TRANSFER_BT709 = 0, ZS_TRANSFER_BT470M = 1, ZS_TRANSFER_BT601 = 2,
+    ZS_TRANSFER_SMPTE240 = 3, ZS_TRANSFER_LINEAR = 4, ZS_TRANSFER_SRGB = 5,
+    ZS_TRANSFER_BT2020_10BIT = 6, ZS_TRANSFER_BT2020_12BIT = 7, ZS_TRANSFER_SMPTE2084 = 8,
+    ZS_TRANSFER_BT2100PQ = 9, ZS_TRANSFER_BT2100HLG = 10, ZS_TRANSFER_LINEAR_SCENE = 11
+};
+enum { /* Color kind */
+    ZS_COLOR_RGB = 0, ZS_COLOR_OKLAB = 1, ZS_COLOR_SRLAB2 = 2, ZS_COLOR_SCALARS = 3
+};
+enum { /* Primaries */
+    ZS_PRIMARIES_BT601_525 = 0, ZS_PRIMARIES_BT601_625 = 1, ZS_PRIMARIES_BT709 = 2,
+    ZS_PRIMARIES_SMPTE240 = 3, ZS_PRIMARIES_BT2020 = 4, ZS_PRIMARIES_BT2100 = 5,
+    ZS_PRIMARIES_P3 = 6, ZS_PRIMARIES_ADOBE_RGB = 7, ZS_PRIMARIES_XYZ = 8
+};
+enum { /* Whitepoint */
+    ZS_WP_A = 0, ZS_WP_B = 1, ZS_WP_C = 2, ZS_WP_D50 = 3, ZS_WP_D55 = 4, ZS_WP_D65 = 5,
+    ZS_WP_D75 = 6, ZS_WP_E = 7, ZS_WP_F2 = 8, ZS_WP_F7 = 9, ZS_WP_F11 = 10
+};
+enum { ZS_ALPHA_STRAIGHT = 0, ZS_ALPHA_PREMULTIPLIED = 1 };
+
+/* Descriptor (buffer.rs:20-27): layout + colour + texel.  row_stride 0 means
+ * tightly packed rows (width * texel bytes). */
+typedef struct zs_descriptor {
+    uint32_t width, height;
+    uint64_t row_stride;
+    uint32_t bits, parts;                               /* Texel */
+    uint32_t color, primaries, transfer, whitepoint;    /* Color */
+    uint32_t alpha;                                     /* ZS_ALPHA_* (extension) */
+    uint32_t reserved;
+} zs_descriptor;
+
+/* Rectangle (command.rs:3496-3592): [x, max_x) x [y, max_y). */
+typedef struct zs_rect { uint32_t x, y, max_x, max_y; } zs_rect;
+
+/* ---- descriptor helpers ------------------------------------------------- */
+/* Descriptor::with_srgb_image for an RGBA8 image (buffer.rs). */
+int zs_descriptor_srgb_rgba8(uint32_t width, uint32_t height, zs_descriptor *out);
+/* Descriptor::is_consistent (buffer.rs) -- 1 when valid, 0 otherwise. */
+int zs_descriptor_is_consistent(const zs_descriptor *desc);
+/* Bytes of the host (tightly packed or row_stride) layout. */
+uint64_t zs_descriptor_byte_len(const zs_descriptor *desc);
+/* Bytes of one texel of `bits`. */
+uint32_t zs_texel_bytes(uint32_t bits);
+
+/* ---- errors ------------------------------------------------------------- */
+const char *zs_last_error(void);
+/* Library version string. */
+const char *zs_version(void);
+
+/* ---- Pool (pool.rs:180-455) --------------------------------------------- */
+typedef struct zs_pool zs_pool;
+zs_pool *zs_pool_new(void);                                   /* Pool::new           pool.rs:182 */
+void zs_pool_free(zs_pool *pool);
+/* Pool::insert (pool.rs:244): copies `bytes` (laid out as `desc`) into pinned host storage. */
+int zs_pool_insert(zs_pool *pool, const zs_descriptor *desc, const void *bytes, uint64_t *key);
+/* Pool::declare (pool.rs:281): an image slot without contents (e.g. an output). */
+int zs_pool_declare(zs_pool *pool, const zs_descriptor *desc, uint64_t *key);
+/* PoolImage::descriptor (pool.rs:661). */
+int zs_pool_descriptor(zs_pool *pool, uint64_t key, zs_descriptor *out);
+/* PoolImage::as_bytes (pool.rs:669): copy the host bytes out (len must match). */
+int zs_pool_read(zs_pool *pool, uint64_t key, void *dst, uint64_t len);
+/* PoolImageMut::as_bytes_mut (pool.rs:704): overwrite the host bytes in place. */
+int zs_pool_write(zs_pool *pool, uint64_t key, const void *src, uint64_t len);
+/* Direct pointer to the pinned host storage (valid until the image is removed). */
+int zs_pool_host_ptr(zs_pool *pool, uint64_t key, void **ptr, uint64_t *len);
+/* PoolImageMut::set_color (pool.rs:719): re-tag the colour of an image. */
+int zs_pool_set_descriptor(zs_pool *pool, uint64_t key, const zs_descriptor *desc);
+/* Pool::upload (pool.rs:292): make the image device resident (cudaMemcpy). */
+int zs_pool_upload(zs_pool *pool, uint64_t key);
+/* Device pointer of a device-resident image (GPU-resident IO). */
+int zs_pool_device_ptr(zs_pool *pool, uint64_t key, void **ptr);
+/* Remove an image. */
+int zs_pool_remove(zs_pool *pool, uint64_t key);
+/* Pool::clear_cache (pool.rs:450): release cached device buffers. */
+int zs_pool_clear_cache(zs_pool *pool);
+
+/* ---- CommandBuffer (command.rs:739-1765) --------------------------------- */
+typedef struct zs_cmd zs_cmd;
+zs_cmd *zs_cmd_new(void);
+void zs_cmd_free(zs_cmd *cmd);
+/* CommandBuffer::input (command.rs:743). */
+int zs_cmd_input(zs_cmd *cmd, const zs_descriptor *desc, uint32_t *reg);
+/* CommandBuffer::crop (command.rs:912). */
+int zs_cmd_crop(zs_cmd *cmd, uint32_t src, const zs_rect *rect, uint32_t *reg);
+/* CommandBuffer::color_convert (command.rs:986): `target` supplies color/texel fields;
+ * its width/height/row_stride are ignored (taken from src). */
+int zs_cmd_color_convert(zs_cmd *cmd, uint32_t src, const zs_descriptor *target, uint32_t *reg);
+/* CommandBuffer::chromatic_adaptation (command.rs:1112); method: 0 Xyz, 1 VonKries,
+ * 2 BradfordVonKries, 3 BradfordNonLinear. */
+int zs_cmd_chromatic_adaptation(zs_cmd *cmd, uint32_t src, uint32_t method, uint32_t target_wp,
+                                uint32_t *reg);
+/* CommandBuffer::inscribe (command.rs:1177).  Keeps the reference semantics exactly,
+ * including Rectangle::normalize's max_y = y + width (command.rs:3536-3543). */
+int zs_cmd_inscribe(zs_cmd *cmd, uint32_t below, const zs_rect *rect, uint32_t above,
+                    uint32_t *reg);
+/* Extension: inscribe at any placement inside `below` without the normalize
+ * stretch (centred placement needs it; no reference counterpart). */
+int zs_cmd_inscribe_placed(zs_cmd *cmd, uint32_t below, const zs_rect *rect, uint32_t above,
+                           uint32_t *reg);
+/* CommandBuffer::extract (command.rs:1221); channel: 0 R, 1 G, 2 B, 3 Alpha. */
+int zs_cmd_extract(zs_cmd *cmd, uint32_t src, uint32_t channel, uint32_t *reg);
+/* CommandBuffer::inject (command.rs:1360). */
+int zs_cmd_inject(zs_cmd *cmd, uint32_t below, uint32_t channel, uint32_t above, uint32_t *reg);
+/* CommandBuffer::transmute (command.rs:1276). */
+int zs_cmd_transmute(zs_cmd *cmd, uint32_t src, const zs_descriptor *target, uint32_t *reg);
+/* CommandBuffer::palette (command.rs:1442); width/height channel: 0 R, 1 G, 2 B, -1 none. */
+int zs_cmd_palette(zs_cmd *cmd, uint32_t palette, int32_t width_channel, int32_t height_channel,
+                   uint32_t indices, uint32_t *reg);
+/* CommandBuffer::bilinear (command.rs:1615); params = u_min,u_max,v_min,v_max,uv_min,uv_max. */
+int zs_cmd_bilinear(zs_cmd *cmd, const zs_descriptor *desc, const float params[24],
+                    uint32_t *reg);
+/* CommandBuffer::solid_rgba (command.rs:1526). */
+int zs_cmd_solid_rgba(zs_cmd *cmd, const zs_descriptor *desc, const float color[4],
+                      uint32_t *reg);
+/* CommandBuffer::affine (command.rs:1636); matrix row-major homogeneous in pixel units;
+ * sampling 0 Nearest, 1 BiLinear (BiLinear is UNIMPLEMENTED upstream, built here). */
+int zs_cmd_affine(zs_cmd *cmd, uint32_t below, const float matrix[9], uint32_t sampling,
+                  uint32_t above, uint32_t *reg);
+/* CommandBuffer::resize (command.rs:1675): the reference's nearest palette resize. */
+int zs_cmd_resize(zs_cmd *cmd, uint32_t src, uint32_t width, uint32_t height, uint32_t *reg);
+/* Extension of resize with a filter: 0 Box (area), 1 Lanczos-3, 2 Triangle. */
+int zs_cmd_resize_filtered(zs_cmd *cmd, uint32_t src, uint32_t width, uint32_t height,
+                           uint32_t filter, uint32_t *reg);
+/* CommandBuffer::blend (command.rs:1509, UNIMPLEMENTED upstream, built here):
+ * mode 0 Alpha/over, 1 multiply, 2 screen, 3 add; `above` placed at rect.x/rect.y. */
+int zs_cmd_blend(zs_cmd *cmd, uint32_t below, const zs_rect *rect, uint32_t above,
+                 uint32_t mode, uint32_t *reg);
+/* Extension: a 3x3 linear map applied to the colour channels in the image's own
+ * colour space (e.g. scaling Oklab L and C); alpha is kept. */
+int zs_cmd_color_matrix(zs_cmd *cmd, uint32_t src, const float matrix[9], uint32_t *reg);
+/* CommandBuffer::output (command.rs:1707). */
+int zs_cmd_output(zs_cmd *cmd, uint32_t src, uint32_t *reg, zs_descriptor *outformat);
+/* Describe a register (command.rs describe_reg). */
+int zs_cmd_describe(const zs_cmd *cmd, uint32_t reg, zs_descriptor *out);
+
+/* ---- Linker / Program (command.rs:2063-2185, program.rs:1284-1423) -------- */
+typedef struct zs_program zs_program;
+/* Linker::compile (command.rs:2069). */
+int zs_compile(const zs_cmd *cmd, zs_program **out);
+void zs_program_free(zs_program *program);
+
+/* Capabilities / lowering options (program.rs:1304 lower_to). */
+enum {
+    ZS_MODE_FUSED = 0,        /* fused per-pixel chains, FP16 storage at unfusable boundaries */
+    ZS_MODE_PER_OP_F32 = 1,   /* one kernel per op, FP32 RGBA intermediates (the plain baseline) */
+    ZS_MODE_PER_OP_F16 = 2    /* one kernel per op, FP16 RGBA intermediates */
+};
+typedef struct zs_capabilities {
+    int32_t device;           /* CUDA device ordinal */
+    uint32_t mode;            /* ZS_MODE_* */
+    uint32_t use_graph;       /* capture the kernel sequence as a CUDA graph and replay it */
+    uint32_t reserved;
+} zs_capabilities;
+
+typedef struct zs_executable zs_executable;
+/* Program::lower_to (program.rs:1304). */
+int zs_lower(const zs_program *program, const zs_capabilities *caps, zs_executable **out);
+void zs_executable_free(zs_executable *exe);
+/* Number of kernel launches one launch of this executable issues. */
+int zs_executable_kernel_count(const zs_executable *exe, uint32_t *count);
+/* Human readable plan (the analogue of Executable::dot, run.rs:491). */
+const char *zs_executable_describe(const zs_executable *exe);
+
+/* ---- Environment / Execution / Retire (run.rs:470-2998) ------------------ */
+typedef struct zs_environment zs_environment;
+typedef struct zs_execution zs_execution;
+/* Executable::from_pool (run.rs:471). */
+int zs_env_new(zs_executable *exe, zs_pool *pool, zs_environment **out);
+void zs_env_free(zs_environment *env);
+/* Environment::bind (run.rs:1171). */
+int zs_env_bind(zs_environment *env, uint32_t reg, uint64_t key);
+/* Environment::bind_output (run.rs:1207): write the output into an existing image. */
+int zs_env_bind_output(zs_environment *env, uint32_t reg, uint64_t key);
+/* Executable::launch (run.rs:1016): consumes `env` (even on failure). */
+int zs_launch(zs_executable *exe, zs_environment *env, zs_execution **out);
+/* Execution::is_running (run.rs:1382). */
+int zs_exec_is_running(const zs_execution *exec);
+/* Execution::step (run.rs:1389): enqueue the next instruction. */
+int zs_exec_step(zs_execution *exec);
+/* SyncPoint::block_on (run.rs:3019): wait for everything enqueued so far. */
+int zs_exec_sync(zs_execution *exec);
+/* Retire::output (run.rs:2809): the output moves into the pool; returns its key. */
+int zs_retire_output(zs_execution *exec, uint32_t reg, uint64_t *key);
+/* Retire::finish (run.rs:2962): release the execution. */
+void zs_exec_free(zs_execution *exec);
+
+/* ---- one-call drop-in for host buffers ------------------------------------ */
+/* Runs the whole executable once: inputs[i] bound to the i-th input register (in
+ * declaration order) from host memory, outputs[j] receive the j-th output (host
+ * memory).  Equivalent to insert/bind/launch/step/retire/read.  Host buffers that
+ * are pinned (zs_host_alloc) transfer at full link speed. */
+int zs_run_host(zs_executable *exe, const void *const *inputs, uint32_t n_inputs,
+                void *const *outputs, uint32_t n_outputs);
+/* Same, with device-resident inputs and outputs (no host copies). */
+int zs_run_device(zs_executable *exe, const void *const *inputs, uint32_t n_inputs,
+                  void *const *outputs, uint32_t n_outputs, void *stream);
+/* Pinned host memory helpers. */
+void *zs_host_alloc(uint64_t bytes);
+void zs_host_free(void *ptr);
+/* Device memory helpers (for device-resident IO through zs_run_device). */
+void *zs_device_alloc(uint64_t bytes);
+void zs_device_free(void *ptr);
+int zs_memcpy_h2d(void *dst, const void *src, uint64_t bytes);
+int zs_memcpy_d2h(void *dst, const void *src, uint64_t bytes);
+int zs_device_synchronize(void);
+
+/* ---- batched uneven images (the reference's batch-reuse case, tests/loop.rs:84-95) ---- */
+/* One persistent launch over many RGBA8 sRGB images of different sizes: per image
+ * the fused colour chain of `chain` (an executable whose single input and output are
+ * RGBA8 images and whose ops are per-pixel), a box fit-resize so the long side is
+ * `canvas`, and a centred inscribe on a transparent canvas x canvas image.
+ * images: device pointers of tightly packed RGBA8 sources; out: n * canvas^2 * 4 bytes. */
+int zs_batch_thumbnails(zs_executable *chain, const void *const *images, const uint32_t *widths,
+                        const uint32_t *heights, uint32_t n, uint32_t canvas, void *out,
+                        void *stream);
+
+/* Number of kernels this library has launched since the process started. */
+uint64_t zs_kernel_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

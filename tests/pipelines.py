@@ -1,0 +1,270 @@
+"""The reference's own test pipelines (lib/zosimos/tests/blend.rs) and the BASELINE
+workloads, each expressed twice: through the executor's API (``ours_*``, runs on the
+GPU) and through the CPU oracle (``oracle_*``).  Both return texel bytes as
+(H, row_bytes) uint8 arrays (or float arrays for float outputs)."""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+import oracle as O
+import zosimos_gb300 as zs
+from zosimos_gb300 import (Affine, AffineSample, Bits, Capabilities, ChromaticAdaptationMethod, ColorKind,
+                           CommandBuffer, Descriptor, Parts, Pool, Primaries, Rectangle, Transfer, Whitepoint)
+
+
+from zosimos_gb300.workloads import rgba_bytes  # noqa: E402
+
+
+def run(cmds, pool, binds, outputs, mode=zs.Mode.Fused):
+    keys = zs.run_pipeline(cmds, pool, binds, outputs, Capabilities(mode=mode))
+    return [pool.read(k) for k in keys]
+
+
+def inv3_f32(m) -> np.ndarray:
+    """Inverse of an f32 row-major 3x3 computed in FP64 by the adjugate, rounded to f32."""
+    a = np.asarray(m, dtype=np.float64).reshape(9)
+    c0 = a[4] * a[8] - a[5] * a[7]
+    c1 = a[5] * a[6] - a[3] * a[8]
+    c2 = a[3] * a[7] - a[4] * a[6]
+    det = a[0] * c0 + a[1] * c1 + a[2] * c2
+    r = np.array([c0, a[2] * a[7] - a[1] * a[8], a[1] * a[5] - a[2] * a[4], c1, a[0] * a[8] - a[2] * a[6],
+                  a[2] * a[3] - a[0] * a[5], c2, a[1] * a[6] - a[0] * a[7], a[0] * a[4] - a[1] * a[3]]) / det
+    return r.astype(np.float32)
+
+
+# ---------------------------------------------------------------- blend.rs:83-120 composed
+
+
+def ours_composed(bg, fg, mode=zs.Mode.Fused):
+    pool = Pool()
+    kb, kf = pool.insert_srgb(bg), pool.insert_srgb(fg)
+    c = CommandBuffer()
+    b = c.input(pool.descriptor(kb))
+    f = c.input(pool.descriptor(kf))
+    r = c.inscribe(b, Rectangle(0, 0, fg.shape[1], fg.shape[0]), f)
+    o, _ = c.output(r)
+    return run(c, pool, [(b, kb), (f, kf)], [o], mode)[0]
+
+
+def oracle_composed(bg, fg):
+    out = rgba_bytes(bg).copy()
+    fh, fw = fg.shape[:2]
+    # Rectangle::normalize (command.rs:3536-3543): max_y = y + width.
+    O.gather_quad(rgba_bytes(fg), fw, fh, out, bg.shape[1], bg.shape[0], 4, (0, 0, fw, fw))
+    return out
+
+
+# ---------------------------------------------------------------- blend.rs:122-167 affine
+
+
+def affine_45(bg, fg, sampling=AffineSample.Nearest) -> Affine:
+    fh, fw = fg.shape[:2]
+    bh, bw = bg.shape[:2]
+    return (Affine.new(sampling).shift(-float(fw // 2), -float(fh // 2)).rotate(math.pi / 4.0)
+            .shift(float(bw // 2), float(bh // 2)))
+
+
+def ours_affine(bg, fg, sampling=AffineSample.Nearest, mode=zs.Mode.Fused):
+    pool = Pool()
+    kb, kf = pool.insert_srgb(bg), pool.insert_srgb(fg)
+    c = CommandBuffer()
+    b = c.input(pool.descriptor(kb))
+    f = c.input(pool.descriptor(kf))
+    r = c.affine(b, affine_45(bg, fg, sampling), f)
+    o, _ = c.output(r)
+    return run(c, pool, [(b, kb), (f, kf)], [o], mode)[0]
+
+
+def oracle_affine(bg, fg):
+    out = rgba_bytes(bg).copy()
+    inv = inv3_f32(affine_45(bg, fg).transformation)
+    fh, fw = fg.shape[:2]
+    O.affine_nearest_bytes(rgba_bytes(fg), fw, fh, out, bg.shape[1], bg.shape[0], 4, inv)
+    return out
+
+
+def oracle_affine_bilinear(bg, fg):
+    below = O.decode(O.SRGB_RGBA8, rgba_bytes(bg), bg.shape[1], bg.shape[0])
+    above = O.decode(O.SRGB_RGBA8, rgba_bytes(fg), fg.shape[1], fg.shape[0])
+    inv = inv3_f32(affine_45(bg, fg, AffineSample.BiLinear).transformation)
+    O.affine(below, above, inv, True)
+    return O.encode(O.SRGB_RGBA8, below)
+
+
+# ---------------------------------------------------------------- blend.rs:169-197 adapted
+
+
+def ours_adapted(bg, mode=zs.Mode.Fused):
+    pool = Pool()
+    kb = pool.insert_srgb(bg)
+    c = CommandBuffer()
+    b = c.input(pool.descriptor(kb))
+    r = c.chromatic_adaptation(b, ChromaticAdaptationMethod.VonKries, Whitepoint.D50)
+    o, _ = c.output(r)
+    return run(c, pool, [(b, kb)], [o], mode)[0]
+
+
+def oracle_adapted(bg):
+    h, w = bg.shape[:2]
+    lin = O.decode(O.SRGB_RGBA8, rgba_bytes(bg), w, h)
+    m = np.linalg.inv(O.rgb_to_xyz("Bt709", "D50")) @ O.adaptation("VonKries", "D65", "D50") @ O.rgb_to_xyz()
+    O.mat3(lin, m)
+    return O.encode(O.SRGB_RGBA8, lin)
+
+
+# ---------------------------------------------------------------- blend.rs:199-225 convert_bt709
+
+
+def ours_convert_bt709(bg, mode=zs.Mode.Fused):
+    pool = Pool()
+    h, w = bg.shape[:2]
+    d709 = Descriptor.srgb_rgba8(w, h).with_color(transfer=Transfer.Bt709)
+    k = pool.insert(d709, rgba_bytes(bg))
+    c = CommandBuffer()
+    i = c.input(d709)
+    r = c.color_convert(i, Descriptor.srgb_rgba8(w, h))
+    o, _ = c.output(r)
+    return run(c, pool, [(i, k)], [o], mode)[0]
+
+
+def oracle_convert_bt709(bg):
+    h, w = bg.shape[:2]
+    f709 = O.Format(O.BITS["UInt8x4"], O.PARTS["RgbA"], O.TRANSFER["Bt709"], False)
+    lin = O.decode(f709, rgba_bytes(bg), w, h)
+    return O.encode(O.SRGB_RGBA8, lin)
+
+
+# ---------------------------------------------------------------- blend.rs:423-447 swapped
+
+
+def ours_swapped(bg, mode=zs.Mode.Fused):
+    pool = Pool()
+    kb = pool.insert_srgb(bg)
+    c = CommandBuffer()
+    i = c.input(pool.descriptor(kb))
+    cr = c.extract(i, 0)
+    cg = c.extract(i, 1)
+    t = c.inject(i, 1, cr)
+    s = c.inject(t, 0, cg)
+    o, _ = c.output(s)
+    return run(c, pool, [(i, kb)], [o], mode)[0]
+
+
+def oracle_swapped(bg):
+    h, w = bg.shape[:2]
+    lin = O.decode(O.SRGB_RGBA8, rgba_bytes(bg), w, h)
+    chans = []
+    for part in ("R", "G"):
+        f = O.Format(O.BITS["UInt8x4"], O.PARTS[part], O.TRANSFER["Srgb"], False)
+        chans.append(O.decode(f, O.encode(f, lin), w, h))
+    x = lin.copy()
+    O.inject(x, chans[0], [0, 1, 0, 0], [1, 0, 0, 0])
+    O.inject(x, chans[1], [1, 0, 0, 0], [0, 1, 0, 0])
+    return O.encode(O.SRGB_RGBA8, x)
+
+
+# ---------------------------------------------------------------- blend.rs:340-375 transmute
+
+
+def luma_alpha16_desc(w, h) -> Descriptor:
+    return Descriptor(w, h, Bits.UInt16x2, Parts.LumaA, ColorKind.Rgb, Primaries.Bt709, Transfer.Srgb,
+                      Whitepoint.D65)
+
+
+def ours_transmute(bg, mode=zs.Mode.Fused):
+    pool = Pool()
+    kb = pool.insert_srgb(bg)
+    h, w = bg.shape[:2]
+    c = CommandBuffer()
+    i = c.input(pool.descriptor(kb))
+    t = c.transmute(i, luma_alpha16_desc(w, h))
+    o, _ = c.output(t)
+    return run(c, pool, [(i, kb)], [o], mode)[0]
+
+
+# ---------------------------------------------------------------- blend.rs:377-421 palette
+
+RAMP = dict(u_min=[0.0, 0.0, 0.0, 1.0], u_max=[0.7, 0.0, 0.0, 1.0], v_min=[0.0, 0.0, 0.0, 1.0],
+            v_max=[0.0, 0.7, 0.0, 1.0], uv_min=[0.0, 0.0, 0.0, 1.0], uv_max=[0.3, 0.3, 0.0, 1.0])
+
+
+def ours_palette(bg, mode=zs.Mode.Fused):
+    pool = Pool()
+    kb = pool.insert_srgb(bg)
+    c = CommandBuffer()
+    i = c.input(pool.descriptor(kb))
+    ramp = c.bilinear(Descriptor.srgb_rgba8(400, 400), **RAMP)
+    p = c.palette(i, 0, 1, ramp)
+    o, _ = c.output(p)
+    return run(c, pool, [(i, kb)], [o], mode)[0]
+
+
+def oracle_palette(bg):
+    # The ramp is computed in f32 exactly like the GPU construct; encode and decode of the
+    # sRGB8 texels are exact (FP64, correctly rounded to f32) like the GPU tables.
+    ramp = O.bilinear_construct(400, 400, **RAMP, f32=True).astype(np.float64)
+    rb = O.encode(O.SRGB_RGBA8, ramp)
+    rd = O.decode(O.SRGB_RGBA8, rb, 400, 400).astype(np.float32)
+    ix, iy = O.palette_index(bg.shape[1], bg.shape[0], rd[..., 0], rd[..., 1])
+    return rgba_bytes(bg[iy, ix])
+
+
+# ---------------------------------------------------------------- blend.rs:449-575 oklab / srlab2
+
+GRID = dict(u_min=[0.4, 0.0, 0.0, 1.0], v_min=[0.4, 0.0, 0.0, 1.0], u_max=[0.4, 0.0, 1.0, 1.0],
+            v_max=[0.4, 1.0, 0.0, 1.0], uv_min=[0.0, 0.0, 0.0, 0.0], uv_max=[0.0, 0.0, 0.0, 0.0])
+
+
+def ours_lab_grid(space: str, mode=zs.Mode.Fused):
+    pool = Pool()
+    c = CommandBuffer()
+    dist = Descriptor.srgb_rgba8(400, 400).with_color(color=ColorKind.Scalars, transfer=Transfer.Linear)
+    grid = c.bilinear(dist, **GRID)
+    kind = ColorKind.Oklab if space == "oklab" else ColorKind.SrLab2
+    lch = c.transmute(grid, dist.with_color(color=kind, parts=Parts.LchA, whitepoint=Whitepoint.D65))
+    conv = c.color_convert(lch, Descriptor.srgb_rgba8(400, 400))
+    o, _ = c.output(conv)
+    return run(c, pool, [], [o], mode)[0]
+
+
+def oracle_lab_grid(space: str):
+    grid = O.bilinear_construct(400, 400, **GRID)
+    fmt_u8 = O.Format(O.BITS["UInt8x4"], O.PARTS["RgbA"], O.TRANSFER["Linear"], False)
+    gb = O.encode(fmt_u8, grid)
+    lch = O.Format(O.BITS["UInt8x4"], O.PARTS["LchA"], O.TRANSFER["LabLch"], False)
+    lab = O.decode(lch, gb, 400, 400)
+    t = np.linalg.inv(O.rgb_to_xyz("Bt709", "D65"))
+    if space == "oklab":
+        O.oklab_decode(lab, t)
+    else:
+        O.srlab2_decode(lab, t, O.whitepoint_xyz("D65"))
+    return O.encode(O.SRGB_RGBA8, lab)
+
+
+# ---------------------------------------------------------------- the fused colour chain (config 2)
+
+from zosimos_gb300.workloads import OKLAB_SCALE, color_chain as chain_commands  # noqa: E402
+
+
+def oracle_chain(img, f32=False):
+    """The same chain, one full pass per op (f32=True: the plain per-op CPU pipeline)."""
+    h, w = img.shape[:2]
+    x = O.decode(O.SRGB_RGBA8, rgba_bytes(img), w, h, f32=f32)
+    a1 = np.linalg.inv(O.rgb_to_xyz("Bt709", "D50")) @ O.adaptation("BradfordVonKries", "D65", "D50") @ O.rgb_to_xyz()
+    O.mat3(x, a1, f32=f32)
+    O.oklab_encode(x, O.rgb_to_xyz("Bt709", "D50"), f32=f32)
+    O.mat3(x, np.asarray(OKLAB_SCALE).reshape(3, 3), f32=f32)
+    O.oklab_decode(x, np.linalg.inv(O.rgb_to_xyz("Bt709", "D50")), f32=f32)
+    a2 = np.linalg.inv(O.rgb_to_xyz()) @ O.adaptation("BradfordVonKries", "D50", "D65") @ O.rgb_to_xyz("Bt709", "D50")
+    O.mat3(x, a2, f32=f32)
+    return O.encode(O.SRGB_RGBA8, x, f32=f32)
+
+
+def ours_chain(img, mode=zs.Mode.Fused):
+    h, w = img.shape[:2]
+    c, i, o = chain_commands(w, h)
+    pool = Pool()
+    k = pool.insert_srgb(img)
+    return run(c, pool, [(i, k)], [o], mode)[0]

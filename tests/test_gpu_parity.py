@@ -1,0 +1,111 @@
+"""GPU parity: the executor's CUDA path against the CPU oracle and the reference's
+golden hashes.  Integer work (copies, gathers, nearest coordinates, transmute) must
+be bit-exact; 8-bit outputs of colour arithmetic within 1 LSB of the FP64 oracle."""
+import numpy as np
+import pytest
+
+import pipelines as P
+import zosimos_gb300 as zs
+from imgutil import blockhash256
+from zosimos_gb300.synthetic import srgb_gradient_noise
+
+pytestmark = pytest.mark.gpu
+LSB = 1   # tolerance of 8-bit outputs against the FP64 oracle
+
+
+def maxdiff(a, b):
+    return int(np.abs(a.astype(np.int64) - b.astype(np.int64)).max())
+
+
+@pytest.mark.parametrize("mode", [zs.Mode.Fused, zs.Mode.PerOpF32, zs.Mode.PerOpF16])
+@pytest.mark.parametrize("shape", [(256, 256), (29, 37), (1, 1), (3, 5)])
+def test_chain_vs_oracle(mode, shape):
+    h, w = shape
+    img = srgb_gradient_noise(w, h, seed=1)
+    ours = P.ours_chain(img, mode)
+    ref = P.oracle_chain(img)
+    assert ours.shape == ref.shape
+    assert maxdiff(ours, ref) <= LSB
+    # alpha is carried exactly
+    assert (ours.reshape(h, w, 4)[..., 3] == img[..., 3]).all()
+
+
+def test_chain_is_one_kernel():
+    c, _, _ = P.chain_commands(64, 64)
+    exe = zs.Linker.from_included().compile(c).lower_to()
+    assert exe.kernel_count() == 1
+    assert "fused chain kernel" in exe.describe()
+
+
+def test_chain_run_host_and_device_agree():
+    img = srgb_gradient_noise(512, 384, seed=2)
+    c, _, _ = P.chain_commands(512, 384)
+    exe = zs.Linker.from_included().compile(c).lower_to()
+    out_h = np.empty((384, 512 * 4), np.uint8)
+    exe.run_host([P.rgba_bytes(img)], [out_h])
+    src = zs.DeviceBuffer(img.nbytes)
+    dst = zs.DeviceBuffer(img.nbytes)
+    src.upload(P.rgba_bytes(img))
+    exe.run_device([src.ptr], [dst.ptr])
+    exe.run_device([src.ptr], [dst.ptr])     # graph replay
+    zs.device_synchronize()
+    out_d = dst.download(np.empty_like(out_h))
+    assert (out_h == out_d).all()
+    assert maxdiff(out_h, P.oracle_chain(img)) <= LSB
+
+
+def test_composed(background, foreground, goldens):
+    ours = P.ours_composed(background, foreground)
+    assert (ours == P.oracle_composed(background, foreground)).all()
+    assert blockhash256(ours.reshape(512, 512, 4)) in goldens["composed"]
+
+
+@pytest.mark.parametrize("mode", [zs.Mode.Fused, zs.Mode.PerOpF32])
+def test_affine_nearest(background, foreground, goldens, mode):
+    ours = P.ours_affine(background, foreground, mode=mode)
+    assert (ours == P.oracle_affine(background, foreground)).all()
+    assert blockhash256(ours.reshape(512, 512, 4)) in goldens["affine"]
+
+
+def test_affine_bilinear(background, foreground):
+    ours = P.ours_affine(background, foreground, zs.AffineSample.BiLinear)
+    assert maxdiff(ours, P.oracle_affine_bilinear(background, foreground)) <= LSB
+
+
+def test_adapted(background, goldens):
+    ours = P.ours_adapted(background)
+    assert maxdiff(ours, P.oracle_adapted(background)) <= LSB
+    assert blockhash256(ours.reshape(512, 512, 4)) in goldens["adapted"]
+
+
+def test_convert_bt709(background, goldens):
+    ours = P.ours_convert_bt709(background)
+    assert maxdiff(ours, P.oracle_convert_bt709(background)) <= LSB
+    assert blockhash256(ours.reshape(512, 512, 4)) in goldens["convert_bt709"]
+
+
+@pytest.mark.parametrize("mode", [zs.Mode.Fused, zs.Mode.PerOpF32])
+def test_swapped(background, goldens, mode):
+    ours = P.ours_swapped(background, mode)
+    assert maxdiff(ours, P.oracle_swapped(background)) <= LSB
+    assert blockhash256(ours.reshape(512, 512, 4)) in goldens["swapped"]
+
+
+def test_transmute_bytes_exact(background):
+    # tests/blend.rs:371-372: the transmuted image has exactly the input bytes.
+    ours = P.ours_transmute(background)
+    assert (ours == P.rgba_bytes(background)).all()
+
+
+def test_palette(background, goldens):
+    ours = P.ours_palette(background)
+    assert (ours == P.oracle_palette(background)).all()
+    h = blockhash256(ours.reshape(400, 400, 4))
+    assert min(bin(int(h, 16) ^ int(g, 16)).count("1") for g in goldens["palette"]) <= 8
+
+
+@pytest.mark.parametrize("space", ["oklab", "srlab2"])
+def test_lab_grid(space, goldens):
+    ours = P.ours_lab_grid(space)
+    assert maxdiff(ours, P.oracle_lab_grid(space)) <= LSB
+    assert blockhash256(ours.reshape(400, 400, 4)) in goldens[space]

@@ -1,0 +1,665 @@
+// capi.cpp -- the extern "C" boundary (include/zosimos.h).  Every entry point catches
+// the internal error type and returns a status code; zs_last_error() holds the text.
+#include <cstring>
+#include <exception>
+#include <string>
+
+#include "zs_host.hpp"
+
+namespace zs {
+const std::string &last_error();
+uint32_t cmd_input(Command &c, const Desc &d);
+uint32_t cmd_crop(Command &c, uint32_t src, const zs_rect &r);
+uint32_t cmd_color_convert(Command &c, uint32_t src, const Desc &target);
+uint32_t cmd_chromatic_adaptation(Command &c, uint32_t src, uint32_t method, uint32_t target_wp);
+uint32_t cmd_color_matrix(Command &c, uint32_t src, const float m[9]);
+uint32_t cmd_extract(Command &c, uint32_t src, uint32_t channel);
+uint32_t cmd_inject(Command &c, uint32_t below, uint32_t channel, uint32_t above);
+uint32_t cmd_transmute(Command &c, uint32_t src, const Desc &target);
+uint32_t cmd_inscribe(Command &c, uint32_t below, const zs_rect &rect, uint32_t above, bool placed);
+uint32_t cmd_palette(Command &c, uint32_t palette, int32_t wch, int32_t hch, uint32_t indices);
+uint32_t cmd_bilinear(Command &c, const Desc &d, const float params[24]);
+uint32_t cmd_solid(Command &c, const Desc &d, const float color[4]);
+uint32_t cmd_affine(Command &c, uint32_t below, const float m[9], uint32_t sampling, uint32_t above);
+uint32_t cmd_resize(Command &c, uint32_t src, uint32_t w, uint32_t h, bool filtered, uint32_t filter);
+uint32_t cmd_blend(Command &c, uint32_t below, const zs_rect &rect, uint32_t above, uint32_t mode);
+uint32_t cmd_output(Command &c, uint32_t src, Desc *outformat);
+int batch_thumbnails(Executable *chain, const void *const *images, const uint32_t *widths, const uint32_t *heights,
+                     uint32_t n, uint32_t canvas, void *out, cudaStream_t stream);
+}  // namespace zs
+
+using namespace zs;
+
+struct zs_pool { Pool p; };
+struct zs_cmd { Command c; };
+struct zs_program { Program p; };
+struct zs_executable { std::unique_ptr<Executable> e; cudaStream_t stream = nullptr; ~zs_executable(); };
+struct zs_environment { Environment env; };
+struct zs_execution { Execution x; std::vector<int> kinds; std::vector<int> args; };
+
+zs_executable::~zs_executable() {
+    if (stream) cudaStreamDestroy(stream);
+}
+
+template <class F>
+static int guarded(F &&f) {
+    try {
+        f();
+        return ZS_OK;
+    } catch (const Error &e) {
+        set_last_error(e.msg);
+        return e.code;
+    } catch (const std::bad_alloc &) {
+        set_last_error("out of host memory");
+        return ZS_ERR_OUT_OF_MEMORY;
+    } catch (const std::exception &e) {
+        set_last_error(e.what());
+        return ZS_ERR_OTHER;
+    } catch (...) {
+        set_last_error("unknown error");
+        return ZS_ERR_OTHER;
+    }
+}
+
+#define NEED(ptr)                                                  \
+    do {                                                           \
+        if (!(ptr)) fail(ZS_ERR_INVALID_ARG, #ptr " is null");     \
+    } while (0)
+
+extern "C" {
+
+const char *zs_last_error(void) { return last_error().c_str(); }
+const char *zs_version(void) { return "zosimos-gb300 0.1 (sm_103a)"; }
+
+uint32_t zs_texel_bytes(uint32_t bits) { return texel_bytes(bits); }
+
+int zs_descriptor_srgb_rgba8(uint32_t width, uint32_t height, zs_descriptor *out) {
+    return guarded([&] {
+        NEED(out);
+        std::memset(out, 0, sizeof(*out));
+        out->width = width;
+        out->height = height;
+        out->bits = ZS_BITS_UINT8X4;
+        out->parts = ZS_PARTS_RGBA;
+        out->color = ZS_COLOR_RGB;
+        out->primaries = ZS_PRIMARIES_BT709;
+        out->transfer = ZS_TRANSFER_SRGB;
+        out->whitepoint = ZS_WP_D65;
+    });
+}
+
+int zs_descriptor_is_consistent(const zs_descriptor *desc) { return desc && is_consistent(*desc) ? 1 : 0; }
+uint64_t zs_descriptor_byte_len(const zs_descriptor *desc) { return desc ? host_len(*desc) : 0; }
+
+// ---------------------------------------------------------------- pool
+
+zs_pool *zs_pool_new(void) {
+    try {
+        return new zs_pool();
+    } catch (...) {
+        return nullptr;
+    }
+}
+void zs_pool_free(zs_pool *pool) { delete pool; }
+
+static uint64_t pool_add(Pool &p, const Desc &d) {
+    auto img = std::make_unique<PoolImage>();
+    img->desc = d;
+    img->len = host_len(d);
+    img->ensure_host();
+    uint64_t key = p.next_key++;
+    p.images[key] = std::move(img);
+    return key;
+}
+
+int zs_pool_insert(zs_pool *pool, const zs_descriptor *desc, const void *bytes, uint64_t *key) {
+    return guarded([&] {
+        NEED(pool); NEED(desc); NEED(bytes); NEED(key);
+        if (!is_consistent(*desc)) fail(ZS_ERR_TYPE, "inconsistent descriptor: " + describe(*desc));
+        uint64_t k = pool_add(pool->p, *desc);
+        PoolImage &img = pool->p.get(k);
+        std::memcpy(img.host, bytes, img.len);
+        *key = k;
+    });
+}
+
+int zs_pool_declare(zs_pool *pool, const zs_descriptor *desc, uint64_t *key) {
+    return guarded([&] {
+        NEED(pool); NEED(desc); NEED(key);
+        if (!is_consistent(*desc)) fail(ZS_ERR_TYPE, "inconsistent descriptor: " + describe(*desc));
+        uint64_t k = pool_add(pool->p, *desc);
+        std::memset(pool->p.get(k).host, 0, pool->p.get(k).len);
+        *key = k;
+    });
+}
+
+int zs_pool_descriptor(zs_pool *pool, uint64_t key, zs_descriptor *out) {
+    return guarded([&] {
+        NEED(pool); NEED(out);
+        *out = pool->p.get(key).desc;
+    });
+}
+
+static void pool_sync_host(PoolImage &img) {
+    if (img.host_valid) return;
+    if (!img.dev_valid) fail(ZS_ERR_OTHER, "image has no contents");
+    check_cuda(cudaMemcpy2D(img.host, host_stride(img.desc), img.dev, row_bytes(img.desc), row_bytes(img.desc),
+                            img.desc.height, cudaMemcpyDeviceToHost),
+               "download");
+    img.host_valid = true;
+}
+
+int zs_pool_read(zs_pool *pool, uint64_t key, void *dst, uint64_t len) {
+    return guarded([&] {
+        NEED(pool); NEED(dst);
+        PoolImage &img = pool->p.get(key);
+        if (len != img.len) fail(ZS_ERR_INVALID_ARG, "length mismatch");
+        pool_sync_host(img);
+        std::memcpy(dst, img.host, len);
+    });
+}
+
+int zs_pool_write(zs_pool *pool, uint64_t key, const void *src, uint64_t len) {
+    return guarded([&] {
+        NEED(pool); NEED(src);
+        PoolImage &img = pool->p.get(key);
+        if (len != img.len) fail(ZS_ERR_INVALID_ARG, "length mismatch");
+        std::memcpy(img.host, src, len);
+        img.host_valid = true;
+        img.dev_valid = false;
+    });
+}
+
+int zs_pool_host_ptr(zs_pool *pool, uint64_t key, void **ptr, uint64_t *len) {
+    return guarded([&] {
+        NEED(pool); NEED(ptr);
+        PoolImage &img = pool->p.get(key);
+        pool_sync_host(img);
+        img.dev_valid = false;   // the caller may write through the pointer
+        *ptr = img.host;
+        if (len) *len = img.len;
+    });
+}
+
+int zs_pool_set_descriptor(zs_pool *pool, uint64_t key, const zs_descriptor *desc) {
+    return guarded([&] {
+        NEED(pool); NEED(desc);
+        PoolImage &img = pool->p.get(key);
+        if (!is_consistent(*desc)) fail(ZS_ERR_TYPE, "inconsistent descriptor");
+        if (host_len(*desc) != img.len || desc->width != img.desc.width || desc->height != img.desc.height)
+            fail(ZS_ERR_TYPE, "descriptor must keep the byte layout");
+        img.desc = *desc;
+    });
+}
+
+static void pool_upload(PoolImage &img) {
+    const uint64_t tight = row_bytes(img.desc) * img.desc.height;
+    if (!img.dev) {
+        check_cuda(cudaMalloc(&img.dev, tight), "cudaMalloc");
+        img.dev_len = tight;
+    }
+    if (!img.dev_valid) {
+        check_cuda(cudaMemcpy2D(img.dev, row_bytes(img.desc), img.host, host_stride(img.desc), row_bytes(img.desc),
+                                img.desc.height, cudaMemcpyHostToDevice),
+                   "upload");
+        img.dev_valid = true;
+    }
+}
+
+int zs_pool_upload(zs_pool *pool, uint64_t key) {
+    return guarded([&] {
+        NEED(pool);
+        pool_upload(pool->p.get(key));
+    });
+}
+
+int zs_pool_device_ptr(zs_pool *pool, uint64_t key, void **ptr) {
+    return guarded([&] {
+        NEED(pool); NEED(ptr);
+        PoolImage &img = pool->p.get(key);
+        if (!img.dev_valid) fail(ZS_ERR_OTHER, "image is not device resident (zs_pool_upload)");
+        *ptr = img.dev;
+    });
+}
+
+int zs_pool_remove(zs_pool *pool, uint64_t key) {
+    return guarded([&] {
+        NEED(pool);
+        if (!pool->p.images.erase(key)) fail(ZS_ERR_MISSING_KEY, "no image with this key");
+    });
+}
+
+int zs_pool_clear_cache(zs_pool *pool) {
+    return guarded([&] {
+        NEED(pool);
+        for (auto &kv : pool->p.images) {
+            PoolImage &img = *kv.second;
+            if (img.dev && img.host_valid) {
+                cudaFree(img.dev);
+                img.dev = nullptr;
+                img.dev_valid = false;
+            }
+        }
+    });
+}
+
+// ---------------------------------------------------------------- command buffer
+
+zs_cmd *zs_cmd_new(void) {
+    try {
+        return new zs_cmd();
+    } catch (...) {
+        return nullptr;
+    }
+}
+void zs_cmd_free(zs_cmd *cmd) { delete cmd; }
+
+#define CMD_BODY(expr)                 \
+    return guarded([&] {               \
+        NEED(cmd);                     \
+        NEED(reg);                     \
+        *reg = (expr);                 \
+    })
+
+int zs_cmd_input(zs_cmd *cmd, const zs_descriptor *desc, uint32_t *reg) {
+    return guarded([&] { NEED(cmd); NEED(desc); NEED(reg); *reg = cmd_input(cmd->c, *desc); });
+}
+int zs_cmd_crop(zs_cmd *cmd, uint32_t src, const zs_rect *rect, uint32_t *reg) {
+    return guarded([&] { NEED(cmd); NEED(rect); NEED(reg); *reg = cmd_crop(cmd->c, src, *rect); });
+}
+int zs_cmd_color_convert(zs_cmd *cmd, uint32_t src, const zs_descriptor *target, uint32_t *reg) {
+    return guarded([&] { NEED(cmd); NEED(target); NEED(reg); *reg = cmd_color_convert(cmd->c, src, *target); });
+}
+int zs_cmd_chromatic_adaptation(zs_cmd *cmd, uint32_t src, uint32_t method, uint32_t target_wp, uint32_t *reg) {
+    CMD_BODY(cmd_chromatic_adaptation(cmd->c, src, method, target_wp));
+}
+int zs_cmd_inscribe(zs_cmd *cmd, uint32_t below, const zs_rect *rect, uint32_t above, uint32_t *reg) {
+    return guarded([&] { NEED(cmd); NEED(rect); NEED(reg); *reg = cmd_inscribe(cmd->c, below, *rect, above, false); });
+}
+int zs_cmd_inscribe_placed(zs_cmd *cmd, uint32_t below, const zs_rect *rect, uint32_t above, uint32_t *reg) {
+    return guarded([&] { NEED(cmd); NEED(rect); NEED(reg); *reg = cmd_inscribe(cmd->c, below, *rect, above, true); });
+}
+int zs_cmd_extract(zs_cmd *cmd, uint32_t src, uint32_t channel, uint32_t *reg) {
+    CMD_BODY(cmd_extract(cmd->c, src, channel));
+}
+int zs_cmd_inject(zs_cmd *cmd, uint32_t below, uint32_t channel, uint32_t above, uint32_t *reg) {
+    CMD_BODY(cmd_inject(cmd->c, below, channel, above));
+}
+int zs_cmd_transmute(zs_cmd *cmd, uint32_t src, const zs_descriptor *target, uint32_t *reg) {
+    return guarded([&] { NEED(cmd); NEED(target); NEED(reg); *reg = cmd_transmute(cmd->c, src, *target); });
+}
+int zs_cmd_palette(zs_cmd *cmd, uint32_t palette, int32_t wch, int32_t hch, uint32_t indices, uint32_t *reg) {
+    CMD_BODY(cmd_palette(cmd->c, palette, wch, hch, indices));
+}
+int zs_cmd_bilinear(zs_cmd *cmd, const zs_descriptor *desc, const float params[24], uint32_t *reg) {
+    return guarded([&] { NEED(cmd); NEED(desc); NEED(params); NEED(reg); *reg = cmd_bilinear(cmd->c, *desc, params); });
+}
+int zs_cmd_solid_rgba(zs_cmd *cmd, const zs_descriptor *desc, const float color[4], uint32_t *reg) {
+    return guarded([&] { NEED(cmd); NEED(desc); NEED(color); NEED(reg); *reg = cmd_solid(cmd->c, *desc, color); });
+}
+int zs_cmd_affine(zs_cmd *cmd, uint32_t below, const float matrix[9], uint32_t sampling, uint32_t above,
+                  uint32_t *reg) {
+    return guarded([&] {
+        NEED(cmd); NEED(matrix); NEED(reg);
+        *reg = cmd_affine(cmd->c, below, matrix, sampling, above);
+    });
+}
+int zs_cmd_resize(zs_cmd *cmd, uint32_t src, uint32_t width, uint32_t height, uint32_t *reg) {
+    CMD_BODY(cmd_resize(cmd->c, src, width, height, false, 0));
+}
+int zs_cmd_resize_filtered(zs_cmd *cmd, uint32_t src, uint32_t width, uint32_t height, uint32_t filter,
+                           uint32_t *reg) {
+    CMD_BODY(cmd_resize(cmd->c, src, width, height, true, filter));
+}
+int zs_cmd_blend(zs_cmd *cmd, uint32_t below, const zs_rect *rect, uint32_t above, uint32_t mode, uint32_t *reg) {
+    return guarded([&] { NEED(cmd); NEED(rect); NEED(reg); *reg = cmd_blend(cmd->c, below, *rect, above, mode); });
+}
+int zs_cmd_color_matrix(zs_cmd *cmd, uint32_t src, const float matrix[9], uint32_t *reg) {
+    return guarded([&] { NEED(cmd); NEED(matrix); NEED(reg); *reg = cmd_color_matrix(cmd->c, src, matrix); });
+}
+int zs_cmd_output(zs_cmd *cmd, uint32_t src, uint32_t *reg, zs_descriptor *outformat) {
+    return guarded([&] { NEED(cmd); NEED(reg); *reg = cmd_output(cmd->c, src, outformat); });
+}
+int zs_cmd_describe(const zs_cmd *cmd, uint32_t reg, zs_descriptor *out) {
+    return guarded([&] { NEED(cmd); NEED(out); *out = cmd->c.describe(reg); });
+}
+
+// ---------------------------------------------------------------- compile / lower
+
+int zs_compile(const zs_cmd *cmd, zs_program **out) {
+    return guarded([&] {
+        NEED(cmd); NEED(out);
+        auto prog = std::make_unique<zs_program>();
+        Program &p = prog->p;
+        p.ops = cmd->c.ops;
+        p.uses.assign(p.ops.size(), 0);
+        for (uint32_t r = 0; r < p.ops.size(); ++r) {
+            const Op &op = p.ops[r];
+            switch (op.kind) {
+            case OpKind::Input: p.inputs.push_back(r); break;
+            case OpKind::Output:
+                p.outputs.push_back(op.a);
+                p.output_regs.push_back(r);
+                p.uses[op.a]++;
+                break;
+            case OpKind::Bilinear:
+            case OpKind::Solid: break;
+            case OpKind::Inject:
+            case OpKind::Inscribe:
+            case OpKind::InscribePlaced:
+            case OpKind::Palette:
+            case OpKind::Affine:
+            case OpKind::Blend:
+                p.uses[op.a]++;
+                p.uses[op.b]++;
+                break;
+            default: p.uses[op.a]++; break;
+            }
+        }
+        if (p.output_regs.empty()) fail(ZS_ERR_OTHER, "program has no output");
+        *out = prog.release();
+    });
+}
+void zs_program_free(zs_program *program) { delete program; }
+
+int zs_lower(const zs_program *program, const zs_capabilities *caps, zs_executable **out) {
+    return guarded([&] {
+        NEED(program); NEED(out);
+        zs_capabilities c{};
+        if (caps) c = *caps;
+        auto exe = std::make_unique<zs_executable>();
+        exe->e = lower(program->p, c);
+        *out = exe.release();
+    });
+}
+void zs_executable_free(zs_executable *exe) { delete exe; }
+
+int zs_executable_kernel_count(const zs_executable *exe, uint32_t *count) {
+    return guarded([&] {
+        NEED(exe); NEED(count);
+        uint32_t n = 0;
+        for (const Step &s : exe->e->steps)
+            if (s.kind != StepKind::Copy) ++n;
+        *count = n;
+    });
+}
+
+const char *zs_executable_describe(const zs_executable *exe) { return exe ? exe->e->plan_text.c_str() : ""; }
+
+// ---------------------------------------------------------------- environment / execution
+
+int zs_env_new(zs_executable *exe, zs_pool *pool, zs_environment **out) {
+    return guarded([&] {
+        NEED(exe); NEED(pool); NEED(out);
+        auto env = std::make_unique<zs_environment>();
+        env->env.exe = exe->e.get();
+        env->env.pool = &pool->p;
+        *out = env.release();
+    });
+}
+void zs_env_free(zs_environment *env) { delete env; }
+
+static bool desc_matches(const Desc &a, const Desc &b) {
+    return a.width == b.width && a.height == b.height && same_chroma(a, b);
+}
+
+int zs_env_bind(zs_environment *env, uint32_t reg, uint64_t key) {
+    return guarded([&] {
+        NEED(env);
+        Executable &E = *env->env.exe;
+        size_t i = 0;
+        for (; i < E.input_regs.size(); ++i)
+            if (E.input_regs[i] == reg) break;
+        if (i == E.input_regs.size()) fail(ZS_ERR_BAD_REGISTER, "register is not an input");
+        PoolImage &img = env->env.pool->get(key);
+        if (!desc_matches(img.desc, E.input_desc[i]))
+            fail(ZS_ERR_MISMATCHED_DESCRIPTOR, "bound image " + describe(img.desc) + " does not match input " +
+                                                   describe(E.input_desc[i]));
+        env->env.binds[reg] = key;
+    });
+}
+
+int zs_env_bind_output(zs_environment *env, uint32_t reg, uint64_t key) {
+    return guarded([&] {
+        NEED(env);
+        Executable &E = *env->env.exe;
+        size_t i = 0;
+        for (; i < E.output_regs.size(); ++i)
+            if (E.output_regs[i] == reg) break;
+        if (i == E.output_regs.size()) fail(ZS_ERR_BAD_REGISTER, "register is not an output");
+        PoolImage &img = env->env.pool->get(key);
+        if (!desc_matches(img.desc, E.output_desc[i])) fail(ZS_ERR_MISMATCHED_DESCRIPTOR, "output image mismatch");
+        env->env.output_binds[reg] = key;
+    });
+}
+
+// Instruction encoding of an execution: kind 0 = upload input i, kind 1 = run step i.
+int zs_launch(zs_executable *exe, zs_environment *env, zs_execution **out) {
+    std::unique_ptr<zs_environment> guard(env);
+    return guarded([&] {
+        NEED(exe); NEED(env); NEED(out);
+        Executable &E = *exe->e;
+        if (env->env.exe != &E) fail(ZS_ERR_INVALID_ARG, "environment belongs to another executable");
+        E.ensure_buffers();
+        auto x = std::make_unique<zs_execution>();
+        Execution &X = x->x;
+        X.exe = &E;
+        X.pool = env->env.pool;
+        X.output_binds = env->env.output_binds;
+        check_cuda(cudaStreamCreateWithFlags(&X.stream, cudaStreamNonBlocking), "stream");
+        X.ptrs = E.dev_buffers;
+        for (size_t i = 0; i < E.input_regs.size(); ++i) {
+            auto it = env->env.binds.find(E.input_regs[i]);
+            if (it == env->env.binds.end()) fail(ZS_ERR_MISSING_KEY, "input register is not bound");
+            PoolImage &img = X.pool->get(it->second);
+            X.input_keys.push_back(it->second);
+            if (img.dev_valid) {
+                X.ptrs[E.input_slot[i]] = img.dev;     // device resident: no copy
+            } else {
+                x->kinds.push_back(0);
+                x->args.push_back((int)i);
+            }
+        }
+        for (size_t s = 0; s < E.steps.size(); ++s) {
+            x->kinds.push_back(1);
+            x->args.push_back((int)s);
+        }
+        X.total = x->kinds.size();
+        *out = x.release();
+    });
+}
+
+int zs_exec_is_running(const zs_execution *exec) { return exec && exec->x.cursor < exec->x.total ? 1 : 0; }
+
+int zs_exec_step(zs_execution *exec) {
+    return guarded([&] {
+        NEED(exec);
+        Execution &X = exec->x;
+        if (X.cursor >= X.total) fail(ZS_ERR_STEP_LIMIT, "execution has no more instructions");
+        const int kind = exec->kinds[X.cursor], arg = exec->args[X.cursor];
+        Executable &E = *X.exe;
+        if (kind == 0) {
+            PoolImage &img = X.pool->get(X.input_keys[arg]);
+            const int slot = E.input_slot[arg];
+            check_cuda(cudaMemcpy2DAsync(X.ptrs[slot], row_bytes(img.desc), img.host, host_stride(img.desc),
+                                         row_bytes(img.desc), img.desc.height, cudaMemcpyHostToDevice, X.stream),
+                       "input upload");
+        } else {
+            E.record_range(X.stream, X.ptrs, (size_t)arg, (size_t)arg + 1);
+        }
+        X.cursor++;
+    });
+}
+
+int zs_exec_sync(zs_execution *exec) {
+    return guarded([&] {
+        NEED(exec);
+        check_cuda(cudaStreamSynchronize(exec->x.stream), "synchronize");
+    });
+}
+
+int zs_retire_output(zs_execution *exec, uint32_t reg, uint64_t *key) {
+    return guarded([&] {
+        NEED(exec); NEED(key);
+        Execution &X = exec->x;
+        Executable &E = *X.exe;
+        while (X.cursor < X.total) {
+            int rc = zs_exec_step(exec);
+            if (rc != ZS_OK) fail(rc, last_error());
+        }
+        size_t i = 0;
+        for (; i < E.output_regs.size(); ++i)
+            if (E.output_regs[i] == reg) break;
+        if (i == E.output_regs.size()) fail(ZS_ERR_BAD_REGISTER, "register is not an output");
+        check_cuda(cudaStreamSynchronize(X.stream), "synchronize");
+        const Desc &d = E.output_desc[i];
+        uint64_t k;
+        auto bound = X.output_binds.find(reg);
+        if (bound != X.output_binds.end()) {
+            k = bound->second;
+        } else {
+            k = pool_add(*X.pool, d);
+        }
+        PoolImage &img = X.pool->get(k);
+        const int slot = E.output_slot[i];
+        check_cuda(cudaMemcpy2D(img.host, host_stride(img.desc), X.ptrs[slot], row_bytes(d), row_bytes(d), d.height,
+                                cudaMemcpyDeviceToHost),
+                   "output download");
+        img.host_valid = true;
+        img.dev_valid = false;
+        *key = k;
+    });
+}
+
+void zs_exec_free(zs_execution *exec) { delete exec; }
+
+// ---------------------------------------------------------------- one-call paths
+
+static cudaStream_t exe_stream(zs_executable *exe) {
+    if (!exe->stream) check_cuda(cudaStreamCreateWithFlags(&exe->stream, cudaStreamNonBlocking), "stream");
+    return exe->stream;
+}
+
+int zs_run_host(zs_executable *exe, const void *const *inputs, uint32_t n_inputs, void *const *outputs,
+                uint32_t n_outputs) {
+    return guarded([&] {
+        NEED(exe);
+        Executable &E = *exe->e;
+        if (n_inputs != E.input_regs.size() || n_outputs != E.output_regs.size())
+            fail(ZS_ERR_INVALID_ARG, "wrong number of inputs or outputs");
+        E.ensure_buffers();
+        cudaStream_t s = exe_stream(exe);
+        std::vector<void *> ptrs = E.dev_buffers;
+        for (uint32_t i = 0; i < n_inputs; ++i) {
+            NEED(inputs[i]);
+            const Slot &sl = E.slots[E.input_slot[i]];
+            check_cuda(cudaMemcpyAsync(ptrs[E.input_slot[i]], inputs[i], sl.bytes, cudaMemcpyHostToDevice, s), "h2d");
+        }
+        E.record(s, ptrs);
+        for (uint32_t j = 0; j < n_outputs; ++j) {
+            NEED(outputs[j]);
+            const Slot &sl = E.slots[E.output_slot[j]];
+            check_cuda(cudaMemcpyAsync(outputs[j], ptrs[E.output_slot[j]], sl.bytes, cudaMemcpyDeviceToHost, s), "d2h");
+        }
+        check_cuda(cudaStreamSynchronize(s), "synchronize");
+    });
+}
+
+int zs_run_device(zs_executable *exe, const void *const *inputs, uint32_t n_inputs, void *const *outputs,
+                  uint32_t n_outputs, void *stream) {
+    return guarded([&] {
+        NEED(exe);
+        Executable &E = *exe->e;
+        if (n_inputs != E.input_regs.size() || n_outputs != E.output_regs.size())
+            fail(ZS_ERR_INVALID_ARG, "wrong number of inputs or outputs");
+        E.ensure_buffers();
+        cudaStream_t s = stream ? (cudaStream_t)stream : exe_stream(exe);
+        std::vector<void *> ptrs = E.dev_buffers;
+        for (uint32_t i = 0; i < n_inputs; ++i) {
+            NEED(inputs[i]);
+            ptrs[E.input_slot[i]] = const_cast<void *>(inputs[i]);
+        }
+        for (uint32_t j = 0; j < n_outputs; ++j) {
+            NEED(outputs[j]);
+            ptrs[E.output_slot[j]] = outputs[j];
+        }
+        if (!E.use_graph) {
+            E.record(s, ptrs);
+            return;
+        }
+        auto it = E.graphs.find(ptrs);
+        if (it == E.graphs.end()) {
+            if (E.graphs.size() >= 16) {          // bounded cache of instantiated graphs
+                auto victim = E.graphs.find(E.graph_order.front());
+                if (victim != E.graphs.end()) {
+                    cudaGraphExecDestroy(victim->second);
+                    E.graphs.erase(victim);
+                }
+                E.graph_order.erase(E.graph_order.begin());
+            }
+            cudaGraph_t g = nullptr;
+            check_cuda(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+            try {
+                E.record(s, ptrs);
+            } catch (...) {
+                cudaStreamEndCapture(s, &g);
+                if (g) cudaGraphDestroy(g);
+                throw;
+            }
+            check_cuda(cudaStreamEndCapture(s, &g), "end capture");
+            cudaGraphExec_t ge = nullptr;
+            cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+            cudaGraphDestroy(g);
+            check_cuda(e, "graph instantiate");
+            it = E.graphs.emplace(ptrs, ge).first;
+            E.graph_order.push_back(ptrs);
+        }
+        check_cuda(cudaGraphLaunch(it->second, s), "graph launch");
+    });
+}
+
+void *zs_host_alloc(uint64_t bytes) {
+    void *p = nullptr;
+    if (cudaMallocHost(&p, bytes ? bytes : 1) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+void zs_host_free(void *ptr) {
+    if (ptr) cudaFreeHost(ptr);
+}
+void *zs_device_alloc(uint64_t bytes) {
+    void *p = nullptr;
+    if (cudaMalloc(&p, bytes ? bytes : 1) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return p;
+}
+void zs_device_free(void *ptr) {
+    if (ptr) cudaFree(ptr);
+}
+int zs_memcpy_h2d(void *dst, const void *src, uint64_t bytes) {
+    return guarded([&] { check_cuda(cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice), "h2d"); });
+}
+int zs_memcpy_d2h(void *dst, const void *src, uint64_t bytes) {
+    return guarded([&] { check_cuda(cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost), "d2h"); });
+}
+int zs_device_synchronize(void) {
+    return guarded([&] { check_cuda(cudaDeviceSynchronize(), "synchronize"); });
+}
+
+int zs_batch_thumbnails(zs_executable *chain, const void *const *images, const uint32_t *widths,
+                        const uint32_t *heights, uint32_t n, uint32_t canvas, void *out, void *stream) {
+    return guarded([&] {
+        NEED(chain); NEED(images); NEED(widths); NEED(heights); NEED(out);
+        cudaStream_t s = stream ? (cudaStream_t)stream : exe_stream(chain);
+        int rc = batch_thumbnails(chain->e.get(), images, widths, heights, n, canvas, out, s);
+        if (rc != ZS_OK) fail(rc, last_error());
+    });
+}
+
+uint64_t zs_kernel_launch_count(void) { return kernel_launch_count(); }
+
+}  // extern "C"

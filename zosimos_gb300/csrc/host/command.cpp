@@ -1,0 +1,309 @@
+// command.cpp -- CommandBuffer: the SSA op builder with the reference's type checks
+// (lib/zosimos/src/command.rs:739-1765) and the per-pixel semantics of each colour op
+// expressed as a host pixel program (matrices kept in FP64 until lowering).
+#include <cmath>
+#include <cstring>
+
+#include "zs_host.hpp"
+
+namespace zs {
+
+uint32_t Command::push(Op op) {
+    ops.push_back(std::move(op));
+    return (uint32_t)ops.size() - 1;
+}
+
+bool Command::is_value(uint32_t reg) const { return reg < ops.size() && ops[reg].kind != OpKind::Output; }
+
+const Desc &Command::describe(uint32_t reg) const {
+    if (!is_value(reg)) fail(ZS_ERR_BAD_REGISTER, "register does not name an image value");
+    return ops[reg].desc;
+}
+
+static Desc with_size(Desc d, uint32_t w, uint32_t h) {
+    d.width = w;
+    d.height = h;
+    d.row_stride = 0;
+    return d;
+}
+
+// ---------------------------------------------------------------- colour semantics
+
+// ColorConversion (command.rs:1009-1085 and :3220-3277).  The RGB->RGB case uses
+// inv(dst.to_xyz) * src.to_xyz; the reference composes dst.to_xyz * inv(src.to_xyz)
+// (command.rs:1022-1025, 3227-3228), which agrees whenever the primaries are equal.
+static HProgram color_convert_program(const Desc &src, const Desc &dst) {
+    HProgram p;
+    const uint32_t sk = src.color, dk = dst.color;
+    if (sk == ZS_COLOR_RGB && dk == ZS_COLOR_RGB) {
+        if (src.whitepoint != dst.whitepoint) fail(ZS_ERR_TYPE, "color_convert between RGB spaces needs the same whitepoint");
+        p.mat(rgb_to_xyz(dst.primaries, dst.whitepoint).inverse() * rgb_to_xyz(src.primaries, src.whitepoint));
+    } else if (sk == ZS_COLOR_RGB && dk == ZS_COLOR_OKLAB) {
+        p.mat(kOklabM1 * rgb_to_xyz(src.primaries, src.whitepoint));   // oklab.frag:34-47
+        p.op(ZS_P_CBRT);
+        p.mat(kOklabM2);
+    } else if (sk == ZS_COLOR_OKLAB && dk == ZS_COLOR_RGB) {
+        p.mat(kOklabM2.inverse());                                       // oklab.frag:50-64
+        p.op(ZS_P_CUBE);
+        p.mat(rgb_to_xyz(dst.primaries, dst.whitepoint).inverse() * kOklabM1.inverse());
+        p.op(ZS_P_CLAMP01);
+    } else if (sk == ZS_COLOR_RGB && dk == ZS_COLOR_SRLAB2) {
+        // srlab2.frag:36-59: lms = HPE * inv(CAT02) * (CAT02 * xyz) = HPE * xyz.
+        p.mat(kHpe * rgb_to_xyz(src.primaries, src.whitepoint));
+        p.op(ZS_P_SRL_NL);
+        p.mat(kHpe.inverse());
+        p.op(ZS_P_SRL_ENC_DIFF);
+    } else if (sk == ZS_COLOR_SRLAB2 && dk == ZS_COLOR_RGB) {
+        // srlab2.frag:62-85 with the whitepoint of the SrLab2 colour.
+        double w[3];
+        whitepoint_xyz(src.whitepoint, w);
+        double wr[3];
+        for (int i = 0; i < 3; ++i) wr[i] = kCat02.m[3 * i] * w[0] + kCat02.m[3 * i + 1] * w[1] + kCat02.m[3 * i + 2] * w[2];
+        p.op(ZS_P_SRL_DEC_DIFF);
+        p.mat(kHpe);
+        p.op(ZS_P_SRL_NLINV);
+        Mat3 tail = rgb_to_xyz(dst.primaries, dst.whitepoint).inverse() * kCat02.inverse() *
+                    Mat3::diag(wr[0], wr[1], wr[2]) * kCat02 * kHpe.inverse();
+        p.mat(tail);
+        p.op(ZS_P_CLAMP01);
+    } else {
+        fail(ZS_ERR_TYPE, "no conversion between these colours");
+    }
+    return p;
+}
+
+}  // namespace zs
+
+using namespace zs;
+
+// The C ABI command-building entry points live here so that they share the checks.
+namespace zs {
+
+uint32_t cmd_input(Command &c, const Desc &d) {
+    if (!is_consistent(d)) fail(ZS_ERR_TYPE, "inconsistent input declared: " + describe(d));
+    Op op{OpKind::Input};
+    op.desc = d;
+    return c.push(op);
+}
+
+uint32_t cmd_crop(Command &c, uint32_t src, const zs_rect &r) {
+    // command.rs:912-919: the result keeps the source descriptor; the linker paints the
+    // selection over the whole target (command.rs:2507-2526).
+    Op op{OpKind::Crop};
+    op.a = src;
+    op.desc = c.describe(src);
+    op.rect = r;
+    if (r.max_x <= r.x || r.max_y <= r.y) fail(ZS_ERR_OTHER, "empty crop");
+    return c.push(op);
+}
+
+uint32_t cmd_color_convert(Command &c, uint32_t src, const Desc &target) {
+    const Desc s = c.describe(src);
+    Desc d = target;
+    d.width = s.width;
+    d.height = s.height;
+    d.row_stride = 0;
+    if (!is_consistent(d)) fail(ZS_ERR_TYPE, "inconsistent conversion target: " + describe(d));
+    Op op{OpKind::ColorConvert};
+    op.a = src;
+    op.desc = d;
+    op.prog = color_convert_program(s, d);
+    return c.push(op);
+}
+
+uint32_t cmd_chromatic_adaptation(Command &c, uint32_t src, uint32_t method, uint32_t target_wp) {
+    const Desc s = c.describe(src);
+    if (s.color != ZS_COLOR_RGB) fail(ZS_ERR_TYPE, "non-rgb chromatic adaptation");
+    if (target_wp > ZS_WP_F11) fail(ZS_ERR_INVALID_ARG, "bad whitepoint");
+    Mat3 adapt;
+    if (!adaptation_matrix(method, s.whitepoint, target_wp, adapt))
+        fail(ZS_ERR_UNIMPLEMENTED, "chromatic adaptation method not implemented");
+    Op op{OpKind::ChromaticAdaptation};
+    op.a = src;
+    op.desc = s;
+    op.desc.whitepoint = target_wp;
+    op.desc.row_stride = 0;
+    // command.rs:2527-2531: from_xyz(target) * adapt * to_xyz(source)
+    op.prog.mat(rgb_to_xyz(s.primaries, target_wp).inverse() * adapt * rgb_to_xyz(s.primaries, s.whitepoint));
+    op.u0 = method;
+    return c.push(op);
+}
+
+uint32_t cmd_color_matrix(Command &c, uint32_t src, const float m[9]) {
+    Op op{OpKind::ColorMatrix};
+    op.a = src;
+    op.desc = c.describe(src);
+    op.desc.row_stride = 0;
+    Mat3 mm{};
+    for (int i = 0; i < 9; ++i) mm.m[i] = m[i];
+    op.prog.mat(mm);
+    return c.push(op);
+}
+
+static int channel_index(uint32_t ch) { return ch <= 3 ? (int)ch : -1; }
+
+uint32_t cmd_extract(Command &c, uint32_t src, uint32_t channel) {
+    const Desc s = c.describe(src);
+    if (channel > 3) fail(ZS_ERR_OTHER, "unsupported channel");
+    // command.rs:1221-1268: Texel::channel_texel keeps the bits and selects the part.
+    if (channel_count_parts(s.parts) < 3 && !(s.parts == ZS_PARTS_LUMAA && channel == 3))
+        fail(ZS_ERR_OTHER, "channel not present in texel");
+    static const uint32_t parts[4] = {ZS_PARTS_R, ZS_PARTS_G, ZS_PARTS_B, ZS_PARTS_A};
+    Op op{OpKind::Extract};
+    op.a = src;
+    op.desc = s;
+    op.desc.parts = parts[channel];
+    op.desc.row_stride = 0;
+    op.u0 = channel;
+    return c.push(op);
+}
+
+uint32_t cmd_inject(Command &c, uint32_t below, uint32_t channel, uint32_t above) {
+    const Desc b = c.describe(below), a = c.describe(above);
+    if (channel > 2) fail(ZS_ERR_OTHER, "inject supports R, G, B");      // ChannelPosition::new
+    if (b.width != a.width || b.height != a.height) fail(ZS_ERR_TYPE, "inject operands differ in size");
+    if (channel_count_parts(a.parts) != 1) fail(ZS_ERR_TYPE, "inject needs a single-channel operand");
+    Op op{OpKind::Inject};
+    op.a = below;
+    op.b = above;
+    op.desc = b;
+    op.desc.row_stride = 0;
+    HInstr i;
+    i.op = ZS_P_INJECT;
+    i.v[channel_index(channel)] = 1.0;                 // select
+    int w = a.parts == ZS_PARTS_R ? 0 : a.parts == ZS_PARTS_G ? 1 : a.parts == ZS_PARTS_B ? 2 :
+            a.parts == ZS_PARTS_A ? 3 : 0;             // channel_weight_vec4 (buffer.rs)
+    i.v[4 + w] = 1.0;
+    op.prog.ins.push_back(i);
+    return c.push(op);
+}
+
+uint32_t cmd_transmute(Command &c, uint32_t src, const Desc &target) {
+    const Desc s = c.describe(src);
+    Desc d = target;
+    if (d.width != s.width || d.height != s.height) fail(ZS_ERR_TYPE, "invalid transmute with mismatched size");
+    if (texel_bytes(d.bits) != texel_bytes(s.bits)) fail(ZS_ERR_TYPE, "transmute needs texels of equal size");
+    d.row_stride = 0;
+    if (!is_consistent(d)) fail(ZS_ERR_TYPE, "invalid transmute with inconsistent result");
+    Op op{OpKind::Transmute};
+    op.a = src;
+    op.desc = d;
+    return c.push(op);
+}
+
+static void check_inside(const Desc &below, const zs_rect &r) {
+    if (r.x > r.max_x || r.y > r.max_y || r.max_x > below.width || r.max_y > below.height)
+        fail(ZS_ERR_OTHER, "placement outside of the image");
+}
+
+uint32_t cmd_inscribe(Command &c, uint32_t below, const zs_rect &rect, uint32_t above, bool placed) {
+    const Desc b = c.describe(below), a = c.describe(above);
+    if (!same_chroma(a, b)) fail(ZS_ERR_TYPE, "inscribe needs equal texel and colour");
+    if (!placed) {
+        // command.rs:1196-1198: the placement must equal the upper image's rectangle.
+        if (!(rect.x == 0 && rect.y == 0 && rect.max_x == a.width && rect.max_y == a.height))
+            fail(ZS_ERR_OTHER, "inscribe placement must be the upper image's rectangle");
+    } else if (rect.max_x - rect.x != a.width || rect.max_y - rect.y != a.height) {
+        fail(ZS_ERR_OTHER, "placement size must equal the upper image size");
+    }
+    check_inside(b, rect);
+    Op op{placed ? OpKind::InscribePlaced : OpKind::Inscribe};
+    op.a = below;
+    op.b = above;
+    op.desc = b;
+    op.desc.row_stride = 0;
+    op.rect = rect;
+    if (!placed) {
+        // Rectangle::normalize (command.rs:3536-3543) sets max_y = y + width.
+        op.rect.max_y = rect.y + (rect.max_x > rect.x ? rect.max_x - rect.x : 0);
+    }
+    return c.push(op);
+}
+
+uint32_t cmd_palette(Command &c, uint32_t palette, int32_t wch, int32_t hch, uint32_t indices) {
+    const Desc lhs = c.describe(palette), rhs = c.describe(indices);
+    if (wch > 2 || hch > 2) fail(ZS_ERR_TYPE, "palette coordinate channel must be R, G or B");
+    Op op{OpKind::Palette};
+    op.a = palette;
+    op.b = indices;
+    op.desc = with_size(lhs, rhs.width, rhs.height);   // command.rs:1468-1472
+    op.i0 = wch;
+    op.i1 = hch;
+    if (wch >= 0) op.fparams[wch] = 1.0f;
+    if (hch >= 0) op.fparams[4 + hch] = 1.0f;
+    return c.push(op);
+}
+
+uint32_t cmd_bilinear(Command &c, const Desc &d, const float params[24]) {
+    if (!is_consistent(d)) fail(ZS_ERR_TYPE, "inconsistent descriptor for bilinear");
+    Op op{OpKind::Bilinear};
+    op.desc = d;
+    op.desc.row_stride = 0;
+    std::memcpy(op.fparams, params, sizeof(float) * 24);
+    return c.push(op);
+}
+
+uint32_t cmd_solid(Command &c, const Desc &d, const float color[4]) {
+    if (!is_consistent(d)) fail(ZS_ERR_TYPE, "inconsistent constant color image created");
+    Op op{OpKind::Solid};
+    op.desc = d;
+    op.desc.row_stride = 0;
+    std::memcpy(op.fparams, color, sizeof(float) * 4);
+    return c.push(op);
+}
+
+uint32_t cmd_affine(Command &c, uint32_t below, const float m[9], uint32_t sampling, uint32_t above) {
+    const Desc b = c.describe(below), a = c.describe(above);
+    if (!same_chroma(a, b)) fail(ZS_ERR_TYPE, "affine needs equal texel and colour");
+    // command.rs:1648-1656: |det| must be at least f32::EPSILON.
+    double det = (double)m[0] * ((double)m[4] * m[8] - (double)m[5] * m[7]) -
+                 (double)m[1] * ((double)m[3] * m[8] - (double)m[5] * m[6]) +
+                 (double)m[2] * ((double)m[3] * m[7] - (double)m[4] * m[6]);
+    if (!(std::fabs(det) >= 1.1920929e-07)) fail(ZS_ERR_OTHER, "degenerate affine transformation");
+    if (sampling > 1) fail(ZS_ERR_INVALID_ARG, "unknown affine sampling");
+    Op op{OpKind::Affine};
+    op.a = below;
+    op.b = above;
+    op.desc = b;
+    op.desc.row_stride = 0;
+    std::memcpy(op.fparams, m, sizeof(float) * 9);
+    op.u0 = sampling;
+    return c.push(op);
+}
+
+uint32_t cmd_resize(Command &c, uint32_t src, uint32_t w, uint32_t h, bool filtered, uint32_t filter) {
+    const Desc s = c.describe(src);
+    if (w == 0 || h == 0) fail(ZS_ERR_OTHER, "empty resize");
+    if (filtered && filter > 2) fail(ZS_ERR_INVALID_ARG, "unknown resize filter");
+    Op op{filtered ? OpKind::ResizeFiltered : OpKind::Resize};
+    op.a = src;
+    op.desc = with_size(s, w, h);
+    op.u0 = filter;
+    return c.push(op);
+}
+
+uint32_t cmd_blend(Command &c, uint32_t below, const zs_rect &rect, uint32_t above, uint32_t mode) {
+    const Desc b = c.describe(below), a = c.describe(above);
+    if (!same_chroma(a, b)) fail(ZS_ERR_TYPE, "blend needs equal texel and colour");
+    if (mode > 3) fail(ZS_ERR_INVALID_ARG, "unknown blend mode");
+    Op op{OpKind::Blend};
+    op.a = below;
+    op.b = above;
+    op.desc = b;
+    op.desc.row_stride = 0;
+    op.rect = rect;
+    op.u0 = mode;
+    return c.push(op);
+}
+
+uint32_t cmd_output(Command &c, uint32_t src, Desc *outformat) {
+    const Desc s = c.describe(src);
+    Op op{OpKind::Output};
+    op.a = src;
+    op.desc = s;
+    op.desc.row_stride = 0;
+    if (outformat) *outformat = op.desc;
+    return c.push(op);
+}
+
+}  // namespace zs

@@ -1,0 +1,605 @@
+// lower.cpp -- Program::lower_to for CUDA (the analogue of program.rs:1304-1651 and the
+// Encoder of program/encoder.rs): turns the SSA op list into raster launches.
+//
+// The reference emits, per op, one render pass plus a staging encode pass after it and
+// a decode pass before the next op (program.rs:1486-1533).  Here each register is
+// either *materialised* (a device buffer in a storage format) or *pending* (a launch
+// under construction: producer + fused pixel program).  Per-pixel colour ops extend
+// the pending program of their operand, so a chain of them becomes one HBM pass; a
+// gather/construct/blend/resample op starts a new launch whose sources are
+// materialised.  Lossy declared intermediate texels are honoured by quantising in
+// registers (QUANT), so results equal the per-op semantics without the round trips.
+//
+// Modes: FUSED (default; FP32 intermediates that must be materialised are stored as
+// FP16), PER_OP_F32 / PER_OP_F16 (one launch per op, linear RGBA intermediates: the
+// plain baseline the fused executor is measured against).
+#include <cmath>
+#include <cstring>
+#include <sstream>
+
+#include "zs_host.hpp"
+
+namespace zs {
+
+struct Pending {
+    ZsRasterArgs a;
+    int src_slot[ZS_MAX_SRCS] = {-1, -1, -1};
+    int idx_x_slot = -1, idx_y_slot = -1, weight_slot = -1;
+    HProgram prog;
+    std::string label;
+};
+
+struct Val {
+    bool materialized = false;
+    int slot = -1;
+    ZsFormat fmt{};
+    std::unique_ptr<Pending> pend;
+};
+
+struct Planner {
+    const Program &P;
+    Executable &E;
+    std::vector<Val> vals;
+    std::vector<int> out_slot_of;     // value register -> output slot (or -1)
+    std::vector<uint32_t> remaining;  // remaining uses
+
+    Planner(const Program &p, Executable &e) : P(p), E(e) {}
+
+    const Desc &desc(uint32_t r) const { return P.ops[r].desc; }
+
+    int new_slot(SlotKind k, int w, int h, const ZsFormat &f, uint32_t reg = 0) {
+        Slot s;
+        s.kind = k;
+        s.width = w;
+        s.height = h;
+        s.fmt = f;
+        s.stride = (int64_t)w * f.bpp;
+        s.bytes = (uint64_t)s.stride * h;
+        s.reg = reg;
+        E.slots.push_back(std::move(s));
+        return (int)E.slots.size() - 1;
+    }
+
+    int table_slot(const void *data, size_t bytes) {
+        Slot s;
+        s.kind = SlotKind::Table;
+        s.bytes = bytes;
+        s.table.assign((const uint8_t *)data, (const uint8_t *)data + bytes);
+        E.slots.push_back(std::move(s));
+        return (int)E.slots.size() - 1;
+    }
+
+    ZsFormat storage_format(uint32_t reg) const {
+        ZsFormat declared = format_of(desc(reg));
+        if (E.mode == ZS_MODE_PER_OP_F32) return linear_f32_format();
+        if (E.mode == ZS_MODE_PER_OP_F16) return linear_f16_format();
+        if (declared.fast == ZS_FAST_F32X4) return linear_f16_format();   // FP16 storage
+        return declared;
+    }
+
+    std::unique_ptr<Pending> new_pending(uint8_t producer, int w, int h, const std::string &label) {
+        auto p = std::make_unique<Pending>();
+        std::memset(&p->a, 0, sizeof(p->a));
+        p->a.producer = producer;
+        p->a.width = w;
+        p->a.height = h;
+        p->label = label;
+        return p;
+    }
+
+    void set_src(Pending &p, int i, uint32_t reg) {
+        Val &v = vals[reg];
+        set_src_slot(p, i, v.slot);
+        p.a.src[i].fmt = v.fmt;
+    }
+
+    void set_src_slot(Pending &p, int i, int slot) {
+        p.src_slot[i] = slot;
+        Slot &s = E.slots[slot];
+        p.a.src[i].fmt = s.fmt;
+        p.a.src[i].width = s.width;
+        p.a.src[i].height = s.height;
+        p.a.src[i].stride = s.stride;
+        if (i + 1 > p.a.nsrc) p.a.nsrc = (uint8_t)(i + 1);
+    }
+
+    void emit_step(Pending &p, int dst_slot) {
+        Slot &d = E.slots[dst_slot];
+        p.prog.optimise();
+        // A trailing quantisation to the very format being stored is implied by the store.
+        while (!p.prog.ins.empty() && p.prog.ins.back().op == ZS_P_QUANT && format_equal(p.prog.ins.back().fa, d.fmt))
+            p.prog.ins.pop_back();
+        Step st;
+        st.kind = StepKind::Raster;
+        st.label = p.label;
+        st.raster = p.a;
+        st.raster.dst_stride = d.stride;
+        st.raster.dst_fmt = d.fmt;
+        st.dst_slot = dst_slot;
+        for (int i = 0; i < ZS_MAX_SRCS; ++i) st.src_slot[i] = p.src_slot[i];
+        st.idx_x_slot = p.idx_x_slot;
+        st.idx_y_slot = p.idx_y_slot;
+        st.weight_slot = p.weight_slot;
+        // Pixel program: FP64 host program -> FP32 parameters.
+        ZsPixelProgram &pp = st.raster.prog;
+        std::memset(&pp, 0, sizeof(pp));
+        int nf = 0, np = 0;
+        auto fmt_id = [&](const ZsFormat &f) -> uint8_t {
+            for (int i = 0; i < nf; ++i)
+                if (format_equal(st.raster.fmts[i], f)) return (uint8_t)i;
+            if (nf >= ZS_MAX_FMTS) fail(ZS_ERR_UNIMPLEMENTED, "too many formats in one fused program");
+            st.raster.fmts[nf] = f;
+            return (uint8_t)nf++;
+        };
+        for (const HInstr &hi : p.prog.ins) {
+            if (pp.n >= ZS_MAX_INSTR) fail(ZS_ERR_UNIMPLEMENTED, "fused program too long");
+            ZsPInstr &o = pp.ins[pp.n++];
+            o.op = hi.op;
+            o.a = hi.a;
+            o.b = hi.b;
+            o.p = (uint16_t)np;
+            if (hi.op == ZS_P_MAT3) {
+                if (np + 9 > ZS_MAX_PARAMS) fail(ZS_ERR_UNIMPLEMENTED, "too many parameters");
+                for (int k = 0; k < 9; ++k) pp.prm[np++] = (float)hi.mat.m[k];
+            } else if (hi.op == ZS_P_INJECT) {
+                if (np + 8 > ZS_MAX_PARAMS) fail(ZS_ERR_UNIMPLEMENTED, "too many parameters");
+                for (int k = 0; k < 8; ++k) pp.prm[np++] = (float)hi.v[k];
+            } else if (hi.op == ZS_P_QUANT) {
+                o.a = fmt_id(hi.fa);
+            } else if (hi.op == ZS_P_TRANSMUTE) {
+                o.a = fmt_id(hi.fa);
+                o.b = fmt_id(hi.fb);
+            }
+        }
+        // Gathers with no program between equal formats copy texel bytes verbatim.
+        const uint8_t pr = p.a.producer;
+        if (pp.n == 0 && (pr == ZS_PR_QUAD || (pr == ZS_PR_AFFINE && !p.a.bilinear) || pr == ZS_PR_PALETTE ||
+                          pr == ZS_PR_INDEX)) {
+            bool same = true;
+            const int gather_src = (pr == ZS_PR_QUAD || pr == ZS_PR_AFFINE) ? 1 : 0;
+            same = format_equal(p.a.src[gather_src].fmt, d.fmt) && p.a.src[gather_src].fmt.bpp == d.fmt.bpp;
+            if (p.a.has_below) same = same && format_equal(p.a.src[0].fmt, d.fmt);
+            st.raster.raw_copy = same ? 1 : 0;
+        }
+        try_chain(st);
+        E.steps.push_back(st);
+    }
+
+    // The canonical colour chain: [M] [cbrt [M]] [cube [M]] [clamp [M]], RGBA8 sRGB in/out.
+    void try_chain(Step &st) {
+        if (E.mode != ZS_MODE_FUSED) return;
+        const ZsRasterArgs &a = st.raster;
+        if (a.producer != ZS_PR_LOAD || a.nsrc != 1) return;
+        if (a.src[0].fmt.fast != ZS_FAST_RGBA8_SRGB || a.dst_fmt.fast != ZS_FAST_RGBA8_SRGB) return;
+        const ZsPixelProgram &pp = a.prog;
+        ZsChainArgs c;
+        std::memset(&c, 0, sizeof(c));
+        for (int k = 0; k < 4; ++k) {
+            c.m[k][0] = c.m[k][4] = c.m[k][8] = 1.0f;
+        }
+        int stage = 0;   // 0: before cbrt (M_a), 1: M_b, 2: M_c, 3: M_d
+        for (int i = 0; i < pp.n; ++i) {
+            const ZsPInstr &o = pp.ins[i];
+            if (o.op == ZS_P_MAT3) {
+                // two matrices in one stage cannot happen after optimise(); guard anyway
+                if (c.flags & (ZS_CHAIN_MA << stage)) return;
+                for (int k = 0; k < 9; ++k) c.m[stage][k] = pp.prm[o.p + k];
+                c.flags |= ZS_CHAIN_MA << stage;
+            } else if (o.op == ZS_P_CBRT && stage < 1) {
+                stage = 1;
+                c.flags |= ZS_CHAIN_CBRT;
+            } else if (o.op == ZS_P_CUBE && stage < 2) {
+                stage = 2;
+                c.flags |= ZS_CHAIN_CUBE;
+            } else if (o.op == ZS_P_CLAMP01 && stage < 3) {
+                stage = 3;
+                c.flags |= ZS_CHAIN_CLAMP;
+            } else {
+                return;
+            }
+        }
+        if (a.src[0].width != a.width || a.src[0].height != a.height) return;
+        c.npx = (int64_t)a.width * a.height;
+        st.kind = StepKind::Chain;
+        st.chain = c;
+        st.chain_src_fast = ZS_FAST_RGBA8_SRGB;
+        st.chain_dst_fast = ZS_FAST_RGBA8_SRGB;
+        st.label += " [fused chain kernel]";
+    }
+
+    void materialize(uint32_t reg) {
+        Val &v = vals[reg];
+        if (v.materialized) return;
+        const Desc &d = desc(reg);
+        int slot;
+        ZsFormat f;
+        if (out_slot_of[reg] >= 0) {
+            slot = out_slot_of[reg];
+            f = E.slots[slot].fmt;
+        } else {
+            f = storage_format(reg);
+            slot = new_slot(SlotKind::Intermediate, d.width, d.height, f);
+        }
+        emit_step(*v.pend, slot);
+        v.pend.reset();
+        v.materialized = true;
+        v.slot = slot;
+        v.fmt = f;
+    }
+
+    // Take the pending launch of `reg` to extend it, or start a LOAD launch from its buffer.
+    std::unique_ptr<Pending> take(uint32_t reg, const std::string &label) {
+        Val &v = vals[reg];
+        if (!v.materialized && v.pend && remaining[reg] == 0 && out_slot_of[reg] < 0) {
+            auto p = std::move(v.pend);
+            v.materialized = true;    // consumed: nothing else may read it
+            v.slot = -1;
+            p->label += " + " + label;
+            return p;
+        }
+        materialize(reg);
+        const Desc &d = desc(reg);
+        auto p = new_pending(ZS_PR_LOAD, d.width, d.height, label);
+        set_src(*p, 0, reg);
+        return p;
+    }
+
+    void need(uint32_t reg) { materialize(reg); }
+
+    void set_pending(uint32_t reg, std::unique_ptr<Pending> p) {
+        Val &v = vals[reg];
+        // The declared texel of the op's result bounds its precision (faithful semantics).
+        ZsFormat declared = format_of(desc(reg));
+        if (!format_is_lossless_f32(declared)) p->prog.quant(declared);
+        v.pend = std::move(p);
+        v.materialized = false;
+        if (E.mode != ZS_MODE_FUSED) materialize(reg);
+    }
+
+    void use(uint32_t reg) {
+        if (remaining[reg] > 0) remaining[reg]--;
+    }
+
+    void run() {
+        const size_t n = P.ops.size();
+        vals.resize(n);
+        out_slot_of.assign(n, -1);
+        remaining = P.uses;
+        // Output slots first (declaration order).
+        for (size_t k = 0; k < P.output_regs.size(); ++k) {
+            uint32_t oreg = P.output_regs[k];
+            uint32_t src = P.ops[oreg].a;
+            const Desc &d = desc(src);
+            int s = new_slot(SlotKind::Output, d.width, d.height, format_of(d), oreg);
+            E.output_slot.push_back(s);
+            E.output_regs.push_back(oreg);
+            E.output_desc.push_back(d);
+            if (out_slot_of[src] < 0 && P.ops[src].kind != OpKind::Input) out_slot_of[src] = s;
+        }
+        for (uint32_t r = 0; r < n; ++r) {
+            const Op &op = P.ops[r];
+            const Desc &d = op.desc;
+            switch (op.kind) {
+            case OpKind::Input: {
+                int s = new_slot(SlotKind::Input, d.width, d.height, format_of(d), r);
+                E.input_slot.push_back(s);
+                E.input_regs.push_back(r);
+                E.input_desc.push_back(d);
+                vals[r].materialized = true;
+                vals[r].slot = s;
+                vals[r].fmt = format_of(d);
+            } break;
+            case OpKind::Output: {
+                uint32_t src = op.a;
+                int slot = out_slot_of[src];
+                use(src);
+                if (slot >= 0 && !vals[src].materialized) {
+                    materialize(src);
+                    break;
+                }
+                // The value lives elsewhere (an input or a shared buffer): copy / convert.
+                need(src);
+                int os = -1;
+                for (size_t k = 0; k < E.output_regs.size(); ++k)
+                    if (E.output_regs[k] == r) os = E.output_slot[k];
+                if (os == vals[src].slot) break;
+                if (format_equal(vals[src].fmt, E.slots[os].fmt)) {
+                    Step st;
+                    st.kind = StepKind::Copy;
+                    st.src_slot[0] = vals[src].slot;
+                    st.dst_slot = os;
+                    st.copy_bytes = E.slots[os].bytes;
+                    st.label = "copy to output";
+                    E.steps.push_back(st);
+                } else {
+                    auto p = new_pending(ZS_PR_LOAD, d.width, d.height, "store output");
+                    set_src(*p, 0, src);
+                    emit_step(*p, os);
+                }
+            } break;
+            case OpKind::ColorConvert:
+            case OpKind::ChromaticAdaptation:
+            case OpKind::ColorMatrix: {
+                use(op.a);
+                auto p = take(op.a, op.kind == OpKind::ColorConvert ? "color_convert"
+                                    : op.kind == OpKind::ColorMatrix ? "color_matrix" : "chromatic_adaptation");
+                for (const HInstr &i : op.prog.ins) p->prog.ins.push_back(i);
+                set_pending(r, std::move(p));
+            } break;
+            case OpKind::Extract: {
+                use(op.a);
+                auto p = take(op.a, "extract");
+                set_pending(r, std::move(p));
+            } break;
+            case OpKind::Transmute: {
+                use(op.a);
+                Val &sv = vals[op.a];
+                ZsFormat from = format_of(desc(op.a)), to = format_of(d);
+                if (sv.materialized && sv.slot >= 0 && format_equal(sv.fmt, from)) {
+                    // Pure reinterpretation of a buffer in its declared format: no work.
+                    vals[r].materialized = true;
+                    vals[r].slot = sv.slot;
+                    vals[r].fmt = to;
+                    break;
+                }
+                auto p = take(op.a, "transmute");
+                HInstr t;
+                t.op = ZS_P_TRANSMUTE;
+                t.fa = from;
+                t.fb = to;
+                p->prog.ins.push_back(t);
+                set_pending(r, std::move(p));
+            } break;
+            case OpKind::Inject: {
+                use(op.a);
+                use(op.b);
+                need(op.b);
+                auto p = take(op.a, "inject");
+                if (p->a.producer != ZS_PR_LOAD || p->a.nsrc != 1) {
+                    // A second pixel-aligned operand cannot join a gather: store it first.
+                    const Desc &bd = desc(op.a);
+                    ZsFormat f = storage_format(op.a);
+                    int slot = new_slot(SlotKind::Intermediate, bd.width, bd.height, f);
+                    emit_step(*p, slot);
+                    p = new_pending(ZS_PR_LOAD, d.width, d.height, "inject");
+                    set_src_slot(*p, 0, slot);
+                }
+                set_src(*p, 1, op.b);
+                for (const HInstr &i : op.prog.ins) p->prog.ins.push_back(i);
+                set_pending(r, std::move(p));
+            } break;
+            case OpKind::Crop:
+            case OpKind::Inscribe:
+            case OpKind::InscribePlaced: {
+                const bool crop = op.kind == OpKind::Crop;
+                if (!crop) { use(op.a); need(op.a); }
+                uint32_t above = crop ? op.a : op.b;
+                use(above);
+                need(above);
+                auto p = new_pending(ZS_PR_QUAD, d.width, d.height, crop ? "crop" : "inscribe");
+                if (!crop) {
+                    set_src(*p, 0, op.a);
+                    p->a.has_below = 1;
+                }
+                set_src(*p, 1, above);
+                const Desc &ad = desc(above);
+                if (crop) {
+                    p->a.rect[0] = 0; p->a.rect[1] = 0; p->a.rect[2] = (int)d.width; p->a.rect[3] = (int)d.height;
+                    p->a.sel[0] = (int)op.rect.x; p->a.sel[1] = (int)op.rect.y;
+                    p->a.sel[2] = (int)op.rect.max_x; p->a.sel[3] = (int)op.rect.max_y;
+                } else {
+                    p->a.rect[0] = (int)op.rect.x; p->a.rect[1] = (int)op.rect.y;
+                    p->a.rect[2] = (int)op.rect.max_x; p->a.rect[3] = (int)op.rect.max_y;
+                    p->a.sel[0] = 0; p->a.sel[1] = 0; p->a.sel[2] = (int)ad.width; p->a.sel[3] = (int)ad.height;
+                }
+                set_pending(r, std::move(p));
+            } break;
+            case OpKind::Affine: {
+                use(op.a);
+                use(op.b);
+                need(op.a);
+                need(op.b);
+                auto p = new_pending(ZS_PR_AFFINE, d.width, d.height, op.u0 ? "affine bilinear" : "affine nearest");
+                set_src(*p, 0, op.a);
+                set_src(*p, 1, op.b);
+                p->a.has_below = 1;
+                p->a.bilinear = (uint8_t)op.u0;
+                Mat3 fwd{};
+                for (int k = 0; k < 9; ++k) fwd.m[k] = op.fparams[k];
+                Mat3 inv = fwd.inverse();
+                for (int k = 0; k < 9; ++k) p->a.aff[k] = (float)inv.m[k];
+                set_pending(r, std::move(p));
+            } break;
+            case OpKind::Palette: {
+                use(op.a);
+                use(op.b);
+                need(op.a);
+                need(op.b);
+                auto p = new_pending(ZS_PR_PALETTE, d.width, d.height, "palette");
+                set_src(*p, 0, op.a);
+                set_src(*p, 1, op.b);
+                for (int k = 0; k < 8; ++k) p->a.cons[k] = op.fparams[k];
+                set_pending(r, std::move(p));
+            } break;
+            case OpKind::Bilinear: {
+                auto p = new_pending(ZS_PR_BILINEAR, d.width, d.height, "bilinear");
+                for (int k = 0; k < 24; ++k) p->a.cons[k] = op.fparams[k];
+                set_pending(r, std::move(p));
+            } break;
+            case OpKind::Solid: {
+                auto p = new_pending(ZS_PR_SOLID, d.width, d.height, "solid");
+                for (int k = 0; k < 4; ++k) p->a.cons[k] = op.fparams[k];
+                set_pending(r, std::move(p));
+            } break;
+            case OpKind::Resize: {
+                use(op.a);
+                need(op.a);
+                const Desc &sd = desc(op.a);
+                auto p = new_pending(ZS_PR_INDEX, d.width, d.height, "resize");
+                set_src(*p, 0, op.a);
+                std::vector<int32_t> ix(d.width), iy(d.height);
+                resize_index(sd.width, d.width, ix.data());
+                resize_index(sd.height, d.height, iy.data());
+                p->idx_x_slot = table_slot(ix.data(), ix.size() * 4);
+                p->idx_y_slot = table_slot(iy.data(), iy.size() * 4);
+                set_pending(r, std::move(p));
+            } break;
+            case OpKind::ResizeFiltered: {
+                use(op.a);
+                need(op.a);
+                const Desc &sd = desc(op.a);
+                // Pass 1: horizontal, into an intermediate (dst width x src height).
+                auto h = new_pending(ZS_PR_RESAMPLE_H, d.width, sd.height, "resample horizontal");
+                set_src(*h, 0, op.a);
+                add_weights(*h, sd.width, d.width, op.u0);
+                ZsFormat mid = E.mode == ZS_MODE_PER_OP_F32 ? linear_f32_format() : linear_f16_format();
+                int ms = new_slot(SlotKind::Intermediate, d.width, sd.height, mid);
+                emit_step(*h, ms);
+                // Pass 2: vertical, pending so that following per-pixel ops fuse into it.
+                auto v = new_pending(ZS_PR_RESAMPLE_V, d.width, d.height, "resample vertical");
+                v->src_slot[0] = ms;
+                v->a.src[0].fmt = mid;
+                v->a.src[0].width = (int)d.width;
+                v->a.src[0].height = (int)sd.height;
+                v->a.src[0].stride = (int64_t)d.width * mid.bpp;
+                v->a.nsrc = 1;
+                add_weights(*v, sd.height, d.height, op.u0);
+                set_pending(r, std::move(v));
+            } break;
+            case OpKind::Blend: {
+                use(op.a);
+                use(op.b);
+                need(op.a);
+                need(op.b);
+                auto p = new_pending(ZS_PR_BLEND, d.width, d.height, "blend");
+                set_src(*p, 0, op.a);
+                set_src(*p, 1, op.b);
+                p->a.rect[0] = (int)op.rect.x;
+                p->a.rect[1] = (int)op.rect.y;
+                p->a.blend_mode = (uint8_t)op.u0;
+                p->a.straight = d.alpha == ZS_ALPHA_PREMULTIPLIED ? 0 : 1;
+                set_pending(r, std::move(p));
+            } break;
+            }
+        }
+        // Anything still pending with an output slot (defensive).
+        for (uint32_t r = 0; r < n; ++r)
+            if (!vals[r].materialized && vals[r].pend && out_slot_of[r] >= 0) materialize(r);
+    }
+
+    // The reference's resize (command.rs:1675-1702): a bilinear grid holding u at pixel
+    // centres, stored as truncated 8-bit staged texels, decoded as q/255, then palette.frag
+    // with the 0.5/size bias and nearest sampling -- all f32.
+    static void resize_index(uint32_t src_len, uint32_t dst_len, int32_t *index) {
+        volatile float fdst = (float)dst_len, fsrc = (float)src_len;
+        for (uint32_t x = 0; x < dst_len; ++x) {
+            volatile float u = ((float)x + 0.5f) / fdst;
+            volatile float scaled = u * 255.0f;
+            uint32_t q = (uint32_t)scaled;
+            volatile float basis = (float)q / 255.0f;
+            volatile float bias = 0.5f / fdst;
+            volatile float t = basis + bias;
+            volatile float pos = t * fsrc;
+            int32_t ix = (int32_t)std::floor((float)pos);
+            if (ix < 0) ix = 0;
+            if (ix > (int32_t)src_len - 1) ix = (int32_t)src_len - 1;
+            index[x] = ix;
+        }
+    }
+
+    void add_weights(Pending &p, uint32_t src_len, uint32_t dst_len, uint32_t filter) {
+        std::vector<int32_t> first, count;
+        std::vector<float> w;
+        int taps = resample_weights(src_len, dst_len, filter, first, count, w);
+        p.idx_x_slot = table_slot(first.data(), first.size() * 4);
+        p.idx_y_slot = table_slot(count.data(), count.size() * 4);
+        p.weight_slot = table_slot(w.data(), w.size() * 4);
+        p.a.taps = taps;
+    }
+
+    // Separable filter weights, FP64-normalised (box = area coverage, Lanczos-3, triangle);
+    // output pixel i is centred at (i + 0.5) * src/dst; the kernel widens by the downscale
+    // factor; taps outside the image are dropped and the rest renormalised.
+    static int resample_weights(uint32_t src_len, uint32_t dst_len, uint32_t filter, std::vector<int32_t> &first,
+                                std::vector<int32_t> &count, std::vector<float> &weights) {
+        const double s = (double)src_len / (double)dst_len, f = s > 1.0 ? s : 1.0;
+        const double R = filter == 1 ? 3.0 : (filter == 2 ? 1.0 : 0.5);
+        const double r = R * f;
+        const int taps = (int)std::ceil(2.0 * R * f) + 2;
+        first.assign(dst_len, 0);
+        count.assign(dst_len, 0);
+        weights.assign((size_t)dst_len * taps, 0.0f);
+        std::vector<double> w(taps);
+        for (uint32_t i = 0; i < dst_len; ++i) {
+            const double c = ((double)i + 0.5) * s;
+            int lo = (int)std::floor(c - r), hi = (int)std::ceil(c + r);
+            if (lo < 0) lo = 0;
+            if (hi > (int)src_len) hi = (int)src_len;
+            int n = 0, start = -1;
+            double sum = 0.0;
+            for (int j = lo; j < hi && n < taps; ++j) {
+                double v;
+                if (filter == 0) {
+                    double a = c - 0.5 * f, b = c + 0.5 * f;
+                    double ov = std::fmin(b, j + 1.0) - std::fmax(a, (double)j);
+                    v = ov > 0 ? ov : 0.0;
+                } else {
+                    double t = (j + 0.5 - c) / f;
+                    if (filter == 1) {
+                        auto sinc = [](double x) {
+                            if (std::fabs(x) < 1e-12) return 1.0;
+                            double px = 3.14159265358979323846 * x;
+                            return std::sin(px) / px;
+                        };
+                        v = std::fabs(t) < 3.0 ? sinc(t) * sinc(t / 3.0) : 0.0;
+                    } else {
+                        v = std::fabs(t) < 1.0 ? 1.0 - std::fabs(t) : 0.0;
+                    }
+                }
+                if (start < 0) {
+                    if (v == 0.0) continue;
+                    start = j;
+                }
+                w[n++] = v;
+                sum += v;
+            }
+            while (n > 0 && w[n - 1] == 0.0) n--;
+            if (start < 0 || sum == 0.0) {
+                int j = (int)std::floor(c);
+                if (j > (int)src_len - 1) j = (int)src_len - 1;
+                start = j;
+                n = 1;
+                w[0] = 1.0;
+                sum = 1.0;
+            }
+            for (int t = 0; t < n; ++t) weights[(size_t)i * taps + t] = (float)(w[t] / sum);
+            first[i] = start;
+            count[i] = n;
+        }
+        return taps;
+    }
+};
+
+std::unique_ptr<Executable> lower(const Program &prog, const zs_capabilities &caps) {
+    auto E = std::make_unique<Executable>();
+    E->device = caps.device;
+    E->mode = caps.mode;
+    E->use_graph = caps.use_graph != 0;
+    if (caps.mode > ZS_MODE_PER_OP_F16) fail(ZS_ERR_INVALID_ARG, "unknown lowering mode");
+    Planner pl(prog, *E);
+    pl.run();
+    std::ostringstream os;
+    os << "executable: " << E->steps.size() << " launches, mode " << E->mode << "\n";
+    for (size_t i = 0; i < E->steps.size(); ++i) {
+        const Step &s = E->steps[i];
+        os << "  [" << i << "] " << (s.kind == StepKind::Chain ? "chain" : s.kind == StepKind::Copy ? "copy" : "raster")
+           << " " << s.label << " -> slot " << s.dst_slot;
+        if (s.kind == StepKind::Raster) os << " (" << s.raster.width << "x" << s.raster.height << ", " << s.raster.prog.n
+                                           << " ops" << (s.raster.raw_copy ? ", raw" : "") << ")";
+        os << "\n";
+    }
+    E->plan_text = os.str();
+    return E;
+}
+
+}  // namespace zs

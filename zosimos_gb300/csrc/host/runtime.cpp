@@ -1,0 +1,129 @@
+// runtime.cpp -- Pool, device buffers, launch recording, CUDA-graph replay and the
+// step-wise Execution (the analogue of lib/zosimos/src/run.rs: Executable::launch
+// :1016-1048, Execution::step :1389-1464, Retire :2786-2998, pool.rs).
+//
+// The reference interprets a stream of GL-like `Low` instructions against wgpu, with
+// one queue submit and host row copies per op.  Here an Execution owns one CUDA
+// stream; its instructions are the host->device copies of bound inputs followed by the
+// executable's kernel launches; results stay device resident until retired.
+#include <cstdlib>
+#include <cstring>
+
+#include "zs_host.hpp"
+
+namespace zs {
+
+static bool have_device() {
+    int n = 0;
+    return cudaGetDeviceCount(&n) == cudaSuccess && n > 0;
+}
+
+static void *host_alloc(uint64_t bytes, bool &pinned) {
+    void *p = nullptr;
+    pinned = false;
+    if (bytes == 0) bytes = 1;
+    if (have_device() && cudaMallocHost(&p, bytes) == cudaSuccess) {
+        pinned = true;
+        return p;
+    }
+    cudaGetLastError();
+    p = std::malloc(bytes);
+    if (!p) fail(ZS_ERR_OUT_OF_MEMORY, "host allocation failed");
+    return p;
+}
+
+static void host_release(void *p, bool pinned) {
+    if (!p) return;
+    if (pinned) cudaFreeHost(p);
+    else std::free(p);
+}
+
+// ---------------------------------------------------------------- pool
+
+PoolImage::~PoolImage() {
+    host_release(host, host_pinned);
+    if (dev) cudaFree(dev);
+}
+
+void PoolImage::ensure_host() {
+    if (!host) host = (uint8_t *)host_alloc(len, host_pinned);
+}
+
+PoolImage &Pool::get(uint64_t key) {
+    auto it = images.find(key);
+    if (it == images.end()) fail(ZS_ERR_MISSING_KEY, "no image with this key in the pool");
+    return *it->second;
+}
+
+// ---------------------------------------------------------------- executable
+
+Executable::~Executable() {
+    for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+    if (graph_stream) cudaStreamDestroy(graph_stream);
+    for (void *p : dev_buffers)
+        if (p) cudaFree(p);
+}
+
+void Executable::ensure_buffers() {
+    if (!dev_buffers.empty()) return;
+    check_cuda(cudaSetDevice(device), "cudaSetDevice");
+    check_cuda(init_device_tables(device), "sRGB tables");
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) == cudaSuccess && sms > 0) sm_count = sms;
+    dev_buffers.assign(slots.size(), nullptr);
+    for (size_t i = 0; i < slots.size(); ++i) {
+        const Slot &s = slots[i];
+        if (s.bytes == 0) continue;
+        void *p = nullptr;
+        check_cuda(cudaMalloc(&p, s.bytes), "cudaMalloc");
+        dev_buffers[i] = p;
+        if (s.kind == SlotKind::Table)
+            check_cuda(cudaMemcpy(p, s.table.data(), s.bytes, cudaMemcpyHostToDevice), "table upload");
+    }
+}
+
+void Executable::record(cudaStream_t stream, const std::vector<void *> &ptrs) {
+    record_range(stream, ptrs, 0, steps.size());
+}
+
+void Executable::record_range(cudaStream_t stream, const std::vector<void *> &ptrs, size_t begin, size_t end) {
+    for (size_t k = begin; k < end && k < steps.size(); ++k) {
+        const Step &st = steps[k];
+        switch (st.kind) {
+        case StepKind::Copy:
+            check_cuda(cudaMemcpyAsync(ptrs[st.dst_slot], ptrs[st.src_slot[0]], st.copy_bytes, cudaMemcpyDeviceToDevice,
+                                       stream),
+                       "device copy");
+            break;
+        case StepKind::Chain: {
+            ZsChainArgs c = st.chain;
+            c.src = (const uint8_t *)ptrs[st.src_slot[0]];
+            c.dst = (uint8_t *)ptrs[st.dst_slot];
+            check_cuda(launch_chain(c, st.chain_src_fast, st.chain_dst_fast, sm_count, stream), st.label.c_str());
+        } break;
+        case StepKind::Raster: {
+            ZsRasterArgs a = st.raster;
+            for (int i = 0; i < ZS_MAX_SRCS; ++i)
+                a.src[i].ptr = st.src_slot[i] >= 0 ? (const uint8_t *)ptrs[st.src_slot[i]] : nullptr;
+            a.dst = (uint8_t *)ptrs[st.dst_slot];
+            a.index_x = st.idx_x_slot >= 0 ? (const int32_t *)ptrs[st.idx_x_slot] : nullptr;
+            a.index_y = st.idx_y_slot >= 0 ? (const int32_t *)ptrs[st.idx_y_slot] : nullptr;
+            a.weights = st.weight_slot >= 0 ? (const float *)ptrs[st.weight_slot] : nullptr;
+            check_cuda(launch_raster(a, sm_count, stream), st.label.c_str());
+        } break;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- execution
+
+Execution::~Execution() {
+    if (stream) {
+        cudaStreamSynchronize(stream);
+        cudaStreamDestroy(stream);
+    }
+    for (void *p : owned)
+        if (p) cudaFree(p);
+}
+
+}  // namespace zs

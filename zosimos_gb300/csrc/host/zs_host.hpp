@@ -1,0 +1,222 @@
+// zs_host.hpp -- host-side model of the executor: descriptors, command buffer,
+// program, lowered executable and runtime objects behind the C ABI.
+//
+// Mirrors the reference's Rust API shape (lib/zosimos/src/command.rs CommandBuffer,
+// Linker; program.rs Program::lower_to; run.rs Executable / Environment /
+// Execution / Retire; pool.rs Pool) with a CUDA runtime underneath.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../../include/zosimos.h"
+#include "../zs_kernels.h"
+#include "../zs_shared.h"
+
+namespace zs {
+
+// ---------------------------------------------------------------- errors
+
+struct Error {
+    int code;
+    std::string msg;
+};
+
+[[noreturn]] void fail(int code, const std::string &msg);
+void check_cuda(cudaError_t e, const char *what);
+void set_last_error(const std::string &msg);
+
+// ---------------------------------------------------------------- descriptors
+
+using Desc = zs_descriptor;
+
+uint32_t texel_bytes(uint32_t bits);
+uint32_t channel_count_bits(uint32_t bits);
+uint32_t channel_count_parts(uint32_t parts);
+bool is_consistent(const Desc &d);
+uint64_t row_bytes(const Desc &d);      // width * texel bytes
+uint64_t host_stride(const Desc &d);    // row_stride or tight
+uint64_t host_len(const Desc &d);
+bool same_chroma(const Desc &a, const Desc &b);   // texel + colour equal (descriptor_chroma)
+ZsFormat format_of(const Desc &d);
+bool format_is_lossless_f32(const ZsFormat &f);
+bool format_equal(const ZsFormat &a, const ZsFormat &b);
+ZsFormat linear_f32_format();
+ZsFormat linear_f16_format();
+std::string describe(const Desc &d);
+
+// ---------------------------------------------------------------- colour matrices (FP64)
+
+struct Mat3 {
+    double m[9];
+    static Mat3 identity();
+    static Mat3 diag(double a, double b, double c);
+    Mat3 operator*(const Mat3 &o) const;
+    Mat3 inverse() const;
+    bool is_identity(double tol = 1e-14) const;
+};
+
+Mat3 rgb_to_xyz(uint32_t primaries, uint32_t whitepoint);
+void whitepoint_xyz(uint32_t whitepoint, double out[3]);
+bool adaptation_matrix(uint32_t method, uint32_t src_wp, uint32_t dst_wp, Mat3 &out);
+extern const Mat3 kOklabM1, kOklabM2, kCat02, kHpe;
+
+// ---------------------------------------------------------------- host pixel program
+
+struct HInstr {
+    uint8_t op = ZS_P_NOP;
+    uint8_t a = 0, b = 0;
+    Mat3 mat{};                 // MAT3
+    double v[8] = {0};          // INJECT select/weights
+    ZsFormat fa{}, fb{};        // QUANT / TRANSMUTE formats
+};
+
+struct HProgram {
+    std::vector<HInstr> ins;
+    void mat(const Mat3 &m);
+    void op(uint8_t o);
+    void quant(const ZsFormat &f);
+    void optimise();            // fold matrices (FP64), drop identities and no-op quantisation
+};
+
+// ---------------------------------------------------------------- command buffer
+
+enum class OpKind {
+    Input, Output, Crop, ColorConvert, ChromaticAdaptation, ColorMatrix, Extract, Inject,
+    Transmute, Inscribe, InscribePlaced, Palette, Bilinear, Solid, Affine, Resize,
+    ResizeFiltered, Blend
+};
+
+struct Op {
+    OpKind kind;
+    uint32_t a = 0, b = 0;       // operand registers
+    Desc desc{};                 // result descriptor
+    zs_rect rect{};
+    float fparams[24] = {0};
+    uint32_t u0 = 0, u1 = 0;     // sampling / filter / mode / channels
+    int32_t i0 = -1, i1 = -1;
+    HProgram prog;               // per-pixel semantics of colour ops
+};
+
+struct Command {
+    std::vector<Op> ops;
+    uint32_t push(Op op);
+    const Desc &describe(uint32_t reg) const;
+    bool is_value(uint32_t reg) const;
+};
+
+// ---------------------------------------------------------------- program
+
+struct Program {
+    std::vector<Op> ops;
+    std::vector<uint32_t> inputs, outputs;   // registers (outputs: the value registers)
+    std::vector<uint32_t> output_regs;       // the Output op registers
+    std::vector<uint32_t> uses;              // use counts of every register
+};
+
+// ---------------------------------------------------------------- executable
+
+enum class SlotKind { Input, Intermediate, Output, Table };
+
+struct Slot {
+    SlotKind kind;
+    uint64_t bytes = 0;
+    int64_t stride = 0;
+    int32_t width = 0, height = 0;
+    ZsFormat fmt{};
+    uint32_t reg = 0;            // Input: input register; Output: output register
+    std::vector<uint8_t> table;  // Table contents (weights / indices), uploaded at lowering
+};
+
+struct SrcRef {
+    int slot = -1;
+    ZsFormat fmt{};
+    int32_t width = 0, height = 0;
+    int64_t stride = 0;
+};
+
+enum class StepKind { Raster, Chain, Copy };
+
+struct Step {
+    StepKind kind;
+    ZsRasterArgs raster;         // pointers filled at launch from slots
+    ZsChainArgs chain;
+    uint8_t chain_src_fast = 0, chain_dst_fast = 0;
+    int src_slot[ZS_MAX_SRCS] = {-1, -1, -1};
+    int dst_slot = -1;
+    int idx_x_slot = -1, idx_y_slot = -1, weight_slot = -1;
+    uint64_t copy_bytes = 0;
+    std::string label;
+};
+
+struct Executable {
+    int device = 0;
+    uint32_t mode = ZS_MODE_FUSED;
+    bool use_graph = false;
+    int sm_count = 148;
+    std::vector<Slot> slots;
+    std::vector<Step> steps;
+    std::vector<uint32_t> input_regs, output_regs;     // value registers in declaration order
+    std::vector<Desc> input_desc, output_desc;
+    std::vector<int> input_slot, output_slot;
+    std::vector<void *> dev_buffers;                   // device allocation per slot (owned ones)
+    std::string plan_text;
+    // CUDA graphs of the launch sequence for zs_run_device, keyed by the bound pointers
+    std::map<std::vector<void *>, cudaGraphExec_t> graphs;
+    std::vector<std::vector<void *>> graph_order;     // insertion order for eviction
+    cudaStream_t graph_stream = nullptr;
+    ~Executable();
+    void ensure_buffers();
+    void record(cudaStream_t stream, const std::vector<void *> &ptrs);
+    void record_range(cudaStream_t stream, const std::vector<void *> &ptrs, size_t begin, size_t end);
+};
+
+std::unique_ptr<Executable> lower(const Program &prog, const zs_capabilities &caps);
+
+// ---------------------------------------------------------------- pool / runtime
+
+struct PoolImage {
+    Desc desc{};
+    uint8_t *host = nullptr;     // pinned (or malloc'd when no device)
+    bool host_pinned = false;
+    uint64_t len = 0;
+    void *dev = nullptr;         // device copy (tight rows)
+    uint64_t dev_len = 0;
+    bool dev_valid = false;      // device holds the current contents
+    bool host_valid = true;
+    ~PoolImage();
+    void ensure_host();
+};
+
+struct Pool {
+    std::map<uint64_t, std::unique_ptr<PoolImage>> images;
+    uint64_t next_key = 1;
+    PoolImage &get(uint64_t key);
+};
+
+struct Environment {
+    Executable *exe = nullptr;
+    Pool *pool = nullptr;
+    std::map<uint32_t, uint64_t> binds;          // input register -> key
+    std::map<uint32_t, uint64_t> output_binds;   // output register -> key
+};
+
+struct Execution {
+    Executable *exe = nullptr;
+    Pool *pool = nullptr;
+    cudaStream_t stream = nullptr;
+    std::vector<void *> ptrs;                    // per slot
+    std::vector<void *> owned;                   // temporary device buffers of this execution
+    std::map<uint32_t, uint64_t> output_binds;
+    size_t cursor = 0;                           // next instruction
+    size_t total = 0;
+    std::vector<uint64_t> input_keys;
+    ~Execution();
+};
+
+}  // namespace zs

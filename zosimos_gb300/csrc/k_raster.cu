@@ -1,0 +1,224 @@
+// k_raster.cu -- the generic raster kernel: one launch per materialised register.
+//
+// Replaces one render pass of the reference (a quad draw of a fragment shader over
+// the target, lib/zosimos/src/program.rs:1486-1533, run.rs:2678-2739) *plus* every
+// per-pixel op the planner fused behind it, so that intermediates never round-trip
+// through HBM.  Producers:
+//   LOAD      pixel-aligned operands (colour ops, inject)            linear/inject.frag
+//   BILINEAR  bilinear.frag:14-20                                     construct
+//   SOLID     solid_rgb                                               construct
+//   QUAD      copy.frag + box.vert:43-59 (crop, inscribe)             nearest gather
+//   AFFINE    affine paint of `above` over `below`                    nearest / bilinear
+//   PALETTE   palette.frag:21-31                                      coordinate gather
+//   INDEX     resize through a nearest index table                    gather
+//   BLEND     blend of `above` at an offset over `below`              (new op)
+//   RESAMPLE  one separable filter pass (FP64-normalised weights)      (new op)
+// Gathers whose source and destination formats agree and that carry no fused
+// program copy texel bytes verbatim (integer-exact).
+#include <atomic>
+
+#include "zs_device.cuh"
+#include "zs_kernels.h"
+
+namespace zs {
+std::atomic<uint64_t> g_kernel_launches{0};
+uint64_t kernel_launch_count() { return g_kernel_launches.load(); }
+}  // namespace zs
+
+__device__ __forceinline__ int zs_quad_src(int p, int t0, int t1, int s0, int s1) {
+    // floor(s0 + (p - t0 + 0.5) * (s1 - s0) / (t1 - t0)) in exact integer arithmetic.
+    long long num = (2LL * (p - t0) + 1) * (long long)(s1 - s0);
+    return s0 + (int)(num / (2LL * (t1 - t0)));
+}
+
+__device__ __forceinline__ void zs_affine_map(const float *inv, int x, int y, float &qx, float &qy) {
+    float cx = (float)x + 0.5f, cy = (float)y + 0.5f;
+    float X = fmaf(inv[0], cx, fmaf(inv[1], cy, inv[2]));
+    float Y = fmaf(inv[3], cx, fmaf(inv[4], cy, inv[5]));
+    float Z = fmaf(inv[6], cx, fmaf(inv[7], cy, inv[8]));
+    if (Z != 1.0f) { X = __fdiv_rn(X, Z); Y = __fdiv_rn(Y, Z); }
+    qx = X;
+    qy = Y;
+}
+
+__device__ __forceinline__ int zs_clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+__device__ __forceinline__ float4 zs_lerp4(float4 a, float4 b, float t) {
+    return make_float4(a.x + (b.x - a.x) * t, a.y + (b.y - a.y) * t, a.z + (b.z - a.z) * t,
+                       a.w + (b.w - a.w) * t);
+}
+
+__global__ void __launch_bounds__(256) zs_raster_kernel(const __grid_constant__ ZsRasterArgs a) {
+    const int64_t n = (int64_t)a.width * a.height;
+    const int64_t step = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += step) {
+        const int y = (int)(i / a.width);
+        const int x = (int)(i - (int64_t)y * a.width);
+        float4 r = make_float4(0.f, 0.f, 0.f, 0.f), r2 = r;
+        uint4 raw = make_uint4(0, 0, 0, 0);
+        bool is_raw = false;
+        const ZsSource &s0 = a.src[0];
+        const ZsSource &s1 = a.src[1];
+        switch (a.producer) {
+        case ZS_PR_LOAD:
+            r = zs_load_px(s0, x, y);
+            if (a.nsrc > 1) r2 = zs_load_px(s1, x, y);
+            break;
+        case ZS_PR_BILINEAR: {
+            // Unfused IEEE operations in a fixed order, so that the value (and any
+            // truncating quantisation of it) is reproducible on the CPU.
+            float u = __fdiv_rn((float)x + 0.5f, (float)a.width), v = __fdiv_rn((float)y + 0.5f, (float)a.height);
+            float uv = __fmul_rn(u, v);
+            const float *p = a.cons;
+            float o[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                float fu = __fadd_rn(__fmul_rn(p[k], 1.f - u), __fmul_rn(p[4 + k], u));
+                float fv = __fadd_rn(__fmul_rn(p[8 + k], 1.f - v), __fmul_rn(p[12 + k], v));
+                float fw = __fadd_rn(__fmul_rn(p[16 + k], 1.f - uv), __fmul_rn(p[20 + k], uv));
+                o[k] = __fadd_rn(__fadd_rn(fu, fv), fw);
+            }
+            r = make_float4(o[0], o[1], o[2], o[3]);
+        } break;
+        case ZS_PR_SOLID:
+            r = make_float4(a.cons[0], a.cons[1], a.cons[2], a.cons[3]);
+            break;
+        case ZS_PR_QUAD: {
+            const bool inside = x >= a.rect[0] && x < a.rect[2] && y >= a.rect[1] && y < a.rect[3];
+            if (inside) {
+                int sx = zs_clampi(zs_quad_src(x, a.rect[0], a.rect[2], a.sel[0], a.sel[2]), 0, s1.width - 1);
+                int sy = zs_clampi(zs_quad_src(y, a.rect[1], a.rect[3], a.sel[1], a.sel[3]), 0, s1.height - 1);
+                if (a.raw_copy) {
+                    raw = zs_load_raw(s1.ptr + (int64_t)sy * s1.stride + (int64_t)sx * s1.fmt.bpp, s1.fmt.bpp);
+                    is_raw = true;
+                } else {
+                    r = zs_load_px(s1, sx, sy);
+                }
+            } else if (a.has_below) {
+                if (a.raw_copy) {
+                    raw = zs_load_raw(s0.ptr + (int64_t)y * s0.stride + (int64_t)x * s0.fmt.bpp, s0.fmt.bpp);
+                    is_raw = true;
+                } else {
+                    r = zs_load_px(s0, x, y);
+                }
+            } else if (a.raw_copy) {
+                is_raw = true;
+            }
+        } break;
+        case ZS_PR_AFFINE: {
+            float qx, qy;
+            zs_affine_map(a.aff, x, y, qx, qy);
+            const bool inside = qx >= 0.0f && qx < (float)s1.width && qy >= 0.0f && qy < (float)s1.height;
+            if (inside && !a.bilinear) {
+                int ix = min((int)floorf(qx), s1.width - 1), iy = min((int)floorf(qy), s1.height - 1);
+                if (a.raw_copy) {
+                    raw = zs_load_raw(s1.ptr + (int64_t)iy * s1.stride + (int64_t)ix * s1.fmt.bpp, s1.fmt.bpp);
+                    is_raw = true;
+                } else {
+                    r = zs_load_px(s1, ix, iy);
+                }
+            } else if (inside) {
+                float tx = qx - 0.5f, ty = qy - 0.5f;
+                float fx0 = floorf(tx), fy0 = floorf(ty);
+                float fx = tx - fx0, fy = ty - fy0;
+                int x0 = (int)fx0, y0 = (int)fy0;
+                int xa = zs_clampi(x0, 0, s1.width - 1), xb = zs_clampi(x0 + 1, 0, s1.width - 1);
+                int ya = zs_clampi(y0, 0, s1.height - 1), yb = zs_clampi(y0 + 1, 0, s1.height - 1);
+                float4 top = zs_lerp4(zs_load_px(s1, xa, ya), zs_load_px(s1, xb, ya), fx);
+                float4 bot = zs_lerp4(zs_load_px(s1, xa, yb), zs_load_px(s1, xb, yb), fx);
+                r = zs_lerp4(top, bot, fy);
+            } else if (a.has_below) {
+                if (a.raw_copy) {
+                    raw = zs_load_raw(s0.ptr + (int64_t)y * s0.stride + (int64_t)x * s0.fmt.bpp, s0.fmt.bpp);
+                    is_raw = true;
+                } else {
+                    r = zs_load_px(s0, x, y);
+                }
+            } else if (a.raw_copy) {
+                is_raw = true;
+            }
+        } break;
+        case ZS_PR_PALETTE: {
+            // palette.frag:22-31: uv = channels . basis + 0.5 / size(rhs); nearest sample of lhs.
+            float4 basis = zs_load_px(s1, x, y);
+            const float *c = a.cons;
+            float u = c[0] * basis.x + c[1] * basis.y + c[2] * basis.z + c[3] * basis.w;
+            float v = c[4] * basis.x + c[5] * basis.y + c[6] * basis.z + c[7] * basis.w;
+            float tu = __fadd_rn(u, __fdiv_rn(0.5f, (float)s1.width));
+            float tv = __fadd_rn(v, __fdiv_rn(0.5f, (float)s1.height));
+            int ix = zs_clampi((int)floorf(__fmul_rn(tu, (float)s0.width)), 0, s0.width - 1);
+            int iy = zs_clampi((int)floorf(__fmul_rn(tv, (float)s0.height)), 0, s0.height - 1);
+            if (a.raw_copy) {
+                raw = zs_load_raw(s0.ptr + (int64_t)iy * s0.stride + (int64_t)ix * s0.fmt.bpp, s0.fmt.bpp);
+                is_raw = true;
+            } else {
+                r = zs_load_px(s0, ix, iy);
+            }
+        } break;
+        case ZS_PR_INDEX: {
+            int ix = a.index_x[x], iy = a.index_y[y];
+            if (a.raw_copy) {
+                raw = zs_load_raw(s0.ptr + (int64_t)iy * s0.stride + (int64_t)ix * s0.fmt.bpp, s0.fmt.bpp);
+                is_raw = true;
+            } else {
+                r = zs_load_px(s0, ix, iy);
+            }
+        } break;
+        case ZS_PR_BLEND: {
+            r = zs_load_px(s0, x, y);
+            int ax = x - a.rect[0], ay = y - a.rect[1];
+            if (ax >= 0 && ay >= 0 && ax < s1.width && ay < s1.height) {
+                float4 s = zs_load_px(s1, ax, ay);
+                zs_blend_px(r, s, a.blend_mode, a.straight);
+            }
+        } break;
+        case ZS_PR_RESAMPLE_H: {
+            int first = a.index_x[x], cnt = a.index_y[x];
+            const float *w = a.weights + (int64_t)x * a.taps;
+            float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int t = 0; t < cnt; ++t) {
+                float4 s = zs_load_px(s0, first + t, y);
+                float wt = w[t];
+                acc.x = fmaf(wt, s.x, acc.x); acc.y = fmaf(wt, s.y, acc.y);
+                acc.z = fmaf(wt, s.z, acc.z); acc.w = fmaf(wt, s.w, acc.w);
+            }
+            r = acc;
+        } break;
+        case ZS_PR_RESAMPLE_V: {
+            int first = a.index_x[y], cnt = a.index_y[y];
+            const float *w = a.weights + (int64_t)y * a.taps;
+            float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int t = 0; t < cnt; ++t) {
+                float4 s = zs_load_px(s0, x, first + t);
+                float wt = w[t];
+                acc.x = fmaf(wt, s.x, acc.x); acc.y = fmaf(wt, s.y, acc.y);
+                acc.z = fmaf(wt, s.z, acc.z); acc.w = fmaf(wt, s.w, acc.w);
+            }
+            r = acc;
+        } break;
+        default: break;
+        }
+        uint8_t *dp = a.dst + (int64_t)y * a.dst_stride + (int64_t)x * a.dst_fmt.bpp;
+        if (is_raw) {
+            zs_store_raw(dp, a.dst_fmt.bpp, raw);
+            continue;
+        }
+        zs_run_program(a.prog, a.fmts, r, r2);
+        zs_store_raw(dp, a.dst_fmt.bpp, zs_encode_raw(a.dst_fmt, r));
+    }
+}
+
+namespace zs {
+
+cudaError_t launch_raster(const ZsRasterArgs &args, int sm_count, cudaStream_t stream) {
+    const int64_t n = (int64_t)args.width * args.height;
+    if (n <= 0) return cudaSuccess;
+    int64_t blocks = (n + 255) / 256;
+    const int64_t cap = (int64_t)(sm_count > 0 ? sm_count : 148) * 8;
+    if (blocks > cap) blocks = cap;
+    zs_raster_kernel<<<(unsigned)blocks, 256, 0, stream>>>(args);
+    g_kernel_launches.fetch_add(1);
+    return cudaGetLastError();
+}
+
+}  // namespace zs

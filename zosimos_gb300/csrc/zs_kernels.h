@@ -1,0 +1,25 @@
+// zs_kernels.h -- host-callable launchers of the CUDA kernels (no torch types).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "zs_shared.h"
+
+namespace zs {
+
+// Exact sRGB8 tables (zs_tables.cu).
+void build_srgb_tables(float *decode, uint32_t *encode);
+cudaError_t init_device_tables(int device);
+
+// Generic raster launch: producer + fused pixel program + store (k_raster.cu).
+cudaError_t launch_raster(const ZsRasterArgs &args, int sm_count, cudaStream_t stream);
+
+// Fused colour chain in canonical form, RGBA8 in / RGBA8 out (k_chain.cu).
+// Returns cudaErrorNotSupported when no specialisation exists for the formats.
+cudaError_t launch_chain(const ZsChainArgs &args, uint8_t src_fast, uint8_t dst_fast, int sm_count,
+                         cudaStream_t stream);
+
+// Number of kernel launches issued since process start (instrumentation for the bench).
+uint64_t kernel_launch_count();
+
+}  // namespace zs

@@ -1,0 +1,147 @@
+// zs_shared.h -- plain-old-data shared by the C++ host planner and the CUDA kernels.
+//
+// A compiled zosimos Program is lowered into a list of raster launches.  Each launch
+// has a *producer* (how the first value of a pixel is obtained: pixel-aligned loads,
+// a construct, a quad/affine/palette gather, a blend or a separable resample pass),
+// a *pixel program* (per-pixel ops fused behind the producer: colour matrices, cube
+// roots, clamps, declared-texel quantisation, inject, ...) and a *store* in the
+// register's storage format.  Everything here is POD so that it can travel as a
+// __grid_constant__ kernel parameter.
+#pragma once
+#include <stdint.h>
+
+#define ZS_MAX_INSTR 48
+#define ZS_MAX_PARAMS 320
+#define ZS_MAX_FMTS 8
+#define ZS_MAX_SRCS 3
+
+// Storage format of one register (what lib/zosimos/src/program.rs:781-946 derives from a
+// Descriptor).  `fast` selects a specialised decode/encode path.
+enum ZsFast : uint8_t {
+    ZS_FAST_GENERIC = 0,
+    ZS_FAST_RGBA8_SRGB = 1,    // native Rgba8UnormSrgb: LUT decode, exact round-to-nearest encode
+    ZS_FAST_RGBA8_UNORM = 2,   // native Rgba8Unorm
+    ZS_FAST_BGRA8_SRGB = 3,
+    ZS_FAST_BGRA8_UNORM = 4,
+    ZS_FAST_F16X4 = 5,         // Float16x4 RgbA, linear transfer
+    ZS_FAST_F32X4 = 6          // Float32x4 RgbA, linear transfer
+};
+
+struct ZsFormat {
+    uint8_t bits;      // SampleBits code (stage.frag:152-171)
+    uint8_t parts;     // SampleParts code (stage.frag:122-142)
+    uint8_t native;    // 1: hardware unorm (round to nearest), 0: staged (truncating)
+    uint8_t bpp;       // bytes per texel
+    uint16_t transfer; // transfer code, 0x100 = LabLch
+    uint8_t fast;      // ZsFast
+    uint8_t pad;
+};
+
+enum ZsPOp : uint8_t {
+    ZS_P_NOP = 0,
+    ZS_P_MAT3,         // r.rgb = M * r.rgb                   (linear.frag)
+    ZS_P_CBRT,         // signed cube root of r.rgb           (oklab.frag:42)
+    ZS_P_CUBE,         // r.rgb^3                             (oklab.frag:58)
+    ZS_P_CLAMP01,      // clamp r.rgb to [0,1]                (oklab.frag:63, srlab2.frag:84)
+    ZS_P_SRL_NL,       // SrLab2 piecewise cube root          (srlab2.frag:87-95)
+    ZS_P_SRL_NLINV,    //                                     (srlab2.frag:105-112)
+    ZS_P_SRL_ENC_DIFF, // (y, (x-y)*5/1.16, (z-y)*2/1.16)     (srlab2.frag:51-57)
+    ZS_P_SRL_DEC_DIFF, //                                     (srlab2.frag:70-74)
+    ZS_P_QUANT,        // encode into fmt[a] and decode back (declared intermediate texel)
+    ZS_P_TRANSMUTE,    // encode into fmt[a], reinterpret the bytes as fmt[b] and decode
+    ZS_P_INJECT,       // r = mix(r, dot(r2, w), select)      (inject.frag:20-25)
+    ZS_P_BLEND,        // r = blend(r (below), r2 (above))    (mode in a, straight alpha in b)
+    ZS_P_MOV2,         // r2 = r
+    ZS_P_SWAP,         // swap r and r2
+    ZS_P_PREMUL,       // r.rgb *= r.a
+    ZS_P_UNPREMUL      // r.rgb /= r.a (0 where a == 0)
+};
+
+struct ZsPInstr {
+    uint8_t op;
+    uint8_t a, b, c;   // small operands (format ids, modes)
+    uint16_t p;        // offset into params
+    uint16_t pad;
+};
+
+struct ZsPixelProgram {
+    int32_t n;
+    int32_t pad;
+    ZsPInstr ins[ZS_MAX_INSTR];
+    float prm[ZS_MAX_PARAMS];
+};
+
+enum ZsProducer : uint8_t {
+    ZS_PR_LOAD = 0,     // r = src0(x,y), r2 = src1(x,y) (pixel aligned)
+    ZS_PR_BILINEAR,     // bilinear.frag construct
+    ZS_PR_SOLID,        // solid colour
+    ZS_PR_QUAD,         // below(x,y); inside target: src1(nearest map of selection)
+    ZS_PR_AFFINE,       // below(x,y); inside transformed quad: sample src1
+    ZS_PR_PALETTE,      // src0(coords from src1(x,y))       (palette.frag)
+    ZS_PR_INDEX,        // src0(ix[x], iy[y])                (resize via a nearest index table)
+    ZS_PR_BLEND,        // below(x,y) blended with src1(x-ox, y-oy)
+    ZS_PR_RESAMPLE_H,   // horizontal filter pass over src0 rows
+    ZS_PR_RESAMPLE_V    // vertical filter pass over src0 columns
+};
+
+struct ZsSource {
+    const uint8_t *ptr;
+    int64_t stride;   // bytes per row
+    int32_t width, height;
+    ZsFormat fmt;
+};
+
+struct ZsRasterArgs {
+    // producer
+    uint8_t producer;
+    uint8_t nsrc;
+    uint8_t raw_copy;     // gather producers: copy texel bytes verbatim (same format, no program)
+    uint8_t has_below;    // QUAD/AFFINE/BLEND: src0 is the image painted over
+    uint8_t bilinear;     // AFFINE: bilinear sampling
+    uint8_t blend_mode;
+    uint8_t straight;
+    uint8_t pad0;
+    ZsSource src[ZS_MAX_SRCS];
+    int32_t rect[4];      // QUAD target rect / BLEND offset rect
+    int32_t sel[4];       // QUAD selection rect in src1
+    float aff[9];         // AFFINE inverse matrix (f32, applied with a fixed fmaf order)
+    float cons[24];       // BILINEAR params / SOLID colour / PALETTE channel weights (8)
+    const int32_t *index_x;   // INDEX producer / RESAMPLE first-tap table
+    const int32_t *index_y;   // INDEX producer / RESAMPLE tap-count table
+    const float *weights;     // RESAMPLE weights [dst][taps]
+    int32_t taps;
+    int32_t pad1;
+    // destination
+    uint8_t *dst;
+    int64_t dst_stride;
+    int32_t width, height;
+    ZsFormat dst_fmt;
+    ZsFormat fmts[ZS_MAX_FMTS];   // formats referenced by QUANT / TRANSMUTE
+    ZsPixelProgram prog;
+};
+
+// Fused colour chain in canonical form (the hot path):
+//   decode -> M_a -> [cbrt] -> M_b -> [cube] -> M_c -> [clamp] -> M_d -> encode
+struct ZsChainArgs {
+    const uint8_t *src;
+    uint8_t *dst;
+    int64_t npx;          // pixels (flat: the chain is pixel-local)
+    float m[4][9];
+    int32_t flags;        // bit0 cbrt, bit1 cube, bit2 clamp, bit3..6 matrix present
+    int32_t pad;
+};
+
+enum {
+    ZS_CHAIN_CBRT = 1,
+    ZS_CHAIN_CUBE = 2,
+    ZS_CHAIN_CLAMP = 4,
+    ZS_CHAIN_MA = 8,
+    ZS_CHAIN_MB = 16,
+    ZS_CHAIN_MC = 32,
+    ZS_CHAIN_MD = 64
+};
+
+// Entry count of the exact sRGB8 encode table: buckets of the float bit pattern
+// (bits >> 16) for x in [2^-13, 1], each holding at most one rounding threshold.
+#define ZS_ENC_BASE (114u << 7)
+#define ZS_ENC_ENTRIES 1665

@@ -1,0 +1,75 @@
+"""Seeded synthetic images for the benchmark workloads (no dataset is available).
+
+Counter-based: every value is splitmix64(key(seed, image, pixel, channel)), so any
+sub-rectangle or image of a batch can be generated independently and identically on
+any machine.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+_M1 = np.uint64(0xBF58476D1CE4E5B9)
+_M2 = np.uint64(0x94D049BB133111EB)
+_GOLD = np.uint64(0x9E3779B97F4A7C15)
+
+
+def splitmix64(x: np.ndarray) -> np.ndarray:
+    z = x + _GOLD
+    z = (z ^ (z >> np.uint64(30))) * _M1
+    z = (z ^ (z >> np.uint64(27))) * _M2
+    return z ^ (z >> np.uint64(31))
+
+
+def _keys(seed: int, image: int, npx: int, channel: int, start: int = 0) -> np.ndarray:
+    base = np.uint64(((seed & 0xFFFF) << 48) | ((image & 0xFFFF) << 32))
+    px = np.arange(start, start + npx, dtype=np.uint64)
+    return base ^ (px * np.uint64(4) + np.uint64(channel))
+
+
+def srgb_gradient_noise(width: int, height: int, seed: int = 1, image: int = 0, noise: int = 16,
+                        random_alpha: bool = True) -> np.ndarray:
+    """RGBA8 sRGB: R = x ramp, G = y ramp, B = diagonal ramp, plus uniform integer noise
+    in [-noise, noise] (clamped), alpha uniform in [0, 255] (or opaque)."""
+    y, x = np.mgrid[0:height, 0:width]
+    r = np.rint(255.0 * x / max(width - 1, 1))
+    g = np.rint(255.0 * y / max(height - 1, 1))
+    b = np.rint(255.0 * (x + y) / max(width + height - 2, 1))
+    out = np.empty((height, width, 4), dtype=np.uint8)
+    n = width * height
+    for c, base in enumerate((r, g, b)):
+        z = splitmix64(_keys(seed, image, n, c))
+        nz = (z % np.uint64(2 * noise + 1)).astype(np.int64) - noise
+        out[..., c] = np.clip(base.reshape(-1) + nz, 0, 255).reshape(height, width)
+    if random_alpha:
+        out[..., 3] = (splitmix64(_keys(seed, image, n, 3)) & np.uint64(255)).astype(np.uint8).reshape(height, width)
+    else:
+        out[..., 3] = 255
+    return out
+
+
+def linear_gradient_gauss(width: int, height: int, seed: int = 3, image: int = 0, sigma: float = 0.05,
+                          dtype=np.float16) -> np.ndarray:
+    """Linear RGBA: gradient ramps plus Gaussian noise (Box-Muller on splitmix64),
+    clamped to [0, 1], alpha 1."""
+    y, x = np.mgrid[0:height, 0:width].astype(np.float64)
+    base = [x / max(width - 1, 1), y / max(height - 1, 1), (x + y) / max(width + height - 2, 1)]
+    n = width * height
+    out = np.empty((height, width, 4), dtype=np.float64)
+    for c in range(3):
+        z1 = splitmix64(_keys(seed, image, n, c))
+        z2 = splitmix64(z1)
+        u1 = ((z1 >> np.uint64(11)).astype(np.float64) + 1.0) / 9007199254740993.0
+        u2 = (z2 >> np.uint64(11)).astype(np.float64) / 9007199254740992.0
+        g = np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)
+        out[..., c] = np.clip(base[c] + sigma * g.reshape(height, width), 0.0, 1.0)
+    out[..., 3] = 1.0
+    return out.astype(dtype)
+
+
+def thumbnail_sizes(count: int = 1024, seed: int = 4, lo: int = 64, hi: int = 4096):
+    """Image sides log-uniform in [lo, hi] (independent width and height)."""
+    z = splitmix64(_keys(seed, 0xFFFF, 2 * count, 0))
+    u = (z >> np.uint64(11)).astype(np.float64) / 9007199254740992.0
+    sides = np.exp(np.log(lo) + u * (np.log(hi) - np.log(lo)))
+    sides = np.clip(np.rint(sides), lo, hi).astype(np.int64)
+    return sides[0::2], sides[1::2]
