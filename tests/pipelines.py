@@ -230,7 +230,9 @@ def ours_lab_grid(space: str, mode=zs.Mode.Fused):
 
 
 def oracle_lab_grid(space: str):
-    grid = O.bilinear_construct(400, 400, **GRID)
+    # bilinear.frag is f32 arithmetic; the construct is restated in f32 with the GPU's
+    # operation order so that the truncating 8-bit grid holds the same bytes.
+    grid = O.bilinear_construct(400, 400, **GRID, f32=True).astype(np.float64)
     fmt_u8 = O.Format(O.BITS["UInt8x4"], O.PARTS["RgbA"], O.TRANSFER["Linear"], False)
     gb = O.encode(fmt_u8, grid)
     lch = O.Format(O.BITS["UInt8x4"], O.PARTS["LchA"], O.TRANSFER["LabLch"], False)

@@ -30,6 +30,25 @@ def test_chain_vs_oracle(mode, shape):
     assert (ours.reshape(h, w, 4)[..., 3] == img[..., 3]).all()
 
 
+def test_identity_chain_is_bit_exact():
+    """sRGB8 -> linear FP32 -> sRGB8 folds to an empty program: the fused kernel's
+    decode table and exact round-to-nearest encode must reproduce every byte."""
+    v = np.arange(256, dtype=np.uint8)
+    img = np.stack(np.meshgrid(v, v[::-1]), -1)                     # 256 x 256 x 2
+    img = np.concatenate([img, (img[..., :1] ^ 0x5A), img[..., 1:] ^ 0x33], -1).astype(np.uint8)
+    c = zs.CommandBuffer()
+    d = zs.Descriptor.srgb_rgba8(256, 256)
+    i = c.input(d)
+    lin = c.color_convert(i, zs.Descriptor.linear_rgba_f32(256, 256))
+    back = c.color_convert(lin, d)
+    o, _ = c.output(back)
+    exe = zs.Linker.from_included().compile(c).lower_to()
+    assert "fused chain kernel" in exe.describe()
+    out = np.empty((256, 1024), np.uint8)
+    exe.run_host([P.rgba_bytes(img)], [out])
+    assert (out == P.rgba_bytes(img)).all()
+
+
 def test_chain_is_one_kernel():
     c, _, _ = P.chain_commands(64, 64)
     exe = zs.Linker.from_included().compile(c).lower_to()

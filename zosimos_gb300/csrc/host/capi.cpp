@@ -41,6 +41,13 @@ zs_executable::~zs_executable() {
     if (stream) cudaStreamDestroy(stream);
 }
 
+static void note_graph_launch(const Executable &E) {
+    uint64_t n = 0;
+    for (const Step &st : E.steps)
+        if (st.kind != StepKind::Copy) ++n;
+    add_kernel_launches(n);
+}
+
 template <class F>
 static int guarded(F &&f) {
     try {
@@ -615,6 +622,7 @@ int zs_run_device(zs_executable *exe, const void *const *inputs, uint32_t n_inpu
             E.graph_order.push_back(ptrs);
         }
         check_cuda(cudaGraphLaunch(it->second, s), "graph launch");
+        note_graph_launch(E);
     });
 }
 

@@ -266,6 +266,13 @@ void HProgram::optimise() {
     std::vector<HInstr> out;
     for (const HInstr &i : ins) {
         if (i.op == ZS_P_QUANT && format_is_lossless_f32(i.fa)) continue;
+        // A value just decoded from (or quantised to) format f is representable in f:
+        // quantising it again is at best a no-op and, for formats whose decode/encode
+        // is not exactly invertible in FP32 (LabLch), would add error.
+        if (i.op == ZS_P_QUANT && !out.empty() &&
+            ((out.back().op == ZS_P_TRANSMUTE && format_equal(out.back().fb, i.fa)) ||
+             (out.back().op == ZS_P_QUANT && format_equal(out.back().fa, i.fa))))
+            continue;
         if (i.op == ZS_P_MAT3 && !out.empty() && out.back().op == ZS_P_MAT3) {
             out.back().mat = i.mat * out.back().mat;     // later matrix applied after: M2 * M1
             continue;

@@ -200,6 +200,13 @@ struct Planner {
         }
         if (a.src[0].width != a.width || a.src[0].height != a.height) return;
         c.npx = (int64_t)a.width * a.height;
+        // Decoded sRGB8 values are in [0, 1]; a non-negative M_a keeps the cube-root
+        // arguments non-negative, so the kernel may skip the sign handling.
+        bool nonneg = true;
+        for (int k = 0; k < 9; ++k) nonneg = nonneg && c.m[0][k] >= 0.0f;
+        if (nonneg) c.flags |= ZS_CHAIN_CBRT_NONNEG;
+        for (int s = 0; s < 4; ++s)
+            for (int k = 0; k < 9; ++k) c.m2[s][k][0] = c.m2[s][k][1] = c.m[s][k];
         st.kind = StepKind::Chain;
         st.chain = c;
         st.chain_src_fast = ZS_FAST_RGBA8_SRGB;

@@ -9,11 +9,20 @@
 // every pass (lib/zosimos/src/program.rs:1486-1533), this is one HBM pass:
 // 4 bytes read and 4 bytes written per pixel.
 //
-// Data path per thread: 16-byte coalesced streaming loads (4 pixels), sRGB decode
-// through a lane-replicated shared table (conflict-free: lane l reads column l),
-// FP32 arithmetic, exact round-to-nearest sRGB encode through the bucketed
-// threshold table, alpha bytes passed through (decode/encode of a unorm8 alpha is
-// the identity), 16-byte streaming stores.
+// The chain is issue-bound on GB300 rather than HBM-bound (about 60 instructions per
+// 8 bytes moved), so the data path is built to minimise instructions per pixel:
+//  * 16-byte coalesced streaming loads/stores; two vectors (8 pixels) computed while the
+//    next two are in flight (software pipeline), 512-thread blocks, two per SM;
+//  * sRGB decode from a lane-replicated shared table (lane l reads column l: no bank
+//    conflicts whatever the data);
+//  * pixels processed in pairs with packed FP32x2 FMA (one instruction, two pixels),
+//    the matrix coefficients read as 64-bit constant operands;
+//  * cube roots as ex2(lg2(x)/3) on the MUFU pipe (the sign fix-up is dropped when the
+//    host proves M_a keeps [0,1]^3 non-negative);
+//  * clamps as saturating adds on the FMA pipe;
+//  * exact round-to-nearest sRGB encode from a bucketed threshold table replicated 4x
+//    across lanes (entry + float bits carries the code into byte 3), packed with PRMT;
+//  * alpha bytes passed through (unorm8 alpha decode + encode is the identity).
 #include <atomic>
 
 #include "zs_device.cuh"
@@ -23,124 +32,216 @@ namespace zs {
 extern std::atomic<uint64_t> g_kernel_launches;
 }
 
-#define ZS_CHAIN_THREADS 256
-#define ZS_CHAIN_UNROLL 2
+#define ZS_CHAIN_THREADS 512
+#define ZS_ENC_REP 4
 
+// Decode rows are 256 bytes apart so that the byte offset of (code, lane) is
+// (code << 8) | (lane << 2): one PRMT builds it from the packed texel.
 struct ZsChainSmem {
-    float lut[256 * 32];
-    uint32_t enc[ZS_ENC_ENTRIES];
+    float lut[256 * 64];                         // [code][lane], lanes 32..63 unused
+    uint32_t enc[ZS_ENCS_ENTRIES * ZS_ENC_REP];   // [bucket][lane & 3], shifted domain
 };
 
-__device__ __forceinline__ void zs_m3(const float *m, float &r, float &g, float &b) {
-    float x = r, y = g, z = b;
-    r = fmaf(m[0], x, fmaf(m[1], y, m[2] * z));
-    g = fmaf(m[3], x, fmaf(m[4], y, m[5] * z));
-    b = fmaf(m[6], x, fmaf(m[7], y, m[8] * z));
+__device__ __forceinline__ float zs_ex2(float x) {
+    float y;
+    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float zs_lg2(float x) {
+    float y;
+    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
 }
 
-template <bool CBRT, bool CUBE, bool CLAMP>
-__device__ __forceinline__ uint32_t zs_chain_px(uint32_t w, const float *lut_lane, const uint32_t *enc,
-                                                const ZsChainArgs &a) {
-    float r = lut_lane[(w & 255u) << 5];
-    float g = lut_lane[((w >> 8) & 255u) << 5];
-    float b = lut_lane[((w >> 16) & 255u) << 5];
-    zs_m3(a.m[0], r, g, b);
-    if (CBRT) { r = zs_scbrt(r); g = zs_scbrt(g); b = zs_scbrt(b); }
-    zs_m3(a.m[1], r, g, b);
-    if (CUBE) { r = r * r * r; g = g * g * g; b = b * b * b; }
-    zs_m3(a.m[2], r, g, b);
-    if (CLAMP) { r = __saturatef(r); g = __saturatef(g); b = __saturatef(b); }
-    zs_m3(a.m[3], r, g, b);
-    return zs_enc_srgb8(enc, r) | (zs_enc_srgb8(enc, g) << 8) | (zs_enc_srgb8(enc, b) << 16) | (w & 0xff000000u);
+template <bool NONNEG>
+__device__ __forceinline__ float zs_cbrt1(float x) {
+    if (NONNEG) return zs_ex2(zs_lg2(x) * (1.0f / 3.0f));
+    return copysignf(zs_ex2(zs_lg2(fabsf(x)) * (1.0f / 3.0f)), x);
 }
 
-template <bool CBRT, bool CUBE, bool CLAMP>
-__global__ void __launch_bounds__(ZS_CHAIN_THREADS) zs_chain_srgb8_kernel(const __grid_constant__ ZsChainArgs a) {
+// saturate(x) as a saturating add on the FMA pipe (the ALU pipe is the busier one).
+__device__ __forceinline__ float zs_sat(float x) {
+    float y;
+    asm("add.rn.sat.f32 %0, %1, 0f00000000;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+__device__ __forceinline__ float2 zs_sat2(float2 v) { return make_float2(zs_sat(v.x), zs_sat(v.y)); }
+
+// rgb' = M rgb on a pixel pair; SAT saturates the results to [0, 1].
+template <bool SAT>
+__device__ __forceinline__ void zs_m3x2(const float (*m)[2], float2 &r, float2 &g, float2 &b) {
+    const float2 *c = reinterpret_cast<const float2 *>(m);
+    const float2 x = r, y = g, z = b;
+    r = __ffma2_rn(c[0], x, __ffma2_rn(c[1], y, __fmul2_rn(c[2], z)));
+    g = __ffma2_rn(c[3], x, __ffma2_rn(c[4], y, __fmul2_rn(c[5], z)));
+    b = __ffma2_rn(c[6], x, __ffma2_rn(c[7], y, __fmul2_rn(c[8], z)));
+    if (SAT) {
+        r = zs_sat2(r);
+        g = zs_sat2(g);
+        b = zs_sat2(b);
+    }
+}
+
+// x in [0, 1] -> table entry + bits of x + 2^-12; the sRGB8 code is byte 3 of the
+// result.  The shift keeps the argument inside the table without an integer clamp.
+__device__ __forceinline__ uint32_t zs_enc_q(const uint32_t *enc_lane, float x) {
+    const uint32_t b = __float_as_uint(x + (1.0f / 4096.0f));
+    return enc_lane[((b >> 16) - ZS_ENCS_BASE) * ZS_ENC_REP] + b;
+}
+
+// Decoded value of byte K of texel w for this lane: (code << 8) | (lane << 2) is the
+// byte offset of the lane-replicated table entry, built by one byte permute.
+template <int K>
+__device__ __forceinline__ float zs_dec(const unsigned char *lut, uint32_t w, uint32_t lane4) {
+    const uint32_t off = __byte_perm(w, lane4, 0x5504u | (K << 4));
+    return *reinterpret_cast<const float *>(lut + off);
+}
+
+__device__ __forceinline__ void zs_cbrt2(float2 &v) {
+    // NONNEG: both arguments are >= 0 (the MUFU log of 0 is -inf, its exp2 is 0).
+    float2 l = make_float2(zs_lg2(v.x), zs_lg2(v.y));
+    l = __fmul2_rn(l, make_float2(1.0f / 3.0f, 1.0f / 3.0f));
+    v = make_float2(zs_ex2(l.x), zs_ex2(l.y));
+}
+
+template <bool CBRT, bool CUBE, bool CLAMP, bool NONNEG>
+__device__ __forceinline__ void zs_chain_pair(uint32_t &wp, uint32_t &wq, const unsigned char *lut,
+                                              uint32_t lane4, const uint32_t *enc_lane,
+                                              const ZsChainArgs &a) {
+    float2 r = make_float2(zs_dec<0>(lut, wp, lane4), zs_dec<0>(lut, wq, lane4));
+    float2 g = make_float2(zs_dec<1>(lut, wp, lane4), zs_dec<1>(lut, wq, lane4));
+    float2 b = make_float2(zs_dec<2>(lut, wp, lane4), zs_dec<2>(lut, wq, lane4));
+    zs_m3x2<false>(a.m2[0], r, g, b);
+    if (CBRT) {
+        if (NONNEG) {
+            zs_cbrt2(r);
+            zs_cbrt2(g);
+            zs_cbrt2(b);
+        } else {
+            r.x = zs_cbrt1<false>(r.x); r.y = zs_cbrt1<false>(r.y);
+            g.x = zs_cbrt1<false>(g.x); g.y = zs_cbrt1<false>(g.y);
+            b.x = zs_cbrt1<false>(b.x); b.y = zs_cbrt1<false>(b.y);
+        }
+    }
+    zs_m3x2<false>(a.m2[1], r, g, b);
+    if (CUBE) {
+        r = __fmul2_rn(__fmul2_rn(r, r), r);
+        g = __fmul2_rn(__fmul2_rn(g, g), g);
+        b = __fmul2_rn(__fmul2_rn(b, b), b);
+    }
+    zs_m3x2<CLAMP>(a.m2[2], r, g, b);
+    zs_m3x2<true>(a.m2[3], r, g, b);
+    const uint32_t rp = zs_enc_q(enc_lane, r.x), gp = zs_enc_q(enc_lane, g.x), bp = zs_enc_q(enc_lane, b.x);
+    const uint32_t rq = zs_enc_q(enc_lane, r.y), gq = zs_enc_q(enc_lane, g.y), bq = zs_enc_q(enc_lane, b.y);
+    wp = __byte_perm(__byte_perm(rp, gp, 0x0073), __byte_perm(bp, wp, 0x0073), 0x5410);
+    wq = __byte_perm(__byte_perm(rq, gq, 0x0073), __byte_perm(bq, wq, 0x0073), 0x5410);
+}
+
+template <bool CBRT, bool CUBE, bool CLAMP, bool NONNEG>
+__global__ void __launch_bounds__(ZS_CHAIN_THREADS, 2) zs_chain_srgb8_kernel(const __grid_constant__ ZsChainArgs a) {
     extern __shared__ __align__(16) unsigned char zs_smem_raw[];
     ZsChainSmem &sm = *reinterpret_cast<ZsChainSmem *>(zs_smem_raw);
-    for (int i = threadIdx.x; i < 256 * 32; i += blockDim.x) sm.lut[i] = zs_srgb_decode_lut[i >> 5];
-    for (int i = threadIdx.x; i < ZS_ENC_ENTRIES; i += blockDim.x) sm.enc[i] = zs_srgb_encode_tab[i];
+    for (int i = threadIdx.x; i < 256 * 32; i += blockDim.x) sm.lut[(i >> 5) * 64 + (i & 31)] = zs_srgb_decode_lut[i >> 5];
+    for (int i = threadIdx.x; i < ZS_ENCS_ENTRIES * ZS_ENC_REP; i += blockDim.x)
+        sm.enc[i] = zs_srgb_encode_tab_shifted[i / ZS_ENC_REP];
     __syncthreads();
-    const float *lut_lane = sm.lut + (threadIdx.x & 31);
-    const uint32_t *enc = sm.enc;
+    const int lane = threadIdx.x & 31;
+    const unsigned char *lut = reinterpret_cast<const unsigned char *>(sm.lut);
+    const uint32_t lane4 = (uint32_t)lane << 2;
+    const uint32_t *enc_lane = sm.enc + (lane & (ZS_ENC_REP - 1));
 
     const uint4 *in = reinterpret_cast<const uint4 *>(a.src);
     uint4 *out = reinterpret_cast<uint4 *>(a.dst);
     const int64_t nvec = a.npx >> 2;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    for (; v + (ZS_CHAIN_UNROLL - 1) * stride < nvec; v += ZS_CHAIN_UNROLL * stride) {
-        uint4 w[ZS_CHAIN_UNROLL];
-#pragma unroll
-        for (int u = 0; u < ZS_CHAIN_UNROLL; ++u) w[u] = __ldcs(in + v + u * stride);
-#pragma unroll
-        for (int u = 0; u < ZS_CHAIN_UNROLL; ++u) {
-            uint4 o;
-            o.x = zs_chain_px<CBRT, CUBE, CLAMP>(w[u].x, lut_lane, enc, a);
-            o.y = zs_chain_px<CBRT, CUBE, CLAMP>(w[u].y, lut_lane, enc, a);
-            o.z = zs_chain_px<CBRT, CUBE, CLAMP>(w[u].z, lut_lane, enc, a);
-            o.w = zs_chain_px<CBRT, CUBE, CLAMP>(w[u].w, lut_lane, enc, a);
-            __stcs(out + v + u * stride, o);
+    if (v + stride < nvec) {
+        // Software pipeline: the next two vectors are in flight while the current two are
+        // computed, so each thread keeps 32 bytes of reads outstanding at all times.
+        uint4 w0 = __ldcs(in + v), w1 = __ldcs(in + v + stride);
+        for (;;) {
+            const int64_t nx = v + 2 * stride;
+            const bool more = nx + stride < nvec;
+            uint4 n0 = w0, n1 = w1;
+            if (more) {
+                n0 = __ldcs(in + nx);
+                n1 = __ldcs(in + nx + stride);
+            }
+            zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG>(w0.x, w0.y, lut, lane4, enc_lane, a);
+            zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG>(w0.z, w0.w, lut, lane4, enc_lane, a);
+            __stcs(out + v, w0);
+            zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG>(w1.x, w1.y, lut, lane4, enc_lane, a);
+            zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG>(w1.z, w1.w, lut, lane4, enc_lane, a);
+            __stcs(out + v + stride, w1);
+            v = nx;
+            if (!more) break;
+            w0 = n0;
+            w1 = n1;
         }
     }
-    for (; v < nvec; v += stride) {
-        uint4 w = __ldcs(in + v), o;
-        o.x = zs_chain_px<CBRT, CUBE, CLAMP>(w.x, lut_lane, enc, a);
-        o.y = zs_chain_px<CBRT, CUBE, CLAMP>(w.y, lut_lane, enc, a);
-        o.z = zs_chain_px<CBRT, CUBE, CLAMP>(w.z, lut_lane, enc, a);
-        o.w = zs_chain_px<CBRT, CUBE, CLAMP>(w.w, lut_lane, enc, a);
-        __stcs(out + v, o);
+    if (v < nvec) {
+        uint4 w = __ldcs(in + v);
+        zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG>(w.x, w.y, lut, lane4, enc_lane, a);
+        zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG>(w.z, w.w, lut, lane4, enc_lane, a);
+        __stcs(out + v, w);
     }
-    // Tail pixels (npx not a multiple of 4).
+    // Tail pixels (npx not a multiple of 4): block 0, threads 0..3.
     const int64_t tail0 = nvec << 2;
     const int64_t t = tail0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (t < a.npx && t < tail0 + 4) {
         const uint32_t *in32 = reinterpret_cast<const uint32_t *>(a.src);
         uint32_t *out32 = reinterpret_cast<uint32_t *>(a.dst);
-        out32[t] = zs_chain_px<CBRT, CUBE, CLAMP>(in32[t], lut_lane, enc, a);
+        uint32_t p = in32[t], q = p;
+        zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG>(p, q, lut, lane4, enc_lane, a);
+        out32[t] = p;
     }
 }
 
 namespace zs {
 
-template <bool CBRT, bool CUBE, bool CLAMP>
+template <bool CBRT, bool CUBE, bool CLAMP, bool NONNEG>
 static cudaError_t launch_chain_t(const ZsChainArgs &args, int sm_count, cudaStream_t stream) {
+    auto kernel = zs_chain_srgb8_kernel<CBRT, CUBE, CLAMP, NONNEG>;
     const size_t smem = sizeof(ZsChainSmem);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaError_t e = cudaFuncSetAttribute(zs_chain_srgb8_kernel<CBRT, CUBE, CLAMP>,
-                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    static int per_sm = 0;
+    if (per_sm == 0) {
+        cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        attr_set = true;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, ZS_CHAIN_THREADS, smem);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) per_sm = 1;
     }
-    int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, zs_chain_srgb8_kernel<CBRT, CUBE, CLAMP>,
-                                                                  ZS_CHAIN_THREADS, smem);
-    if (e != cudaSuccess) return e;
-    if (per_sm < 1) per_sm = 1;
     const int64_t nvec = (args.npx + 3) / 4;
     int64_t blocks = (nvec + ZS_CHAIN_THREADS - 1) / ZS_CHAIN_THREADS;
     const int64_t cap = (int64_t)(sm_count > 0 ? sm_count : 148) * per_sm;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
-    zs_chain_srgb8_kernel<CBRT, CUBE, CLAMP><<<(unsigned)blocks, ZS_CHAIN_THREADS, smem, stream>>>(args);
+    kernel<<<(unsigned)blocks, ZS_CHAIN_THREADS, smem, stream>>>(args);
     g_kernel_launches.fetch_add(1);
     return cudaGetLastError();
+}
+
+template <bool NONNEG>
+static cudaError_t launch_chain_n(const ZsChainArgs &args, int sm_count, cudaStream_t stream) {
+    const bool cb = args.flags & ZS_CHAIN_CBRT, cu = args.flags & ZS_CHAIN_CUBE, cl = args.flags & ZS_CHAIN_CLAMP;
+    if (cb && cu && cl) return launch_chain_t<true, true, true, NONNEG>(args, sm_count, stream);
+    if (cb && cu && !cl) return launch_chain_t<true, true, false, NONNEG>(args, sm_count, stream);
+    if (cb && !cu && cl) return launch_chain_t<true, false, true, NONNEG>(args, sm_count, stream);
+    if (cb && !cu && !cl) return launch_chain_t<true, false, false, NONNEG>(args, sm_count, stream);
+    if (!cb && cu && cl) return launch_chain_t<false, true, true, NONNEG>(args, sm_count, stream);
+    if (!cb && cu && !cl) return launch_chain_t<false, true, false, NONNEG>(args, sm_count, stream);
+    if (!cb && !cu && cl) return launch_chain_t<false, false, true, NONNEG>(args, sm_count, stream);
+    return launch_chain_t<false, false, false, NONNEG>(args, sm_count, stream);
 }
 
 cudaError_t launch_chain(const ZsChainArgs &args, uint8_t src_fast, uint8_t dst_fast, int sm_count,
                          cudaStream_t stream) {
     if (src_fast != ZS_FAST_RGBA8_SRGB || dst_fast != ZS_FAST_RGBA8_SRGB) return cudaErrorNotSupported;
     if (args.npx <= 0) return cudaSuccess;
-    const bool cb = args.flags & ZS_CHAIN_CBRT, cu = args.flags & ZS_CHAIN_CUBE, cl = args.flags & ZS_CHAIN_CLAMP;
-    if (cb && cu && cl) return launch_chain_t<true, true, true>(args, sm_count, stream);
-    if (cb && cu && !cl) return launch_chain_t<true, true, false>(args, sm_count, stream);
-    if (cb && !cu && cl) return launch_chain_t<true, false, true>(args, sm_count, stream);
-    if (cb && !cu && !cl) return launch_chain_t<true, false, false>(args, sm_count, stream);
-    if (!cb && cu && cl) return launch_chain_t<false, true, true>(args, sm_count, stream);
-    if (!cb && cu && !cl) return launch_chain_t<false, true, false>(args, sm_count, stream);
-    if (!cb && !cu && cl) return launch_chain_t<false, false, true>(args, sm_count, stream);
-    return launch_chain_t<false, false, false>(args, sm_count, stream);
+    if ((args.flags & ZS_CHAIN_CBRT_NONNEG) || !(args.flags & ZS_CHAIN_CBRT))
+        return launch_chain_n<true>(args, sm_count, stream);
+    return launch_chain_n<false>(args, sm_count, stream);
 }
 
 }  // namespace zs

@@ -23,6 +23,7 @@
 namespace zs {
 std::atomic<uint64_t> g_kernel_launches{0};
 uint64_t kernel_launch_count() { return g_kernel_launches.load(); }
+void add_kernel_launches(uint64_t n) { g_kernel_launches.fetch_add(n); }
 }  // namespace zs
 
 __device__ __forceinline__ int zs_quad_src(int p, int t0, int t1, int s0, int s1) {

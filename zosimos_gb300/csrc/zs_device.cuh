@@ -18,6 +18,7 @@
 // device).  All device code is one translation unit (zs_device_all.cu).
 __device__ float zs_srgb_decode_lut[256];
 __device__ uint32_t zs_srgb_encode_tab[ZS_ENC_ENTRIES];
+__device__ uint32_t zs_srgb_encode_tab_shifted[ZS_ENCS_ENTRIES];
 
 // ---------------------------------------------------------------- transfer functions
 

@@ -8,7 +8,7 @@
 namespace zs {
 
 // Exact sRGB8 tables (zs_tables.cu).
-void build_srgb_tables(float *decode, uint32_t *encode);
+void build_srgb_tables(float *decode, uint32_t *encode, uint32_t *encode_shifted);
 cudaError_t init_device_tables(int device);
 
 // Generic raster launch: producer + fused pixel program + store (k_raster.cu).
@@ -21,5 +21,7 @@ cudaError_t launch_chain(const ZsChainArgs &args, uint8_t src_fast, uint8_t dst_
 
 // Number of kernel launches issued since process start (instrumentation for the bench).
 uint64_t kernel_launch_count();
+// Kernels launched through a replayed CUDA graph (counted on the host at replay).
+void add_kernel_launches(uint64_t n);
 
 }  // namespace zs

@@ -127,8 +127,9 @@ struct ZsChainArgs {
     uint8_t *dst;
     int64_t npx;          // pixels (flat: the chain is pixel-local)
     float m[4][9];
-    int32_t flags;        // bit0 cbrt, bit1 cube, bit2 clamp, bit3..6 matrix present
+    int32_t flags;        // ZS_CHAIN_* bits
     int32_t pad;
+    float m2[4][9][2];    // the same matrices with every coefficient duplicated (f32x2 operands)
 };
 
 enum {
@@ -138,10 +139,16 @@ enum {
     ZS_CHAIN_MA = 8,
     ZS_CHAIN_MB = 16,
     ZS_CHAIN_MC = 32,
-    ZS_CHAIN_MD = 64
+    ZS_CHAIN_MD = 64,
+    ZS_CHAIN_CBRT_NONNEG = 128   // M_a maps [0,1]^3 to non-negative values: no sign handling
 };
 
 // Entry count of the exact sRGB8 encode table: buckets of the float bit pattern
 // (bits >> 16) for x in [2^-13, 1], each holding at most one rounding threshold.
 #define ZS_ENC_BASE (114u << 7)
 #define ZS_ENC_ENTRIES 1665
+// The same encode for x' = saturate(x) + 2^-12, which lies in [2^-12, 1 + 2^-12] and
+// needs no integer clamp: buckets (bits(x') >> 16) - ZS_ENCS_BASE.
+#define ZS_ENCS_BASE (115u << 7)
+#define ZS_ENCS_ENTRIES 1537
+#define ZS_ENCS_SHIFT 0x39800000u   /* bits of 2^-12 */

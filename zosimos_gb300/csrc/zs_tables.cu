@@ -35,17 +35,17 @@ static uint32_t fbits(float f) {
     return b;
 }
 
-void build_srgb_tables(float *decode, uint32_t *encode) {
-    for (int v = 0; v < 256; ++v) decode[v] = (float)eotf_srgb(v / 255.0);
+// Bucketed threshold table: entry j covers the floats whose bits >> 16 == base + j.
+static void build_encode(uint32_t *encode, uint32_t entries, uint32_t base, double shift) {
     uint32_t thr[255];
     for (int k = 0; k < 255; ++k) {
-        double x = eotf_srgb((k + 0.5) / 255.0);
+        double x = eotf_srgb((k + 0.5) / 255.0) + shift;
         float f = (float)x;
         if ((double)f < x) f = std::nextafter(f, 2.0f);
         thr[k] = fbits(f);
     }
-    for (uint32_t j = 0; j < ZS_ENC_ENTRIES; ++j) {
-        uint32_t start = (j + ZS_ENC_BASE) << 16, end = start + 0x10000u;
+    for (uint32_t j = 0; j < entries; ++j) {
+        uint32_t start = (j + base) << 16, end = start + 0x10000u;
         uint32_t code = 0, inside = 0, nin = 0;
         for (int k = 0; k < 255; ++k) {
             if (thr[k] <= start) code = (uint32_t)k + 1;
@@ -57,6 +57,13 @@ void build_srgb_tables(float *decode, uint32_t *encode) {
     }
 }
 
+void build_srgb_tables(float *decode, uint32_t *encode, uint32_t *encode_shifted) {
+    for (int v = 0; v < 256; ++v) decode[v] = (float)eotf_srgb(v / 255.0);
+    build_encode(encode, ZS_ENC_ENTRIES, ZS_ENC_BASE, 0.0);
+    // x' = x + 2^-12 (x in [0, 1]); thresholds move by the same exact shift.
+    build_encode(encode_shifted, ZS_ENCS_ENTRIES, ZS_ENCS_BASE, 1.0 / 4096.0);
+}
+
 static std::mutex g_tables_mutex;
 static std::vector<int> g_tables_ready;
 
@@ -66,10 +73,10 @@ cudaError_t init_device_tables(int device) {
     if ((int)g_tables_ready.size() <= device) g_tables_ready.resize(device + 1, 0);
     if (g_tables_ready[device]) return cudaSuccess;
     static float dec[256];
-    static uint32_t enc[ZS_ENC_ENTRIES];
+    static uint32_t enc[ZS_ENC_ENTRIES], encs[ZS_ENCS_ENTRIES];
     static bool built = false;
     if (!built) {
-        build_srgb_tables(dec, enc);
+        build_srgb_tables(dec, enc, encs);
         built = true;
     }
     int prev = 0;
@@ -78,6 +85,7 @@ cudaError_t init_device_tables(int device) {
     if (prev != device && (e = cudaSetDevice(device)) != cudaSuccess) return e;
     e = cudaMemcpyToSymbol(zs_srgb_decode_lut, dec, sizeof(dec));
     if (e == cudaSuccess) e = cudaMemcpyToSymbol(zs_srgb_encode_tab, enc, sizeof(enc));
+    if (e == cudaSuccess) e = cudaMemcpyToSymbol(zs_srgb_encode_tab_shifted, encs, sizeof(encs));
     if (prev != device) cudaSetDevice(prev);
     if (e == cudaSuccess) g_tables_ready[device] = 1;
     return e;
