@@ -270,3 +270,69 @@ def ours_chain(img, mode=zs.Mode.Fused):
     pool = Pool()
     k = pool.insert_srgb(img)
     return run(c, pool, [(i, k)], [o], mode)[0]
+
+
+# ---------------------------------------------------------------- decode / blend / resize (two images)
+
+from zosimos_gb300.workloads import blend_resize  # noqa: E402
+
+
+def ours_blend_resize(img_a, img_b, out=(384, 384), mode=zs.Mode.Fused):
+    h, w = img_a.shape[:2]
+    c, a, b, o = blend_resize(w, h, *out)
+    pool = Pool()
+    ka, kb = pool.insert_srgb(img_a), pool.insert_srgb(img_b)
+    return run(c, pool, [(a, ka), (b, kb)], [o], mode)[0]
+
+
+def oracle_blend_resize(img_a, img_b, out=(384, 384)):
+    h, w = img_a.shape[:2]
+    la = O.decode(O.SRGB_RGBA8, rgba_bytes(img_a), w, h)
+    lb = O.decode(O.SRGB_RGBA8, rgba_bytes(img_b), w, h)
+    O.blend(la, lb, (0, 0), "Over", straight=True)
+    canvas = np.zeros((out[1], out[0], 4))
+    aff = Affine.new(AffineSample.BiLinear).scale(out[0] / w, out[1] / h)
+    O.affine(canvas, la, inv3_f32(aff.transformation), True)
+    return O.encode(O.SRGB_RGBA8, canvas)
+
+
+# ---------------------------------------------------------------- resample sweep (RGBA16F)
+
+from zosimos_gb300.workloads import resample as resample_cmds, rotation as rotation_cmds  # noqa: E402
+
+
+def f16_bytes(img: np.ndarray) -> np.ndarray:
+    h, w = img.shape[:2]
+    return np.ascontiguousarray(img.astype(np.float16)).view(np.uint8).reshape(h, w * 8)
+
+
+def f16_from_bytes(b: np.ndarray, w: int, h: int) -> np.ndarray:
+    return np.ascontiguousarray(b).view(np.float16).reshape(h, w, 4).astype(np.float64)
+
+
+def ours_resample(img16, out, filt, mode=zs.Mode.Fused):
+    h, w = img16.shape[:2]
+    c, i, o = resample_cmds(w, h, out[0], out[1], filt)
+    pool = Pool()
+    k = pool.insert(Descriptor.linear_rgba_f16(w, h), f16_bytes(img16))
+    return f16_from_bytes(run(c, pool, [(i, k)], [o], mode)[0], out[0], out[1])
+
+
+def oracle_resample(img16, out, filt):
+    return O.resample(img16.astype(np.float64), out[0], out[1], filt)
+
+
+def ours_rotation(img16, degrees, mode=zs.Mode.Fused):
+    h, w = img16.shape[:2]
+    c, i, o, _ = rotation_cmds(w, h, degrees)
+    pool = Pool()
+    k = pool.insert(Descriptor.linear_rgba_f16(w, h), f16_bytes(img16))
+    return f16_from_bytes(run(c, pool, [(i, k)], [o], mode)[0], w, h)
+
+
+def oracle_rotation(img16, degrees):
+    h, w = img16.shape[:2]
+    _, _, _, rot = rotation_cmds(w, h, degrees)
+    canvas = np.zeros((h, w, 4))
+    O.affine(canvas, img16.astype(np.float64), inv3_f32(rot.transformation), True)
+    return canvas

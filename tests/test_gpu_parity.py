@@ -128,3 +128,52 @@ def test_lab_grid(space, goldens):
     ours = P.ours_lab_grid(space)
     assert maxdiff(ours, P.oracle_lab_grid(space)) <= LSB
     assert blockhash256(ours.reshape(400, 400, 4)) in goldens[space]
+
+
+@pytest.mark.parametrize("mode", [zs.Mode.Fused, zs.Mode.PerOpF32, zs.Mode.PerOpF16])
+def test_blend_resize(mode):
+    a = srgb_gradient_noise(512, 512, seed=1, image=0)
+    b = srgb_gradient_noise(512, 512, seed=1, image=1)
+    ours = P.ours_blend_resize(a, b, mode=mode)
+    assert maxdiff(ours, P.oracle_blend_resize(a, b)) <= LSB
+
+
+F16_TOL = 2.0e-3   # max-abs error of RGBA16F outputs in [0, 1] against FP64 (f16 storage ~4.9e-4/step)
+
+
+@pytest.mark.parametrize("filt", [zs.Filter.Lanczos3, zs.Filter.Box, zs.Filter.Triangle])
+@pytest.mark.parametrize("factor", [2.0, 3.7, 8.0])
+@pytest.mark.parametrize("mode", [zs.Mode.Fused, zs.Mode.PerOpF32])
+def test_resample(filt, factor, mode):
+    from zosimos_gb300.synthetic import linear_gradient_gauss
+    img = linear_gradient_gauss(1024, 768, seed=3)
+    out = (int(round(1024 / factor)), int(round(768 / factor)))
+    ours = P.ours_resample(img, out, filt, mode)
+    ref = P.oracle_resample(img, out, filt)
+    assert ours.shape == ref.shape
+    assert np.abs(ours - ref).max() <= F16_TOL
+
+
+def test_resample_upscale():
+    from zosimos_gb300.synthetic import linear_gradient_gauss
+    img = linear_gradient_gauss(100, 60, seed=5)
+    ours = P.ours_resample(img, (317, 200), zs.Filter.Lanczos3)
+    assert np.abs(ours - P.oracle_resample(img, (317, 200), zs.Filter.Lanczos3)).max() <= F16_TOL
+
+
+@pytest.mark.parametrize("mode", [zs.Mode.Fused, zs.Mode.PerOpF32])
+def test_rotation(mode):
+    from zosimos_gb300.synthetic import linear_gradient_gauss
+    img = linear_gradient_gauss(640, 480, seed=3)
+    ours = P.ours_rotation(img, 17.0, mode)
+    ref = P.oracle_rotation(img, 17.0)
+    # coverage (pixel centre inside the rotated quad) is decided in identical f32 arithmetic
+    assert ((ours[..., 3] == 0) == (ref[..., 3] == 0)).all()
+    assert np.abs(ours - ref).max() <= F16_TOL
+
+
+def test_blend_resize_plan():
+    c, _, _, _ = P.blend_resize()
+    fused = zs.Linker.from_included().compile(c).lower_to()
+    plain = zs.Linker.from_included().compile(c).lower_to(zs.Capabilities(mode=zs.Mode.PerOpF32))
+    assert fused.kernel_count() < plain.kernel_count()

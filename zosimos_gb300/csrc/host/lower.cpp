@@ -159,6 +159,13 @@ struct Planner {
             const int gather_src = (pr == ZS_PR_QUAD || pr == ZS_PR_AFFINE) ? 1 : 0;
             same = format_equal(p.a.src[gather_src].fmt, d.fmt) && p.a.src[gather_src].fmt.bpp == d.fmt.bpp;
             if (p.a.has_below) same = same && format_equal(p.a.src[0].fmt, d.fmt);
+            if ((pr == ZS_PR_QUAD || pr == ZS_PR_AFFINE) && !p.a.has_below) {
+                // Uncovered pixels take the constant canvas colour: zero bytes only when
+                // the colour is zero and the format stores zero as zero bytes.
+                const bool zero = p.a.cons[0] == 0.f && p.a.cons[1] == 0.f && p.a.cons[2] == 0.f && p.a.cons[3] == 0.f;
+                const bool plain = d.fmt.fast != ZS_FAST_GENERIC;
+                same = same && zero && plain;
+            }
             st.raster.raw_copy = same ? 1 : 0;
         }
         try_chain(st);
@@ -244,14 +251,46 @@ struct Planner {
             p->label += " + " + label;
             return p;
         }
-        materialize(reg);
+        need(reg);
         const Desc &d = desc(reg);
         auto p = new_pending(ZS_PR_LOAD, d.width, d.height, label);
         set_src(*p, 0, reg);
         return p;
     }
 
-    void need(uint32_t reg) { materialize(reg); }
+    // A source operand must be readable from a buffer.  A pending value that is just the
+    // decode of one buffer (LOAD with an empty program, e.g. sRGB8 -> linear FP32 whose
+    // matrix folded to the identity) is forwarded to that buffer instead of being stored.
+    void need(uint32_t reg) {
+        Val &v = vals[reg];
+        if (!v.materialized && v.pend && out_slot_of[reg] < 0 && v.pend->a.producer == ZS_PR_LOAD &&
+            v.pend->a.nsrc == 1) {
+            HProgram p = v.pend->prog;
+            p.optimise();
+            if (p.ins.empty()) {
+                v.materialized = true;
+                v.slot = v.pend->src_slot[0];
+                v.fmt = v.pend->a.src[0].fmt;
+                v.pend.reset();
+                return;
+            }
+        }
+        materialize(reg);
+    }
+
+    // A register that is a still-pending solid colour whose program is empty (its
+    // declared texel does not quantise it): its value is the constant itself.
+    bool solid_value(uint32_t reg, float out[4]) {
+        Val &v = vals[reg];
+        if (E.mode != ZS_MODE_FUSED || v.materialized || !v.pend || v.pend->a.producer != ZS_PR_SOLID ||
+            out_slot_of[reg] >= 0)
+            return false;
+        HProgram p = v.pend->prog;
+        p.optimise();
+        if (!p.ins.empty()) return false;
+        for (int k = 0; k < 4; ++k) out[k] = v.pend->a.cons[k];
+        return true;
+    }
 
     void set_pending(uint32_t reg, std::unique_ptr<Pending> p) {
         Val &v = vals[reg];
@@ -404,12 +443,21 @@ struct Planner {
             case OpKind::Affine: {
                 use(op.a);
                 use(op.b);
-                need(op.a);
                 need(op.b);
                 auto p = new_pending(ZS_PR_AFFINE, d.width, d.height, op.u0 ? "affine bilinear" : "affine nearest");
-                set_src(*p, 0, op.a);
+                float solid[4];
+                if (solid_value(op.a, solid)) {
+                    // Painting onto a constant canvas: the canvas is never stored.
+                    p->a.has_below = 0;
+                    for (int k = 0; k < 4; ++k) p->a.cons[k] = solid[k];
+                    p->label = "solid canvas + " + p->label;
+                    p->a.nsrc = 2;
+                } else {
+                    need(op.a);
+                    set_src(*p, 0, op.a);
+                    p->a.has_below = 1;
+                }
                 set_src(*p, 1, op.b);
-                p->a.has_below = 1;
                 p->a.bilinear = (uint8_t)op.u0;
                 Mat3 fwd{};
                 for (int k = 0; k < 9; ++k) fwd.m[k] = op.fparams[k];

@@ -103,7 +103,9 @@ __global__ void __launch_bounds__(256) zs_raster_kernel(const __grid_constant__ 
                     r = zs_load_px(s0, x, y);
                 }
             } else if (a.raw_copy) {
-                is_raw = true;
+                is_raw = true;                      // zero canvas: zero bytes
+            } else {
+                r = make_float4(a.cons[0], a.cons[1], a.cons[2], a.cons[3]);   // constant canvas
             }
         } break;
         case ZS_PR_AFFINE: {
@@ -136,7 +138,9 @@ __global__ void __launch_bounds__(256) zs_raster_kernel(const __grid_constant__ 
                     r = zs_load_px(s0, x, y);
                 }
             } else if (a.raw_copy) {
-                is_raw = true;
+                is_raw = true;                      // zero canvas: zero bytes
+            } else {
+                r = make_float4(a.cons[0], a.cons[1], a.cons[2], a.cons[3]);   // constant canvas
             }
         } break;
         case ZS_PR_PALETTE: {

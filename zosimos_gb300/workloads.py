@@ -35,3 +35,50 @@ def color_chain(w: int, h: int):
     out = c.color_convert(d65, src)
     o, _ = c.output(out)
     return c, i, o
+
+
+def blend_resize(w: int = 512, h: int = 512, out_w: int = 384, out_h: int = 384):
+    """Two RGBA8 sRGB images: decode to linear FP32, alpha-over B onto A, bilinear affine
+    resize (scale out/in) onto a transparent canvas, sRGB encode to RGBA8.
+    Returns (commands, input A, input B, output register)."""
+    from . import Affine, AffineSample, Blend, Rectangle
+    c = CommandBuffer()
+    src = Descriptor.srgb_rgba8(w, h)
+    a = c.input(src)
+    b = c.input(src)
+    la = c.color_convert(a, Descriptor.linear_rgba_f32(w, h))
+    lb = c.color_convert(b, Descriptor.linear_rgba_f32(w, h))
+    over = c.blend(la, Rectangle(0, 0, w, h), lb, Blend.Alpha)
+    canvas = c.solid_rgba(Descriptor.linear_rgba_f32(out_w, out_h), [0.0, 0.0, 0.0, 0.0])
+    scale = Affine.new(AffineSample.BiLinear).scale(out_w / w, out_h / h)
+    resized = c.affine(canvas, scale, over)
+    out = c.color_convert(resized, Descriptor.srgb_rgba8(out_w, out_h))
+    o, _ = c.output(out)
+    return c, a, b, o
+
+
+def resample(w: int, h: int, out_w: int, out_h: int, filt: int):
+    """RGBA16F linear image -> separable filtered resize (Box / Lanczos3 / Triangle) ->
+    RGBA16F.  Returns (commands, input, output)."""
+    c = CommandBuffer()
+    i = c.input(Descriptor.linear_rgba_f16(w, h))
+    r = c.resize_filtered(i, (out_w, out_h), filt)
+    o, _ = c.output(r)
+    return c, i, o
+
+
+def rotation(w: int, h: int, degrees: float):
+    """RGBA16F linear image rotated about its centre (bilinear) onto a transparent canvas
+    of the same size.  Returns (commands, input, output)."""
+    import math
+
+    from . import Affine, AffineSample
+    c = CommandBuffer()
+    d = Descriptor.linear_rgba_f16(w, h)
+    i = c.input(d)
+    canvas = c.solid_rgba(d, [0.0, 0.0, 0.0, 0.0])
+    rot = (Affine.new(AffineSample.BiLinear).shift(-w / 2.0, -h / 2.0).rotate(math.radians(degrees))
+           .shift(w / 2.0, h / 2.0))
+    r = c.affine(canvas, rot, i)
+    o, _ = c.output(r)
+    return c, i, o, rot
