@@ -277,6 +277,21 @@ int zs_batch_thumbnails(zs_executable *chain, const void *const *images, const u
                         const uint32_t *heights, uint32_t n, uint32_t canvas, void *out,
                         void *stream);
 
+/* ---- resample without any device allocation ------------------------------------ */
+/* No counterpart in the reference.  For callers that may not allocate device memory
+ * while they run (a pre-budgeted host application, a plugin inside someone else's
+ * allocator, a latency-critical loop): the separable resample of
+ * zs_cmd_resize_filtered for tightly packed RGBA16F linear images, with src/dst
+ * supplied by the caller and every temporary (filter tables, FP16 intermediate) kept
+ * in one fixed 32 MiB device array per GPU.  Calls that need more than that array
+ * (tables + dst_width * src_height * 8 bytes) return ZS_ERR_INVALID_ARG.  All calls on
+ * a device share the array: calls that overlap on the GPU race, so order them on one
+ * stream.  The first call on a device resolves the array's address for the current
+ * device; make it before any stream capture.  filter: 0 Box, 1 Lanczos-3, 2 Triangle;
+ * stream may be null (the legacy default stream). */
+int zs_resample_rgba16f_noalloc(const void *src, uint32_t src_width, uint32_t src_height, void *dst,
+                                uint32_t dst_width, uint32_t dst_height, uint32_t filter, void *stream);
+
 /* Number of kernels this library has launched since the process started. */
 uint64_t zs_kernel_launch_count(void);
 

@@ -5,3 +5,4 @@
 #include "k_raster.cu"
 #include "k_chain.cu"
 #include "k_batch.cu"
+#include "k_noalloc.cu"
