@@ -252,6 +252,10 @@ from zosimos_gb300.workloads import OKLAB_SCALE, color_chain as chain_commands  
 
 def oracle_chain(img, f32=False):
     """The same chain, one full pass per op (f32=True: the plain per-op CPU pipeline)."""
+    return O.encode(O.SRGB_RGBA8, oracle_chain_linear(img, f32), f32=f32)
+
+
+def oracle_chain_linear(img, f32=False):
     h, w = img.shape[:2]
     x = O.decode(O.SRGB_RGBA8, rgba_bytes(img), w, h, f32=f32)
     a1 = np.linalg.inv(O.rgb_to_xyz("Bt709", "D50")) @ O.adaptation("BradfordVonKries", "D65", "D50") @ O.rgb_to_xyz()
@@ -261,7 +265,46 @@ def oracle_chain(img, f32=False):
     O.oklab_decode(x, np.linalg.inv(O.rgb_to_xyz("Bt709", "D50")), f32=f32)
     a2 = np.linalg.inv(O.rgb_to_xyz()) @ O.adaptation("BradfordVonKries", "D50", "D65") @ O.rgb_to_xyz("Bt709", "D50")
     O.mat3(x, a2, f32=f32)
-    return O.encode(O.SRGB_RGBA8, x, f32=f32)
+    return x
+
+
+# ---------------------------------------------------------------- batched uneven thumbnails (config 4)
+
+
+def fit_size(w, h, canvas):
+    if w >= h:
+        return canvas, max(1, int(round(h * canvas / w)))
+    return max(1, int(round(w * canvas / h))), canvas
+
+
+def oracle_thumbnails(images, canvas=256):
+    out = []
+    for img in images:
+        h, w = img.shape[:2]
+        tw, th = fit_size(w, h, canvas)
+        lin = oracle_chain_linear(img)
+        small = O.resample(lin, tw, th, "Box")
+        full = np.zeros((canvas, canvas, 4))
+        x0, y0 = (canvas - tw) // 2, (canvas - th) // 2
+        full[y0:y0 + th, x0:x0 + tw] = small
+        out.append(O.encode(O.SRGB_RGBA8, full))
+    return out
+
+
+def ours_thumbnails(images, canvas=256):
+    c, _, _ = chain_commands(1, 1)
+    exe = zs.Linker.from_included().compile(c).lower_to()
+    bufs = []
+    for img in images:
+        b = zs.DeviceBuffer(img.nbytes)
+        b.upload(rgba_bytes(img))
+        bufs.append(b)
+    out = zs.DeviceBuffer(len(images) * canvas * canvas * 4)
+    exe.batch_thumbnails([b.ptr for b in bufs], [im.shape[1] for im in images], [im.shape[0] for im in images],
+                         canvas, out.ptr)
+    zs.device_synchronize()
+    res = out.download(np.empty((len(images), canvas, canvas * 4), np.uint8))
+    return [res[i] for i in range(len(images))]
 
 
 def ours_chain(img, mode=zs.Mode.Fused):
@@ -336,3 +379,27 @@ def oracle_rotation(img16, degrees):
     canvas = np.zeros((h, w, 4))
     O.affine(canvas, img16.astype(np.float64), inv3_f32(rot.transformation), True)
     return canvas
+
+
+# ---------------------------------------------------------------- layer compositing stack
+
+from zosimos_gb300.workloads import BLEND_CYCLE, layer_affine, layer_stack  # noqa: E402
+
+
+def ours_layer_stack(layers16, transforms, mode=zs.Mode.Fused):
+    h, w = layers16[0].shape[:2]
+    c, inputs, o = layer_stack(w, h, transforms)
+    pool = Pool()
+    d16 = Descriptor.linear_rgba_f16(w, h).with_color(alpha=1)
+    binds = [(reg, pool.insert(d16, f16_bytes(img))) for reg, img in zip(inputs, layers16)]
+    return f16_from_bytes(run(c, pool, binds, [o], mode)[0], w, h)
+
+
+def oracle_layer_stack(layers16, transforms):
+    h, w = layers16[0].shape[:2]
+    acc = np.zeros((h, w, 4))
+    for i, (img, (deg, s)) in enumerate(zip(layers16, transforms)):
+        placed = np.zeros((h, w, 4))
+        O.affine(placed, img.astype(np.float64), inv3_f32(layer_affine(w, h, deg, s).transformation), True)
+        O.blend(acc, placed, (0, 0), BLEND_CYCLE[i % 4], straight=False)
+    return acc

@@ -172,6 +172,35 @@ def test_rotation(mode):
     assert np.abs(ours - ref).max() <= F16_TOL
 
 
+@pytest.mark.parametrize("mode", [zs.Mode.Fused, zs.Mode.PerOpF32])
+def test_layer_stack(mode):
+    from zosimos_gb300.synthetic import layer_transforms, premultiplied_layer
+    n, w, h = 6, 384, 256
+    layers = [premultiplied_layer(w, h, seed=5, image=i) for i in range(n)]
+    transforms = layer_transforms(n, seed=5)
+    ours = P.ours_layer_stack(layers, transforms, mode)
+    ref = P.oracle_layer_stack(layers, transforms)
+    assert np.abs(ours - ref).max() <= F16_TOL
+
+
+def test_layer_stack_is_one_kernel():
+    from zosimos_gb300.synthetic import layer_transforms
+    c, _, _ = P.layer_stack(256, 256, layer_transforms(32))
+    exe = zs.Linker.from_included().compile(c).lower_to()
+    assert exe.kernel_count() == 1 and "32 layers" in exe.describe()
+
+
+def test_batch_thumbnails():
+    from zosimos_gb300.synthetic import thumbnail_sizes
+    ws, hs = thumbnail_sizes(10, seed=4, lo=40, hi=700)
+    images = [srgb_gradient_noise(int(w), int(h), seed=4, image=i) for i, (w, h) in enumerate(zip(ws, hs))]
+    images.append(srgb_gradient_noise(100, 60, seed=4, image=99))     # upscale case
+    ours = P.ours_thumbnails(images, 256)
+    ref = P.oracle_thumbnails(images, 256)
+    for o, r in zip(ours, ref):
+        assert maxdiff(o, r) <= LSB
+
+
 def test_blend_resize_plan():
     c, _, _, _ = P.blend_resize()
     fused = zs.Linker.from_included().compile(c).lower_to()

@@ -1,0 +1,172 @@
+"""Host-side behaviour of the C ABI that needs no GPU: the library loads and exports
+every symbol include/zosimos.h declares; command type checks mirror the reference's
+CommandBuffer errors (lib/zosimos/src/command.rs); compile/lower plans have the
+expected shape (fusion) -- lowering is host work and runs without a device."""
+import math
+import os
+import re
+
+import numpy as np
+import pytest
+
+import zosimos_gb300 as zs
+from zosimos_gb300 import (Affine, AffineSample, Bits, ColorKind, CommandBuffer, Descriptor, Linker, Parts,
+                           Rectangle, Transfer, Whitepoint, ZosimosError)
+from zosimos_gb300.workloads import blend_resize, color_chain, resample, rotation
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_symbols():
+    text = open(os.path.join(ROOT, "include", "zosimos.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(zs_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol():
+    lib = zs._lib()
+    missing = [s for s in header_symbols() if not hasattr(lib, s)]
+    assert not missing, missing
+    assert len(header_symbols()) > 60
+
+
+def test_library_path_is_in_tree():
+    assert zs.library_path().startswith(os.path.join(ROOT, "zosimos_gb300"))
+
+
+def lower(c, mode=zs.Mode.Fused):
+    return Linker.from_included().compile(c).lower_to(zs.Capabilities(mode=mode))
+
+
+def test_colour_chain_fuses_to_one_kernel():
+    c, _, _ = color_chain(4096, 4096)
+    fused = lower(c)
+    assert fused.kernel_count() == 1 and "fused chain kernel" in fused.describe()
+    assert lower(c, zs.Mode.PerOpF32).kernel_count() == 7
+    assert lower(c, zs.Mode.PerOpF16).kernel_count() == 7
+
+
+def test_blend_resize_plan():
+    c, _, _, _ = blend_resize()
+    assert lower(c).kernel_count() == 2          # blend, affine + encode (canvas never stored)
+    assert lower(c, zs.Mode.PerOpF32).kernel_count() == 6
+
+
+def test_resample_and_rotation_plans():
+    c, _, _ = resample(1024, 768, 512, 384, zs.Filter.Lanczos3)
+    assert lower(c).kernel_count() == 2
+    c, _, _, _ = rotation(640, 480, 17.0)
+    assert lower(c).kernel_count() == 1
+
+
+def test_inscribe_requires_upper_rectangle():
+    # command.rs:1196-1198
+    c = CommandBuffer()
+    b = c.input(Descriptor.srgb_rgba8(64, 64))
+    a = c.input(Descriptor.srgb_rgba8(16, 8))
+    with pytest.raises(ZosimosError) as e:
+        c.inscribe(b, Rectangle(4, 4, 20, 12), a)
+    assert e.value.code == 4
+    c.inscribe(b, Rectangle(0, 0, 16, 8), a)
+    c.inscribe_placed(b, Rectangle(4, 4, 20, 12), a)
+
+
+def test_inscribe_conflicting_types():
+    c = CommandBuffer()
+    b = c.input(Descriptor.srgb_rgba8(64, 64))
+    a = c.input(Descriptor.linear_rgba_f32(16, 8))
+    with pytest.raises(ZosimosError) as e:
+        c.inscribe(b, Rectangle(0, 0, 16, 8), a)
+    assert e.value.is_type_err
+
+
+def test_affine_rejects_degenerate_matrix():
+    c = CommandBuffer()
+    b = c.input(Descriptor.srgb_rgba8(64, 64))
+    a = c.input(Descriptor.srgb_rgba8(16, 8))
+    with pytest.raises(ZosimosError):
+        c.affine(b, Affine.new().scale(0.0, 1.0), a)
+    c.affine(b, Affine.new(AffineSample.BiLinear).rotate(math.pi / 4), a)
+
+
+def test_color_convert_needs_same_whitepoint():
+    c = CommandBuffer()
+    i = c.input(Descriptor.srgb_rgba8(8, 8))
+    with pytest.raises(ZosimosError):
+        c.color_convert(i, Descriptor.srgb_rgba8(8, 8).with_color(whitepoint=Whitepoint.D50))
+    c.color_convert(i, Descriptor.srgb_rgba8(8, 8).with_color(transfer=Transfer.Bt709))
+
+
+def test_bradford_nonlinear_is_unimplemented():
+    c = CommandBuffer()
+    i = c.input(Descriptor.srgb_rgba8(8, 8))
+    with pytest.raises(ZosimosError) as e:
+        c.chromatic_adaptation(i, zs.ChromaticAdaptationMethod.BradfordNonLinear, Whitepoint.D50)
+    assert e.value.code == 2
+
+
+def test_transmute_checks_texel_size():
+    c = CommandBuffer()
+    i = c.input(Descriptor.srgb_rgba8(8, 8))
+    with pytest.raises(ZosimosError):
+        c.transmute(i, Descriptor.linear_rgba_f16(8, 8))
+    c.transmute(i, Descriptor(8, 8, Bits.UInt16x2, Parts.LumaA))
+
+
+def test_blend_unimplemented_upstream_is_built_here():
+    c = CommandBuffer()
+    b = c.input(Descriptor.srgb_rgba8(8, 8))
+    a = c.input(Descriptor.srgb_rgba8(8, 8))
+    for mode in (zs.Blend.Alpha, zs.Blend.Multiply, zs.Blend.Screen, zs.Blend.Add):
+        c.blend(b, Rectangle(0, 0, 8, 8), a, mode)
+
+
+def test_inconsistent_descriptors_rejected():
+    assert not Descriptor(0, 8).is_consistent()
+    assert not Descriptor(8, 8, Bits.UInt8x4, Parts.RgbA, ColorKind.Oklab).is_consistent()
+    assert Descriptor(8, 8, Bits.UInt8x4, Parts.LchA, ColorKind.Oklab).is_consistent()
+    with pytest.raises(ZosimosError):
+        CommandBuffer().input(Descriptor(0, 8))
+
+
+def test_bad_register_and_missing_output():
+    c = CommandBuffer()
+    with pytest.raises(ZosimosError) as e:
+        c.crop(7, Rectangle(0, 0, 1, 1))
+    assert e.value.code == 3
+    c.input(Descriptor.srgb_rgba8(8, 8))
+    with pytest.raises(ZosimosError):
+        Linker.from_included().compile(c)          # no output
+
+
+def test_pool_roundtrip_and_binding_checks():
+    pool = zs.Pool()
+    img = (np.arange(8 * 8 * 4) % 251).astype(np.uint8).reshape(8, 8, 4)
+    k = pool.insert_srgb(img)
+    assert (pool.read(k).reshape(8, 8, 4) == img).all()
+    assert pool.descriptor(k).width == 8
+    c = CommandBuffer()
+    i = c.input(Descriptor.srgb_rgba8(8, 8))
+    o, _ = c.output(c.color_convert(i, Descriptor.linear_rgba_f32(8, 8)))
+    exe = Linker.from_included().compile(c).lower_to()
+    env = exe.from_pool(pool)
+    env.bind(i, k)
+    k2 = pool.insert_srgb(np.zeros((4, 4, 4), np.uint8))
+    with pytest.raises(ZosimosError) as e:
+        env.bind(i, k2)                     # StartError::MismatchedDescriptor
+    assert e.value.code == 6
+    with pytest.raises(ZosimosError) as e:
+        env.bind(o, k)                      # not an input register
+    assert e.value.code == 3
+    pool.remove(k2)
+    with pytest.raises(ZosimosError):
+        pool.remove(k2)
+
+
+def test_noalloc_rejects_oversized_without_device():
+    import ctypes
+    fn = zs._lib().zs_resample_rgba16f_noalloc
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_uint32,
+                   ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p]
+    fn.restype = ctypes.c_int32
+    assert fn(ctypes.c_void_p(16), 8192, 8192, ctypes.c_void_p(16), 4096, 4096, 1, None) == 10

@@ -549,6 +549,17 @@ class Executable:
         outs = (ctypes.c_void_p * len(outputs))(*[a.ctypes.data for a in outputs])
         _check(_lib().zs_run_host(self._h, ins, len(inputs), outs, len(outputs)))
 
+    def batch_thumbnails(self, images: Sequence[int], widths: Sequence[int], heights: Sequence[int], canvas: int,
+                         out: int, stream: int = 0) -> None:
+        """One persistent launch over many device-resident RGBA8 sRGB images: this
+        executable's fused colour chain, box fit-resize to `canvas`, centred on a
+        transparent canvas x canvas image; `out` receives n * canvas^2 * 4 bytes."""
+        n = len(images)
+        ptrs = (ctypes.c_void_p * n)(*images)
+        ws = (ctypes.c_uint32 * n)(*widths)
+        hs = (ctypes.c_uint32 * n)(*heights)
+        _check(_lib().zs_batch_thumbnails(self._h, ptrs, ws, hs, n, canvas, out, stream or None))
+
     def run_device(self, inputs: Sequence[int], outputs: Sequence[int], stream: int = 0) -> None:
         """One launch on device pointers (no host copies); graph-replayed when enabled."""
         ins = (ctypes.c_void_p * len(inputs))(*inputs)

@@ -27,6 +27,8 @@ struct Pending {
     int idx_x_slot = -1, idx_y_slot = -1, weight_slot = -1;
     HProgram prog;
     std::string label;
+    // ZS_PR_LAYERS: base (src_slot[0] when has_below, else a.cons[0..3]) and the layers.
+    std::vector<LayerRef> layers;
 };
 
 struct Val {
@@ -103,7 +105,73 @@ struct Planner {
         if (i + 1 > p.a.nsrc) p.a.nsrc = (uint8_t)(i + 1);
     }
 
+    void emit_layers(Pending &p, int dst_slot) {
+        Slot &d = E.slots[dst_slot];
+        p.prog.optimise();
+        while (!p.prog.ins.empty() && p.prog.ins.back().op == ZS_P_QUANT && format_equal(p.prog.ins.back().fa, d.fmt))
+            p.prog.ins.pop_back();
+        Step st;
+        st.kind = StepKind::Layers;
+        st.label = p.label;
+        st.dst_slot = dst_slot;
+        auto L = std::make_shared<ZsLayersArgs>();
+        std::memset(L.get(), 0, sizeof(ZsLayersArgs));
+        L->width = p.a.width;
+        L->height = p.a.height;
+        L->has_base = p.a.has_below;
+        if (p.a.has_below) {
+            st.base_slot = p.src_slot[0];
+            L->base = p.a.src[0];
+        } else {
+            for (int k = 0; k < 4; ++k) L->base_color[k] = p.a.cons[k];
+        }
+        L->dst_stride = d.stride;
+        L->dst_fmt = d.fmt;
+        int nf = 0;
+        auto fmt_id = [&](const ZsFormat &f) -> uint8_t {
+            for (int i = 0; i < nf; ++i)
+                if (format_equal(L->fmts[i], f)) return (uint8_t)i;
+            if (nf >= ZS_MAX_FMTS) fail(ZS_ERR_UNIMPLEMENTED, "too many formats in one layer stack");
+            L->fmts[nf] = f;
+            return (uint8_t)nf++;
+        };
+        L->nlayers = (int32_t)p.layers.size();
+        for (size_t i = 0; i < p.layers.size(); ++i) {
+            const LayerRef &lr = p.layers[i];
+            L->layers[i] = lr.proto;
+            if (lr.quant_sample) L->layers[i].quant_sample = (uint8_t)(fmt_id(lr.sample_fmt) + 1);
+            if (lr.quant_acc) L->layers[i].quant_acc = (uint8_t)(fmt_id(lr.acc_fmt) + 1);
+            st.layer_slots.push_back(lr.slot);
+        }
+        int np = 0;
+        for (const HInstr &hi : p.prog.ins) {
+            if (L->prog.n >= ZS_MAX_INSTR) fail(ZS_ERR_UNIMPLEMENTED, "fused program too long");
+            ZsPInstr &o = L->prog.ins[L->prog.n++];
+            o.op = hi.op;
+            o.a = hi.a;
+            o.b = hi.b;
+            o.p = (uint16_t)np;
+            if (hi.op == ZS_P_MAT3) {
+                for (int k = 0; k < 9; ++k) L->prog.prm[np++] = (float)hi.mat.m[k];
+            } else if (hi.op == ZS_P_QUANT) {
+                o.a = fmt_id(hi.fa);
+            } else if (hi.op == ZS_P_TRANSMUTE) {
+                o.a = fmt_id(hi.fa);
+                o.b = fmt_id(hi.fb);
+            } else if (hi.op == ZS_P_INJECT || hi.op == ZS_P_BLEND) {
+                fail(ZS_ERR_UNIMPLEMENTED, "binary op after a layer stack");
+            }
+        }
+        st.layers = L;
+        st.label += " [fused layer stack, " + std::to_string(p.layers.size()) + " layers]";
+        E.steps.push_back(st);
+    }
+
     void emit_step(Pending &p, int dst_slot) {
+        if (p.a.producer == ZS_PR_LAYERS) {
+            emit_layers(p, dst_slot);
+            return;
+        }
         Slot &d = E.slots[dst_slot];
         p.prog.optimise();
         // A trailing quantisation to the very format being stored is implied by the store.
@@ -287,13 +355,90 @@ struct Planner {
             return false;
         HProgram p = v.pend->prog;
         p.optimise();
-        if (!p.ins.empty()) return false;
+        // Quantising to the declared texel leaves 0 and 1 unchanged in every format.
+        bool exact = true;
+        for (int k = 0; k < 4; ++k) exact = exact && (v.pend->a.cons[k] == 0.0f || v.pend->a.cons[k] == 1.0f);
+        for (const HInstr &i : p.ins)
+            if (!(i.op == ZS_P_QUANT && exact && i.fa.fast != ZS_FAST_GENERIC)) return false;
         for (int k = 0; k < 4; ++k) out[k] = v.pend->a.cons[k];
+        return true;
+    }
+
+    // blend(acc, affine(constant canvas, A, layer)) at offset 0: append the layer to a
+    // layer stack instead of storing the transformed layer and the blended image.
+    bool try_layer(uint32_t r, const Op &op) {
+        if (E.mode != ZS_MODE_FUSED || op.rect.x != 0 || op.rect.y != 0) return false;
+        Val &tv = vals[op.b];
+        if (tv.materialized || !tv.pend || tv.pend->a.producer != ZS_PR_AFFINE || tv.pend->a.has_below ||
+            remaining[op.b] != 0 || out_slot_of[op.b] >= 0)
+            return false;
+        const Desc &d = P.ops[r].desc;
+        if (desc(op.b).width != d.width || desc(op.b).height != d.height) return false;
+        HProgram tp = tv.pend->prog;
+        tp.optimise();
+        if (tp.ins.size() > 1 || (tp.ins.size() == 1 && !(tp.ins[0].op == ZS_P_QUANT && tp.ins[0].fa.fast != ZS_FAST_GENERIC)))
+            return false;
+        // The accumulator side: extend its stack, start from a constant, or start from a buffer.
+        std::unique_ptr<Pending> p;
+        Val &av = vals[op.a];
+        float solid[4];
+        if (!av.materialized && av.pend && av.pend->a.producer == ZS_PR_LAYERS && remaining[op.a] == 0 &&
+            out_slot_of[op.a] < 0 && av.pend->prog.ins.empty() && av.pend->layers.size() < ZS_MAX_LAYERS) {
+            p = std::move(av.pend);
+            av.materialized = true;
+            av.slot = -1;
+        } else {
+            p = new_pending(ZS_PR_LAYERS, d.width, d.height, "layer stack");
+            if (solid_value(op.a, solid)) {
+                p->a.has_below = 0;
+                for (int k = 0; k < 4; ++k) p->a.cons[k] = solid[k];
+            } else {
+                need(op.a);
+                set_src(*p, 0, op.a);
+                p->a.has_below = 1;
+            }
+        }
+        const Pending &t = *tv.pend;
+        LayerRef lr;
+        lr.slot = t.src_slot[1];
+        lr.proto.stride = t.a.src[1].stride;
+        lr.proto.width = t.a.src[1].width;
+        lr.proto.height = t.a.src[1].height;
+        lr.proto.fmt = t.a.src[1].fmt;
+        for (int k = 0; k < 9; ++k) lr.proto.inv[k] = t.a.aff[k];
+        for (int k = 0; k < 4; ++k) lr.proto.canvas[k] = t.a.cons[k];
+        lr.proto.bilinear = t.a.bilinear;
+        lr.proto.mode = (uint8_t)op.u0;
+        lr.proto.straight = d.alpha == ZS_ALPHA_PREMULTIPLIED ? 0 : 1;
+        if (tp.ins.size() == 1) {
+            lr.quant_sample = true;
+            lr.sample_fmt = tp.ins[0].fa;
+        }
+        p->layers.push_back(lr);
+        tv.pend.reset();
+        tv.materialized = true;     // consumed by the stack
+        tv.slot = -1;
+        set_pending(r, std::move(p));
         return true;
     }
 
     void set_pending(uint32_t reg, std::unique_ptr<Pending> p) {
         Val &v = vals[reg];
+        if (p->a.producer == ZS_PR_LAYERS && p->prog.ins.empty() && !p->layers.empty()) {
+            // The declared texel of the blended result quantises the accumulator.
+            ZsFormat declared = format_of(desc(reg));
+            if (!format_is_lossless_f32(declared)) {
+                if (declared.fast == ZS_FAST_GENERIC) {
+                    p->prog.quant(declared);          // rare: ends the stack
+                } else {
+                    p->layers.back().quant_acc = true;
+                    p->layers.back().acc_fmt = declared;
+                }
+            }
+            v.pend = std::move(p);
+            v.materialized = false;
+            return;
+        }
         // The declared texel of the op's result bounds its precision (faithful semantics).
         ZsFormat declared = format_of(desc(reg));
         if (!format_is_lossless_f32(declared)) p->prog.quant(declared);
@@ -524,6 +669,7 @@ struct Planner {
             case OpKind::Blend: {
                 use(op.a);
                 use(op.b);
+                if (try_layer(r, op)) break;
                 need(op.a);
                 need(op.b);
                 auto p = new_pending(ZS_PR_BLEND, d.width, d.height, "blend");
@@ -647,7 +793,9 @@ std::unique_ptr<Executable> lower(const Program &prog, const zs_capabilities &ca
     os << "executable: " << E->steps.size() << " launches, mode " << E->mode << "\n";
     for (size_t i = 0; i < E->steps.size(); ++i) {
         const Step &s = E->steps[i];
-        os << "  [" << i << "] " << (s.kind == StepKind::Chain ? "chain" : s.kind == StepKind::Copy ? "copy" : "raster")
+        os << "  [" << i << "] "
+           << (s.kind == StepKind::Chain ? "chain" : s.kind == StepKind::Copy ? "copy"
+               : s.kind == StepKind::Layers ? "layers" : "raster")
            << " " << s.label << " -> slot " << s.dst_slot;
         if (s.kind == StepKind::Raster) os << " (" << s.raster.width << "x" << s.raster.height << ", " << s.raster.prog.n
                                            << " ops" << (s.raster.raw_copy ? ", raw" : "") << ")";

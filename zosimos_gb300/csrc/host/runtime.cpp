@@ -59,6 +59,7 @@ PoolImage &Pool::get(uint64_t key) {
 
 Executable::~Executable() {
     for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+    if (batch_scratch) cudaFree(batch_scratch);
     if (graph_stream) cudaStreamDestroy(graph_stream);
     for (void *p : dev_buffers)
         if (p) cudaFree(p);
@@ -95,6 +96,14 @@ void Executable::record_range(cudaStream_t stream, const std::vector<void *> &pt
                                        stream),
                        "device copy");
             break;
+        case StepKind::Layers: {
+            ZsLayersArgs &L = *st.layers;      // pointers change per launch: patch a copy
+            ZsLayersArgs a = L;
+            if (st.base_slot >= 0) a.base.ptr = (const uint8_t *)ptrs[st.base_slot];
+            for (size_t i = 0; i < st.layer_slots.size(); ++i) a.layers[i].ptr = (const uint8_t *)ptrs[st.layer_slots[i]];
+            a.dst = (uint8_t *)ptrs[st.dst_slot];
+            check_cuda(launch_layers(a, sm_count, stream), st.label.c_str());
+        } break;
         case StepKind::Chain: {
             ZsChainArgs c = st.chain;
             c.src = (const uint8_t *)ptrs[st.src_slot[0]];

@@ -140,10 +140,21 @@ struct SrcRef {
     int64_t stride = 0;
 };
 
-enum class StepKind { Raster, Chain, Copy };
+enum class StepKind { Raster, Chain, Copy, Layers };
+
+// One layer of a fused layer stack: its source buffer and the sampling/blend setup.
+struct LayerRef {
+    int slot = -1;
+    ZsLayer proto{};
+    bool quant_sample = false, quant_acc = false;
+    ZsFormat sample_fmt{}, acc_fmt{};
+};
 
 struct Step {
     StepKind kind;
+    std::shared_ptr<ZsLayersArgs> layers;   // Layers: template (pointers filled at launch)
+    std::vector<int> layer_slots;
+    int base_slot = -1;
     ZsRasterArgs raster;         // pointers filled at launch from slots
     ZsChainArgs chain;
     uint8_t chain_src_fast = 0, chain_dst_fast = 0;
@@ -165,6 +176,8 @@ struct Executable {
     std::vector<Desc> input_desc, output_desc;
     std::vector<int> input_slot, output_slot;
     std::vector<void *> dev_buffers;                   // device allocation per slot (owned ones)
+    void *batch_scratch = nullptr;                     // batched thumbnails: image table + queue head
+    size_t batch_bytes = 0;
     std::string plan_text;
     // CUDA graphs of the launch sequence for zs_run_device, keyed by the bound pointers
     std::map<std::vector<void *>, cudaGraphExec_t> graphs;

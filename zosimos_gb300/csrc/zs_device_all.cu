@@ -4,5 +4,6 @@
 #include "zs_tables.cu"
 #include "k_raster.cu"
 #include "k_chain.cu"
+#include "k_layers.cu"
 #include "k_batch.cu"
 #include "k_noalloc.cu"

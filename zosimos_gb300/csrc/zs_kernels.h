@@ -19,6 +19,9 @@ cudaError_t launch_raster(const ZsRasterArgs &args, int sm_count, cudaStream_t s
 cudaError_t launch_chain(const ZsChainArgs &args, uint8_t src_fast, uint8_t dst_fast, int sm_count,
                          cudaStream_t stream);
 
+// A stack of affine-transformed layers blended in one pass (k_layers.cu).
+cudaError_t launch_layers(const ZsLayersArgs &args, int sm_count, cudaStream_t stream);
+
 // Number of kernel launches issued since process start (instrumentation for the bench).
 uint64_t kernel_launch_count();
 // Kernels launched through a replayed CUDA graph (counted on the host at replay).

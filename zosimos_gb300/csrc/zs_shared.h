@@ -81,7 +81,8 @@ enum ZsProducer : uint8_t {
     ZS_PR_INDEX,        // src0(ix[x], iy[y])                (resize via a nearest index table)
     ZS_PR_BLEND,        // below(x,y) blended with src1(x-ox, y-oy)
     ZS_PR_RESAMPLE_H,   // horizontal filter pass over src0 rows
-    ZS_PR_RESAMPLE_V    // vertical filter pass over src0 columns
+    ZS_PR_RESAMPLE_V,   // vertical filter pass over src0 columns
+    ZS_PR_LAYERS        // planner only: a layer stack, launched by k_layers.cu
 };
 
 struct ZsSource {
@@ -118,6 +119,41 @@ struct ZsRasterArgs {
     ZsFormat dst_fmt;
     ZsFormat fmts[ZS_MAX_FMTS];   // formats referenced by QUANT / TRANSMUTE
     ZsPixelProgram prog;
+};
+
+// A stack of layers composited in one pass: for every output pixel, start from the
+// base (a constant or a buffer) and for each layer sample it through its inverse affine
+// (nearest or bilinear, the layer's canvas colour outside it) and blend the sample onto
+// the accumulator, which stays in FP32 registers.
+#define ZS_MAX_LAYERS 64
+
+struct ZsLayer {
+    const uint8_t *ptr;
+    int64_t stride;
+    int32_t width, height;
+    ZsFormat fmt;
+    float inv[9];          // output pixel centre -> layer pixel coordinates (fixed fmaf order)
+    float canvas[4];       // value where the layer does not cover the pixel
+    uint8_t bilinear;
+    uint8_t mode;          // blend mode
+    uint8_t straight;      // operands carry straight alpha
+    uint8_t quant_sample;  // index+1 into fmts: quantise the sampled layer value (declared texel)
+    uint8_t quant_acc;     // index+1 into fmts: quantise the accumulator after the blend
+    uint8_t pad[3];
+};
+
+struct ZsLayersArgs {
+    int32_t nlayers;
+    int32_t width, height;
+    int32_t has_base;      // 1: base buffer in `base`, 0: constant base_color
+    ZsSource base;
+    float base_color[4];
+    ZsLayer layers[ZS_MAX_LAYERS];
+    uint8_t *dst;
+    int64_t dst_stride;
+    ZsFormat dst_fmt;
+    ZsFormat fmts[ZS_MAX_FMTS];
+    ZsPixelProgram prog;   // per-pixel ops fused after the stack
 };
 
 // Fused colour chain in canonical form (the hot path):

@@ -66,6 +66,40 @@ def linear_gradient_gauss(width: int, height: int, seed: int = 3, image: int = 0
     return out.astype(dtype)
 
 
+def _uniform(seed: int, image: int, n: int, channel: int) -> np.ndarray:
+    z = splitmix64(_keys(seed, image, n, channel))
+    return (z >> np.uint64(11)).astype(np.float64) / 9007199254740992.0
+
+
+def premultiplied_layer(width: int, height: int, seed: int = 5, image: int = 0, blobs: int = 8,
+                        dtype=np.float16) -> np.ndarray:
+    """Premultiplied linear RGBA: gradient + Gaussian-noise colour, alpha = clamped sum of
+    2D Gaussian blobs (sigma in [128, 768] px at 4096 px, scaled with the image)."""
+    rgb = linear_gradient_gauss(width, height, seed=seed, image=image, dtype=np.float64)
+    u = _uniform(seed, image ^ 0x8000, 4 * blobs, 7)
+    y, x = np.mgrid[0:height, 0:width].astype(np.float64)
+    scale = max(width, height) / 4096.0
+    alpha = np.zeros((height, width))
+    for b in range(blobs):
+        cx, cy = u[4 * b] * width, u[4 * b + 1] * height
+        sigma = (128.0 + 640.0 * u[4 * b + 2]) * scale
+        amp = 0.3 + 0.7 * u[4 * b + 3]
+        alpha += amp * np.exp(-((x - cx) ** 2 + (y - cy) ** 2) / (2.0 * sigma * sigma))
+    alpha = np.clip(alpha, 0.0, 1.0)
+    out = rgb.copy()
+    out[..., :3] *= alpha[..., None]
+    out[..., 3] = alpha
+    return out.astype(dtype)
+
+
+def layer_transforms(count: int, seed: int = 5):
+    """Per layer: rotation U(-30, 30) degrees and a log-uniform scale in [0.5, 2]."""
+    u = _uniform(seed, 0x7FFF, 2 * count, 9)
+    rot = (u[0::2] * 60.0 - 30.0).tolist()
+    scale = np.exp(np.log(0.5) + u[1::2] * (np.log(2.0) - np.log(0.5))).tolist()
+    return list(zip(rot, scale))
+
+
 def thumbnail_sizes(count: int = 1024, seed: int = 4, lo: int = 64, hi: int = 4096):
     """Image sides log-uniform in [lo, hi] (independent width and height)."""
     z = splitmix64(_keys(seed, 0xFFFF, 2 * count, 0))

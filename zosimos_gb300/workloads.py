@@ -67,6 +67,41 @@ def resample(w: int, h: int, out_w: int, out_h: int, filt: int):
     return c, i, o
 
 
+BLEND_CYCLE = (0, 1, 2, 3)   # over, multiply, screen, add
+
+
+def layer_affine(w: int, h: int, degrees: float, scale: float):
+    """Rotate about the centre and scale, bilinear sampling."""
+    import math
+
+    from . import Affine, AffineSample
+    return (Affine.new(AffineSample.BiLinear).shift(-w / 2.0, -h / 2.0).rotate(math.radians(degrees))
+            .scale(scale, scale).shift(w / 2.0, h / 2.0))
+
+
+def layer_stack(w: int, h: int, transforms):
+    """Premultiplied RGBA16F layers, each under its own affine (bilinear) onto a transparent
+    canvas and blended onto the stack with the modes cycling over / multiply / screen /
+    add; accumulation declared FP32, result stored RGBA16F.
+    Returns (commands, input registers, output register)."""
+    c = CommandBuffer()
+    d16 = Descriptor.linear_rgba_f16(w, h).with_color(alpha=1)
+    d32 = Descriptor.linear_rgba_f32(w, h).with_color(alpha=1)
+    acc = c.solid_rgba(d32, [0.0, 0.0, 0.0, 0.0])
+    canvas = c.solid_rgba(d32, [0.0, 0.0, 0.0, 0.0])
+    inputs = []
+    from . import Rectangle
+    for i, (deg, s) in enumerate(transforms):
+        layer = c.input(d16)
+        inputs.append(layer)
+        wide = c.color_convert(layer, d32)
+        placed = c.affine(canvas, layer_affine(w, h, deg, s), wide)
+        acc = c.blend(acc, Rectangle(0, 0, w, h), placed, BLEND_CYCLE[i % 4])
+    out = c.color_convert(acc, d16)
+    o, _ = c.output(out)
+    return c, inputs, o
+
+
 def rotation(w: int, h: int, degrees: float):
     """RGBA16F linear image rotated about its centre (bilinear) onto a transparent canvas
     of the same size.  Returns (commands, input, output)."""
