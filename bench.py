@@ -300,6 +300,161 @@ def run_ours(args, rank, world, dist):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- secondary workloads
+# (not the headline line: each prints its own JSON line with fused vs plain per-op FP32)
+
+
+def _timer(stream):
+    import torch
+
+    def timed(fn, steps, warmup):
+        for i in range(warmup):
+            fn(i)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for i in range(steps):
+            fn(i)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / steps
+
+    return timed
+
+
+def _line(name, src_px, algo_bytes, ms_fused, ms_plain, extra=None):
+    peak, kind = _peaks()
+    d = {"workload": name, "metric": "Mpix/s (source pixels)", "unit": "Mpix/s",
+         "fused_mpix_s": round(src_px / (ms_fused * 1e-3) / 1e6, 1), "fused_ms": round(ms_fused, 4),
+         "algorithmic_bytes": algo_bytes,
+         "hbm_frac": round(algo_bytes / (ms_fused * 1e-3) / 1e9 / peak, 4), "peak_gbs": peak, "peak_kind": kind}
+    if ms_plain is not None:
+        d["plain_per_op_fp32_mpix_s"] = round(src_px / (ms_plain * 1e-3) / 1e6, 1)
+        d["plain_ms"] = round(ms_plain, 4)
+        d["speedup_vs_plain_fp32"] = round(ms_plain / ms_fused, 2)
+    if extra:
+        d.update(extra)
+    print(json.dumps(d), flush=True)
+
+
+def workload_blend_resize(args, stream, sh):
+    import zosimos_gb300 as zs
+    from zosimos_gb300.synthetic import srgb_gradient_noise
+    from zosimos_gb300.workloads import blend_resize, rgba_bytes
+    timed = _timer(stream)
+    c, _, _, _ = blend_resize()
+    fused = zs.Linker.from_included().compile(c).lower_to(zs.Capabilities(mode=zs.Mode.Fused))
+    plain = zs.Linker.from_included().compile(c).lower_to(zs.Capabilities(mode=zs.Mode.PerOpF32))
+    rot = 64          # 64 input sets (268 MB) so the working set does not stay in L2
+    a = rgba_bytes(srgb_gradient_noise(512, 512, seed=1, image=0))
+    b = rgba_bytes(srgb_gradient_noise(512, 512, seed=1, image=1))
+    ins = [(zs.DeviceBuffer(a.nbytes), zs.DeviceBuffer(b.nbytes)) for _ in range(rot)]
+    outs = [zs.DeviceBuffer(384 * 384 * 4) for _ in range(rot)]
+    for x, y in ins:
+        x.upload(a)
+        y.upload(b)
+    run = lambda exe: (lambda i: exe.run_device([ins[i % rot][0].ptr, ins[i % rot][1].ptr], [outs[i % rot].ptr], sh))
+    msf = timed(run(fused), args.steps, args.warmup)
+    msp = timed(run(plain), args.steps, args.warmup)
+    _line("blend_resize 2x512^2 RGBA8 -> over -> bilinear 384^2 -> RGBA8", 2 * 512 * 512,
+          2 * 512 * 512 * 4 + 384 * 384 * 4, msf, msp,
+          {"fused_kernels": fused.kernel_count(), "plain_kernels": plain.kernel_count()})
+
+
+def workload_resample(args, stream, sh):
+    import numpy as np
+
+    import zosimos_gb300 as zs
+    from zosimos_gb300.synthetic import linear_gradient_gauss
+    from zosimos_gb300.workloads import resample, rotation
+    timed = _timer(stream)
+    n = 8192
+    img = np.ascontiguousarray(linear_gradient_gauss(n, n, seed=3)).view(np.uint8)
+    src = zs.DeviceBuffer(img.nbytes)
+    src.upload(img)
+    steps = max(3, args.steps // 10)
+    for filt, fname in ((zs.Filter.Lanczos3, "lanczos3"), (zs.Filter.Box, "box")):
+        for factor in (2.0, 3.7, 8.0):
+            ow = int(round(n / factor))
+            c, _, _ = resample(n, n, ow, ow, filt)
+            exes = [zs.Linker.from_included().compile(c).lower_to(zs.Capabilities(mode=m))
+                    for m in (zs.Mode.Fused, zs.Mode.PerOpF32)]
+            dst = zs.DeviceBuffer(ow * ow * 8)
+            ms = [timed(lambda i, e=e: e.run_device([src.ptr], [dst.ptr], sh), steps, args.warmup) for e in exes]
+            _line(f"resample {fname} 8192^2 RGBA16F /{factor} -> {ow}^2", n * n, n * n * 8 + ow * ow * 8,
+                  ms[0], ms[1])
+            dst.free()
+    c, _, _, _ = rotation(n, n, 17.0)
+    exes = [zs.Linker.from_included().compile(c).lower_to(zs.Capabilities(mode=m))
+            for m in (zs.Mode.Fused, zs.Mode.PerOpF32)]
+    dst = zs.DeviceBuffer(n * n * 8)
+    ms = [timed(lambda i, e=e: e.run_device([src.ptr], [dst.ptr], sh), steps, args.warmup) for e in exes]
+    _line("rotate 17 deg bilinear 8192^2 RGBA16F", n * n, 2 * n * n * 8, ms[0], ms[1])
+
+
+def workload_thumbnails(args, stream, sh):
+    import numpy as np
+
+    import zosimos_gb300 as zs
+    from zosimos_gb300.synthetic import srgb_gradient_noise, thumbnail_sizes
+    from zosimos_gb300.workloads import color_chain, rgba_bytes
+    timed = _timer(stream)
+    ws, hs = thumbnail_sizes(1024, seed=4)
+    # Sources: top-left crops of one seeded 4096^2 image, each in its own tight buffer.
+    atlas = rgba_bytes(srgb_gradient_noise(4096, 4096, seed=4))
+    bufs = []
+    for w, h in zip(ws, hs):
+        b = zs.DeviceBuffer(int(w) * int(h) * 4)
+        b.upload(np.ascontiguousarray(atlas[:h, :w * 4]))
+        bufs.append(b)
+    c, _, _ = color_chain(1, 1)
+    exe = zs.Linker.from_included().compile(c).lower_to()
+    out = zs.DeviceBuffer(1024 * 256 * 256 * 4)
+    ptrs, wl, hl = [b.ptr for b in bufs], [int(w) for w in ws], [int(h) for h in hs]
+    run = lambda i: exe.batch_thumbnails(ptrs, wl, hl, 256, out.ptr, sh)
+    ms = timed(run, max(3, args.steps // 20), args.warmup)
+    src_px = int(sum(int(w) * int(h) for w, h in zip(ws, hs)))
+    _line("thumbnails 1024 uneven RGBA8 -> colour chain -> box fit 256 -> centred 256^2", src_px,
+          src_px * 4 + 1024 * 256 * 256 * 4, ms, None,
+          {"images": 1024, "source_gpx": round(src_px / 1e9, 3), "launches_per_batch": 1})
+
+
+def workload_layers(args, stream, sh):
+    import numpy as np
+
+    import zosimos_gb300 as zs
+    from zosimos_gb300.synthetic import layer_transforms, premultiplied_layer
+    from zosimos_gb300.workloads import layer_stack
+    timed = _timer(stream)
+    n, w = 32, 4096
+    distinct = 4      # four generated layers, bound cyclically to the 32 inputs
+    layers = []
+    for i in range(distinct):
+        img = np.ascontiguousarray(premultiplied_layer(w, w, seed=5, image=i)).view(np.uint8)
+        b = zs.DeviceBuffer(img.nbytes)
+        b.upload(img)
+        layers.append(b)
+    c, _, _ = layer_stack(w, w, layer_transforms(n, seed=5))
+    exes = [zs.Linker.from_included().compile(c).lower_to(zs.Capabilities(mode=m))
+            for m in (zs.Mode.Fused, zs.Mode.PerOpF32)]
+    dst = zs.DeviceBuffer(w * w * 8)
+    ins = [layers[i % distinct].ptr for i in range(n)]
+    steps = max(3, args.steps // 40)
+    ms = [timed(lambda i, e=e: e.run_device(ins, [dst.ptr], sh), steps, args.warmup) for e in exes]
+    _line("layer stack 32 x 4096^2 premultiplied RGBA16F, affine + blend per layer", n * w * w,
+          n * w * w * 8 + w * w * 8, ms[0], ms[1],
+          {"fused_kernels": exes[0].kernel_count(), "plain_kernels": exes[1].kernel_count()})
+
+
+def run_workloads(args):
+    import torch
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    stream = torch.cuda.Stream()
+    names = ["blend_resize", "resample", "thumbnails", "layers"] if args.workload == "all" else [args.workload]
+    for name in names:
+        globals()["workload_" + name](args, stream, stream.cuda_stream)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -309,8 +464,14 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=10.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true", help="short fixed launch sequence for ncu captures")
+    ap.add_argument("--workload", default="chain",
+                    choices=["chain", "blend_resize", "resample", "thumbnails", "layers", "all"],
+                    help="chain (default) is the headline line; the others print secondary lines")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
+    if args.workload != "chain" and args.impl == "ours":
+        run_workloads(args)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     dist = None
