@@ -295,6 +295,12 @@ int zs_resample_rgba16f_noalloc(const void *src, uint32_t src_width, uint32_t sr
 /* Number of kernels this library has launched since the process started. */
 uint64_t zs_kernel_launch_count(void);
 
+/* Device status word of `device` (ZS_DEVSTAT_* bits of zs_shared.h; bit 0: a bounded wait of
+ * a kernel on its own bulk copies gave up, and that launch's output is incomplete), read
+ * after synchronising and cleared.  zs_exec_sync reports a set bit as ZS_ERR_TIMEOUT.
+ * No counterpart in the reference (wgpu reports device loss through its own callbacks). */
+int zs_device_status(int device, uint32_t *flags);
+
 #ifdef __cplusplus
 }
 #endif

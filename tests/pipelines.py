@@ -365,6 +365,25 @@ def oracle_resample(img16, out, filt):
     return O.resample(img16.astype(np.float64), out[0], out[1], filt)
 
 
+def ours_resample_srgb8(img8, out, filt, mode=zs.Mode.Fused):
+    """resize_filtered of a native RGBA8 sRGB image (filtered in linear light, stored sRGB)."""
+    h, w = img8.shape[:2]
+    c = CommandBuffer()
+    i = c.input(Descriptor.srgb_rgba8(w, h))
+    o, _ = c.output(c.resize_filtered(i, out, filt))
+    pool = Pool()
+    k = pool.insert(Descriptor.srgb_rgba8(w, h), rgba_bytes(img8))
+    return np.frombuffer(run(c, pool, [(i, k)], [o], mode)[0], np.uint8).reshape(out[1], out[0], 4)
+
+
+def oracle_resample_srgb8(img8, out, filt):
+    h, w = img8.shape[:2]
+    f = O.Format(O.BITS["UInt8x4"], O.PARTS["RgbA"], O.TRANSFER["Srgb"], True)
+    lin = O.decode(f, img8.reshape(h, w * 4), w, h)
+    res = O.resample(lin, out[0], out[1], filt)
+    return O.encode(f, res).reshape(out[1], out[0], 4)
+
+
 def ours_rotation(img16, degrees, mode=zs.Mode.Fused):
     h, w = img16.shape[:2]
     c, i, o, _ = rotation_cmds(w, h, degrees)

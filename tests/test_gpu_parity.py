@@ -161,6 +161,29 @@ def test_resample_upscale():
     assert np.abs(ours - P.oracle_resample(img, (317, 200), zs.Filter.Lanczos3)).max() <= F16_TOL
 
 
+@pytest.mark.parametrize("src,out", [((301, 203), (150, 101)), ((301, 203), (37, 25)), ((257, 64), (600, 31))])
+@pytest.mark.parametrize("mode", [zs.Mode.Fused, zs.Mode.PerOpF32])
+def test_resample_ragged(src, out, mode):
+    # Row strides that are not a multiple of 16 bytes (rows staged with plain loads),
+    # partial edge tiles, and a horizontal upscale with a vertical downscale.
+    from zosimos_gb300.synthetic import linear_gradient_gauss
+    img = linear_gradient_gauss(src[0], src[1], seed=11)
+    ours = P.ours_resample(img, out, zs.Filter.Lanczos3, mode)
+    assert np.abs(ours - P.oracle_resample(img, out, zs.Filter.Lanczos3)).max() <= F16_TOL
+
+
+@pytest.mark.parametrize("filt", [zs.Filter.Lanczos3, zs.Filter.Box, zs.Filter.Triangle])
+def test_resample_srgb8(filt):
+    # 8-bit sRGB source and target: decoded through the LUT, filtered in FP32 linear light,
+    # encoded with the exact round-to-nearest table; within one 8-bit step of FP64.
+    from zosimos_gb300.synthetic import srgb_gradient_noise
+    img = srgb_gradient_noise(640, 480, seed=9)
+    out = (256, 192)
+    ours = P.ours_resample_srgb8(img, out, filt).astype(np.int32)
+    ref = P.oracle_resample_srgb8(img, out, filt).astype(np.int32)
+    assert np.abs(ours - ref).max() <= 1
+
+
 @pytest.mark.parametrize("mode", [zs.Mode.Fused, zs.Mode.PerOpF32])
 def test_rotation(mode):
     from zosimos_gb300.synthetic import linear_gradient_gauss

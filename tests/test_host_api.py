@@ -54,6 +54,11 @@ def test_blend_resize_plan():
 
 def test_resample_and_rotation_plans():
     c, _, _ = resample(1024, 768, 512, 384, zs.Filter.Lanczos3)
+    fused = lower(c)
+    assert fused.kernel_count() == 1 and "resample 2d" in fused.describe()
+    assert lower(c, zs.Mode.PerOpF32).kernel_count() == 2
+    # A downscale whose tile span does not fit shared memory keeps the two-pass form.
+    c, _, _ = resample(65536, 64, 128, 64, zs.Filter.Lanczos3)
     assert lower(c).kernel_count() == 2
     c, _, _, _ = rotation(640, 480, 17.0)
     assert lower(c).kernel_count() == 1

@@ -163,6 +163,7 @@ def _lib():
             "zs_host_alloc": ([U64], P), "zs_host_free": ([P], None), "zs_device_alloc": ([U64], P),
             "zs_device_free": ([P], None), "zs_memcpy_h2d": ([P, P, U64], I32), "zs_memcpy_d2h": ([P, P, U64], I32),
             "zs_device_synchronize": ([], I32), "zs_kernel_launch_count": ([], U64),
+            "zs_device_status": ([ctypes.c_int32, pU32], I32),
             "zs_descriptor_is_consistent": ([pD], I32), "zs_descriptor_byte_len": ([pD], U64),
             "zs_texel_bytes": ([U32], U32),
             "zs_batch_thumbnails": ([P, P, P, P, U32, U32, P, P], I32),
@@ -183,6 +184,14 @@ def _check(rc: int) -> None:
 
 def kernel_launch_count() -> int:
     return int(_lib().zs_kernel_launch_count())
+
+
+def device_status(device: int = 0) -> int:
+    """Synchronise `device` and return (and clear) its status word: bit 0 set means a
+    kernel's bounded wait on its own bulk copies gave up and its output is incomplete."""
+    flags = ctypes.c_uint32(0)
+    _check(_lib().zs_device_status(device, ctypes.byref(flags)))
+    return int(flags.value)
 
 
 # ---------------------------------------------------------------- value types

@@ -502,6 +502,9 @@ int zs_exec_sync(zs_execution *exec) {
     return guarded([&] {
         NEED(exec);
         check_cuda(cudaStreamSynchronize(exec->x.stream), "synchronize");
+        uint32_t flags = 0;
+        check_cuda(read_device_status(exec->x.exe->device, &flags, true), "device status");
+        if (flags) fail(ZS_ERR_TIMEOUT, "a kernel's bounded wait on its bulk copies gave up");
     });
 }
 
@@ -669,5 +672,18 @@ int zs_batch_thumbnails(zs_executable *chain, const void *const *images, const u
 }
 
 uint64_t zs_kernel_launch_count(void) { return kernel_launch_count(); }
+
+int zs_device_status(int device, uint32_t *flags) {
+    return guarded([&] {
+        NEED(flags);
+        int prev = 0;
+        check_cuda(cudaGetDevice(&prev), "get device");
+        check_cuda(cudaSetDevice(device), "set device");
+        cudaError_t e = cudaDeviceSynchronize();
+        cudaSetDevice(prev);
+        check_cuda(e, "synchronize");
+        check_cuda(read_device_status(device, flags, true), "device status");
+    });
+}
 
 }  // extern "C"

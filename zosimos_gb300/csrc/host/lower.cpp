@@ -25,6 +25,7 @@ struct Pending {
     ZsRasterArgs a;
     int src_slot[ZS_MAX_SRCS] = {-1, -1, -1};
     int idx_x_slot = -1, idx_y_slot = -1, weight_slot = -1;
+    int vfirst_slot = -1, vcount_slot = -1, vweight_slot = -1;
     HProgram prog;
     std::string label;
     // ZS_PR_LAYERS: base (src_slot[0] when has_below, else a.cons[0..3]) and the layers.
@@ -188,6 +189,9 @@ struct Planner {
         st.idx_x_slot = p.idx_x_slot;
         st.idx_y_slot = p.idx_y_slot;
         st.weight_slot = p.weight_slot;
+        st.vfirst_slot = p.vfirst_slot;
+        st.vcount_slot = p.vcount_slot;
+        st.vweight_slot = p.vweight_slot;
         // Pixel program: FP64 host program -> FP32 parameters.
         ZsPixelProgram &pp = st.raster.prog;
         std::memset(&pp, 0, sizeof(pp));
@@ -648,6 +652,7 @@ struct Planner {
                 use(op.a);
                 need(op.a);
                 const Desc &sd = desc(op.a);
+                if (E.mode == ZS_MODE_FUSED && try_resample_2d(r, op, sd, d)) break;
                 // Pass 1: horizontal, into an intermediate (dst width x src height).
                 auto h = new_pending(ZS_PR_RESAMPLE_H, d.width, sd.height, "resample horizontal");
                 set_src(*h, 0, op.a);
@@ -706,6 +711,61 @@ struct Planner {
             if (ix > (int32_t)src_len - 1) ix = (int32_t)src_len - 1;
             index[x] = ix;
         }
+    }
+
+    // Widest source span (first tap of the tile's first output .. last tap of its last)
+    // over the tiles of one axis, or -1 when the windows are not monotone (a tile's span
+    // would then not cover every window inside it).
+    static int tile_span(const std::vector<int32_t> &first, const std::vector<int32_t> &count, int tile) {
+        const int n = (int)first.size();
+        for (int i = 1; i < n; ++i)
+            if (first[i] < first[i - 1] || first[i] + count[i] < first[i - 1] + count[i - 1]) return -1;
+        int span = 0;
+        for (int t0 = 0; t0 < n; t0 += tile) {
+            const int t1 = std::min(t0 + tile, n) - 1;
+            span = std::max(span, first[t1] + count[t1] - first[t0]);
+        }
+        return span;
+    }
+
+    // resize_filtered as one tiled launch (k_resample.cu): the horizontally filtered rows
+    // stay in shared memory, so no intermediate image is stored.
+    bool try_resample_2d(uint32_t r, const Op &op, const Desc &sd, const Desc &d) {
+        std::vector<int32_t> hf, hc, vf, vc;
+        std::vector<float> hw, vw;
+        const int htaps = resample_weights(sd.width, d.width, op.u0, hf, hc, hw);
+        const int vtaps = resample_weights(sd.height, d.height, op.u0, vf, vc, vw);
+        const int span = tile_span(hf, hc, ZS_RS_TW);
+        if (span < 0 || tile_span(vf, vc, ZS_RS_TH) < 0) return false;
+        // Two staged batches of rows, the filtered-row buffers and the tile's weights
+        // (at the tallest tile) must fit one CTA.
+        const size_t bpp = vals[op.a].fmt.bpp;
+        const size_t rowbytes = ((span * bpp + 15) & ~(size_t)15) + 16;
+        const size_t weights = 4 * (ZS_RS_TW * (size_t)(htaps | 1) + ZS_RS_TH * (size_t)vtaps) + 32;
+        if (2 * ZS_RS_RB * rowbytes + 2 * ZS_RS_RB * ZS_RS_TW * 16 + weights + 16 > ZS_RS_MAX_SMEM) return false;
+        // Tile height: the tallest that still leaves several tiles per CTA slot (fewer
+        // source rows are then re-read as the vertical filter halo of the next tile).
+        const int tiles_x = ((int)d.width + ZS_RS_TW - 1) / ZS_RS_TW;
+        int th = 8;
+        for (int cand : {32, 16})
+            if ((int64_t)tiles_x * (((int)d.height + cand - 1) / cand) >= 6 * 152) {
+                th = cand;
+                break;
+            }
+        auto p = new_pending(ZS_PR_RESAMPLE_2D, d.width, d.height, "resample 2d");
+        set_src(*p, 0, op.a);
+        p->a.tile_rows = th;
+        p->idx_x_slot = table_slot(hf.data(), hf.size() * 4);
+        p->idx_y_slot = table_slot(hc.data(), hc.size() * 4);
+        p->weight_slot = table_slot(hw.data(), hw.size() * 4);
+        p->vfirst_slot = table_slot(vf.data(), vf.size() * 4);
+        p->vcount_slot = table_slot(vc.data(), vc.size() * 4);
+        p->vweight_slot = table_slot(vw.data(), vw.size() * 4);
+        p->a.taps = htaps;
+        p->a.vtaps = vtaps;
+        p->a.max_span = span;
+        set_pending(r, std::move(p));
+        return true;
     }
 
     void add_weights(Pending &p, uint32_t src_len, uint32_t dst_len, uint32_t filter) {

@@ -118,6 +118,9 @@ void Executable::record_range(cudaStream_t stream, const std::vector<void *> &pt
             a.index_x = st.idx_x_slot >= 0 ? (const int32_t *)ptrs[st.idx_x_slot] : nullptr;
             a.index_y = st.idx_y_slot >= 0 ? (const int32_t *)ptrs[st.idx_y_slot] : nullptr;
             a.weights = st.weight_slot >= 0 ? (const float *)ptrs[st.weight_slot] : nullptr;
+            a.vfirst = st.vfirst_slot >= 0 ? (const int32_t *)ptrs[st.vfirst_slot] : nullptr;
+            a.vcount = st.vcount_slot >= 0 ? (const int32_t *)ptrs[st.vcount_slot] : nullptr;
+            a.vweights = st.vweight_slot >= 0 ? (const float *)ptrs[st.vweight_slot] : nullptr;
             check_cuda(launch_raster(a, sm_count, stream), st.label.c_str());
         } break;
         }

@@ -161,6 +161,7 @@ struct Step {
     int src_slot[ZS_MAX_SRCS] = {-1, -1, -1};
     int dst_slot = -1;
     int idx_x_slot = -1, idx_y_slot = -1, weight_slot = -1;
+    int vfirst_slot = -1, vcount_slot = -1, vweight_slot = -1;   // RESAMPLE_2D vertical tables
     uint64_t copy_bytes = 0;
     std::string label;
 };

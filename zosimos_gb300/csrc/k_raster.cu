@@ -218,6 +218,7 @@ namespace zs {
 cudaError_t launch_raster(const ZsRasterArgs &args, int sm_count, cudaStream_t stream) {
     const int64_t n = (int64_t)args.width * args.height;
     if (n <= 0) return cudaSuccess;
+    if (args.producer == ZS_PR_RESAMPLE_2D) return launch_resample2d(args, sm_count, stream);
     int64_t blocks = (n + 255) / 256;
     const int64_t cap = (int64_t)(sm_count > 0 ? sm_count : 148) * 8;
     if (blocks > cap) blocks = cap;

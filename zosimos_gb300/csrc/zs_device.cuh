@@ -19,6 +19,9 @@
 __device__ float zs_srgb_decode_lut[256];
 __device__ uint32_t zs_srgb_encode_tab[ZS_ENC_ENTRIES];
 __device__ uint32_t zs_srgb_encode_tab_shifted[ZS_ENCS_ENTRIES];
+// Sticky error bits set by kernels whose bounded waits gave up (ZS_DEVSTAT_*); the host
+// reads and clears them after synchronising.
+__device__ unsigned int zs_device_status_word;
 
 // ---------------------------------------------------------------- transfer functions
 

@@ -3,6 +3,7 @@
 // relocatable device code.
 #include "zs_tables.cu"
 #include "k_raster.cu"
+#include "k_resample.cu"
 #include "k_chain.cu"
 #include "k_layers.cu"
 #include "k_batch.cu"

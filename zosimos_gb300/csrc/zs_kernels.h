@@ -13,6 +13,9 @@ cudaError_t init_device_tables(int device);
 
 // Generic raster launch: producer + fused pixel program + store (k_raster.cu).
 cudaError_t launch_raster(const ZsRasterArgs &args, int sm_count, cudaStream_t stream);
+// Both passes of a separable resample in one tiled launch (k_resample.cu); launch_raster
+// dispatches ZS_PR_RESAMPLE_2D here.
+cudaError_t launch_resample2d(const ZsRasterArgs &args, int sm_count, cudaStream_t stream);
 
 // Fused colour chain in canonical form, RGBA8 in / RGBA8 out (k_chain.cu).
 // Returns cudaErrorNotSupported when no specialisation exists for the formats.
@@ -22,6 +25,8 @@ cudaError_t launch_chain(const ZsChainArgs &args, uint8_t src_fast, uint8_t dst_
 // A stack of affine-transformed layers blended in one pass (k_layers.cu).
 cudaError_t launch_layers(const ZsLayersArgs &args, int sm_count, cudaStream_t stream);
 
+// Device status word (ZS_DEVSTAT_* bits) of `device`, optionally cleared after reading.
+cudaError_t read_device_status(int device, uint32_t *flags, bool clear);
 // Number of kernel launches issued since process start (instrumentation for the bench).
 uint64_t kernel_launch_count();
 // Kernels launched through a replayed CUDA graph (counted on the host at replay).

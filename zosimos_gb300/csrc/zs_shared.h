@@ -82,7 +82,8 @@ enum ZsProducer : uint8_t {
     ZS_PR_BLEND,        // below(x,y) blended with src1(x-ox, y-oy)
     ZS_PR_RESAMPLE_H,   // horizontal filter pass over src0 rows
     ZS_PR_RESAMPLE_V,   // vertical filter pass over src0 columns
-    ZS_PR_LAYERS        // planner only: a layer stack, launched by k_layers.cu
+    ZS_PR_LAYERS,       // planner only: a layer stack, launched by k_layers.cu
+    ZS_PR_RESAMPLE_2D   // both separable passes in one tiled launch (k_resample.cu)
 };
 
 struct ZsSource {
@@ -112,6 +113,14 @@ struct ZsRasterArgs {
     const float *weights;     // RESAMPLE weights [dst][taps]
     int32_t taps;
     int32_t pad1;
+    // RESAMPLE_2D: the vertical tables (the horizontal ones are index_x/index_y/weights)
+    const int32_t *vfirst;
+    const int32_t *vcount;
+    const float *vweights;
+    int32_t vtaps;
+    int32_t max_span;         // widest source column span of one output tile
+    int32_t tile_rows;        // output rows per tile: 8, 16 or 32
+    int32_t stages;           // staged batches of source rows (set by the launcher)
     // destination
     uint8_t *dst;
     int64_t dst_stride;
@@ -120,6 +129,18 @@ struct ZsRasterArgs {
     ZsFormat fmts[ZS_MAX_FMTS];   // formats referenced by QUANT / TRANSMUTE
     ZsPixelProgram prog;
 };
+
+// RESAMPLE_2D output tile (columns x rows; the rows per launch are 8, 16 or ZS_RS_TH) and
+// the source rows staged per batch.  One CTA's shared memory holds `stages` batches of
+// raw source rows, two batches of filtered rows and the tile's weight tables.
+#define ZS_RS_TW 64
+#define ZS_RS_TH 32
+#define ZS_RS_RB 8
+#define ZS_RS_MAX_SMEM (200 * 1024)
+#define ZS_RS_STAGE_BUDGET (96 * 1024)   // staged source rows of one CTA (2 CTAs per SM)
+
+// Bits of the device status word.
+#define ZS_DEVSTAT_WAIT_TIMEOUT 1u   // an mbarrier wait on a bulk copy exceeded its limit
 
 // A stack of layers composited in one pass: for every output pixel, start from the
 // base (a constant or a buffer) and for each layer sample it through its inverse affine

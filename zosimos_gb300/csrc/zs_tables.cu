@@ -91,4 +91,20 @@ cudaError_t init_device_tables(int device) {
     return e;
 }
 
+cudaError_t read_device_status(int device, uint32_t *flags, bool clear) {
+    int prev = 0;
+    cudaError_t e = cudaGetDevice(&prev);
+    if (e != cudaSuccess) return e;
+    if (prev != device && (e = cudaSetDevice(device)) != cudaSuccess) return e;
+    unsigned int v = 0;
+    e = cudaMemcpyFromSymbol(&v, zs_device_status_word, sizeof(v));
+    if (e == cudaSuccess && clear && v) {
+        const unsigned int zero = 0;
+        e = cudaMemcpyToSymbol(zs_device_status_word, &zero, sizeof(zero));
+    }
+    if (prev != device) cudaSetDevice(prev);
+    *flags = v;
+    return e;
+}
+
 }  // namespace zs
