@@ -368,10 +368,24 @@ def workload_resample(args, stream, sh):
     from zosimos_gb300.synthetic import linear_gradient_gauss
     from zosimos_gb300.workloads import resample, rotation
     timed = _timer(stream)
-    n = 8192
+    n = 4096 if args.profile else 8192
     img = np.ascontiguousarray(linear_gradient_gauss(n, n, seed=3)).view(np.uint8)
     src = zs.DeviceBuffer(img.nbytes)
     src.upload(img)
+    if args.profile:
+        # A short, fixed sequence for ncu (4096^2 RGBA16F source, 128 MiB > L2): one fused
+        # launch each of Lanczos-3 /2, Lanczos-3 /8 and box /2.
+        import torch
+        for filt, factor in ((zs.Filter.Lanczos3, 2.0), (zs.Filter.Lanczos3, 8.0), (zs.Filter.Box, 2.0)):
+            ow = int(round(n / factor))
+            c, _, _ = resample(n, n, ow, ow, filt)
+            exe = zs.Linker.from_included().compile(c).lower_to(zs.Capabilities(mode=zs.Mode.Fused))
+            dst = zs.DeviceBuffer(ow * ow * 8)
+            exe.run_device([src.ptr], [dst.ptr], sh)
+            torch.cuda.synchronize()
+            dst.free()
+        print("profile run done", flush=True)
+        return
     steps = max(3, args.steps // 10)
     for filt, fname in ((zs.Filter.Lanczos3, "lanczos3"), (zs.Filter.Box, "box")):
         for factor in (2.0, 3.7, 8.0):

@@ -212,8 +212,14 @@ typedef struct zs_capabilities {
     int32_t device;           /* CUDA device ordinal */
     uint32_t mode;            /* ZS_MODE_* */
     uint32_t use_graph;       /* capture the kernel sequence as a CUDA graph and replay it */
-    uint32_t reserved;
+    uint32_t flags;           /* ZS_CAP_* bits */
 } zs_capabilities;
+
+enum {
+    /* resize_filtered: use the FP32 SIMT resample kernel even where the tensor-core path
+     * (f16 band matrices, FP32 accumulation) applies. */
+    ZS_CAP_SIMT_RESAMPLE = 1
+};
 
 typedef struct zs_executable zs_executable;
 /* Program::lower_to (program.rs:1304). */

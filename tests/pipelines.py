@@ -17,8 +17,8 @@ from zosimos_gb300 import (Affine, AffineSample, Bits, Capabilities, ChromaticAd
 from zosimos_gb300.workloads import rgba_bytes  # noqa: E402
 
 
-def run(cmds, pool, binds, outputs, mode=zs.Mode.Fused):
-    keys = zs.run_pipeline(cmds, pool, binds, outputs, Capabilities(mode=mode))
+def run(cmds, pool, binds, outputs, mode=zs.Mode.Fused, simt_resample=False):
+    keys = zs.run_pipeline(cmds, pool, binds, outputs, Capabilities(mode=mode, simt_resample=simt_resample))
     return [pool.read(k) for k in keys]
 
 
@@ -353,12 +353,18 @@ def f16_from_bytes(b: np.ndarray, w: int, h: int) -> np.ndarray:
     return np.ascontiguousarray(b).view(np.float16).reshape(h, w, 4).astype(np.float64)
 
 
-def ours_resample(img16, out, filt, mode=zs.Mode.Fused):
+def ours_resample(img16, out, filt, mode=zs.Mode.Fused, simt_resample=False):
     h, w = img16.shape[:2]
     c, i, o = resample_cmds(w, h, out[0], out[1], filt)
     pool = Pool()
     k = pool.insert(Descriptor.linear_rgba_f16(w, h), f16_bytes(img16))
-    return f16_from_bytes(run(c, pool, [(i, k)], [o], mode)[0], out[0], out[1])
+    return f16_from_bytes(run(c, pool, [(i, k)], [o], mode, simt_resample)[0], out[0], out[1])
+
+
+def resample_plan(w, h, out, filt, simt_resample=False) -> str:
+    c, _, _ = resample_cmds(w, h, out[0], out[1], filt)
+    exe = zs.Linker.from_included().compile(c).lower_to(Capabilities(simt_resample=simt_resample))
+    return exe.describe()
 
 
 def oracle_resample(img16, out, filt):

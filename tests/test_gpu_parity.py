@@ -161,6 +161,31 @@ def test_resample_upscale():
     assert np.abs(ours - P.oracle_resample(img, (317, 200), zs.Filter.Lanczos3)).max() <= F16_TOL
 
 
+@pytest.mark.parametrize("filt", [zs.Filter.Lanczos3, zs.Filter.Box, zs.Filter.Triangle])
+@pytest.mark.parametrize("src,out", [((1024, 768), (512, 384)), ((1024, 768), (277, 208)), ((640, 300), (640, 131)),
+                                     ((200, 130), (317, 200)), ((518, 390), (129, 97))])
+def test_resample_tensor_cores(filt, src, out):
+    # The vertical pass on the tensor cores (f16 band matrices, FP32 accumulation in TMEM),
+    # against FP64, and against the FP32 SIMT kernel on the same input.
+    from zosimos_gb300.synthetic import linear_gradient_gauss
+    img = linear_gradient_gauss(src[0], src[1], seed=13)
+    plan = P.resample_plan(src[0], src[1], out, filt)
+    ours = P.ours_resample(img, out, filt)
+    simt = P.ours_resample(img, out, filt, simt_resample=True)
+    ref = P.oracle_resample(img, out, filt)
+    assert np.abs(ours - ref).max() <= F16_TOL, plan
+    assert np.abs(simt - ref).max() <= F16_TOL
+    assert np.abs(ours - simt).max() <= F16_TOL
+
+
+def test_resample_tensor_core_plan():
+    # RGBA16F sources with 16-byte rows take the tensor-core kernel where the staged columns
+    # of a tile fit one MMA; the SIMT flag and odd widths keep the FP32 SIMT kernel.
+    assert "tensor cores" in P.resample_plan(1024, 768, (512, 384), zs.Filter.Lanczos3)
+    assert "tensor cores" not in P.resample_plan(1024, 768, (512, 384), zs.Filter.Lanczos3, simt_resample=True)
+    assert "tensor cores" not in P.resample_plan(1023, 768, (512, 384), zs.Filter.Lanczos3)
+
+
 @pytest.mark.parametrize("src,out", [((301, 203), (150, 101)), ((301, 203), (37, 25)), ((257, 64), (600, 31))])
 @pytest.mark.parametrize("mode", [zs.Mode.Fused, zs.Mode.PerOpF32])
 def test_resample_ragged(src, out, mode):

@@ -112,7 +112,7 @@ class _CRect(ctypes.Structure):
 
 class _CCaps(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("mode", ctypes.c_uint32), ("use_graph", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32)]
+                ("flags", ctypes.c_uint32)]
 
 
 _LIB = None
@@ -325,10 +325,12 @@ class Affine:
 
 @dataclass
 class Capabilities:
-    """Lowering options (program.rs Capabilities): device, executor mode, graph replay."""
+    """Lowering options (program.rs Capabilities): device, executor mode, graph replay and
+    `simt_resample` (resize_filtered on the FP32 SIMT kernel instead of the tensor cores)."""
     device: int = 0
     mode: int = Mode.Fused
     use_graph: bool = True
+    simt_resample: bool = False
 
 
 # ---------------------------------------------------------------- pool
@@ -516,7 +518,7 @@ class Program:
 
     def lower_to(self, caps: Optional[Capabilities] = None) -> "Executable":
         caps = caps or Capabilities()
-        c = _CCaps(caps.device, caps.mode, int(caps.use_graph), 0)
+        c = _CCaps(caps.device, caps.mode, int(caps.use_graph), 1 if caps.simt_resample else 0)
         h = ctypes.c_void_p()
         _check(_lib().zs_lower(self._h, ctypes.byref(c), ctypes.byref(h)))
         return Executable(h)

@@ -26,6 +26,7 @@ struct Pending {
     int src_slot[ZS_MAX_SRCS] = {-1, -1, -1};
     int idx_x_slot = -1, idx_y_slot = -1, weight_slot = -1;
     int vfirst_slot = -1, vcount_slot = -1, vweight_slot = -1;
+    int vimg_slot = -1, vimg_index_slot = -1;
     HProgram prog;
     std::string label;
     // ZS_PR_LAYERS: base (src_slot[0] when has_below, else a.cons[0..3]) and the layers.
@@ -192,6 +193,8 @@ struct Planner {
         st.vfirst_slot = p.vfirst_slot;
         st.vcount_slot = p.vcount_slot;
         st.vweight_slot = p.vweight_slot;
+        st.vimg_slot = p.vimg_slot;
+        st.vimg_index_slot = p.vimg_index_slot;
         // Pixel program: FP64 host program -> FP32 parameters.
         ZsPixelProgram &pp = st.raster.prog;
         std::memset(&pp, 0, sizeof(pp));
@@ -740,9 +743,9 @@ struct Planner {
         // Two staged batches of rows, the filtered-row buffers and the tile's weights
         // (at the tallest tile) must fit one CTA.
         const size_t bpp = vals[op.a].fmt.bpp;
-        const size_t rowbytes = ((span * bpp + 15) & ~(size_t)15) + 16;
+        const size_t rowbytes = (size_t)ZS_RS_ROWBYTES((size_t)span, bpp);
         const size_t weights = 4 * (ZS_RS_TW * (size_t)(htaps | 1) + ZS_RS_TH * (size_t)vtaps) + 32;
-        if (2 * ZS_RS_RB * rowbytes + 2 * ZS_RS_RB * ZS_RS_TW * 16 + weights + 16 > ZS_RS_MAX_SMEM) return false;
+        if (2 * ZS_RS_RB * rowbytes + 2 * ZS_RS_RB * (ZS_RS_TW + 1) * 16 + weights + 16 > ZS_RS_MAX_SMEM) return false;
         // Tile height: the tallest that still leaves several tiles per CTA slot (fewer
         // source rows are then re-read as the vertical filter halo of the next tile).
         const int tiles_x = ((int)d.width + ZS_RS_TW - 1) / ZS_RS_TW;
@@ -764,8 +767,88 @@ struct Planner {
         p->a.taps = htaps;
         p->a.vtaps = vtaps;
         p->a.max_span = span;
+        const Slot &ss = E.slots[vals[op.a].slot];
+        if (!(E.flags & ZS_CAP_SIMT_RESAMPLE) && vals[op.a].fmt.fast == ZS_FAST_F16X4 && ss.stride % 16 == 0)
+            plan_resample_tc(*p, hf, hc, vf, vc, vw, vtaps, d);
         set_pending(r, std::move(p));
         return true;
+    }
+
+    // IEEE binary16 bits of `f`, round to nearest even (subnormals kept).
+    static uint16_t f32_to_f16_bits(float f) {
+        uint32_t x;
+        std::memcpy(&x, &f, 4);
+        const uint32_t sign = (x >> 16) & 0x8000u, ax = x & 0x7FFFFFFFu;
+        if (ax >= 0x7F800000u) return (uint16_t)(sign | 0x7C00u | (ax > 0x7F800000u ? 0x200u : 0u));
+        const int e = (int)(ax >> 23) - 127 + 15;
+        uint32_t mant = ax & 0x7FFFFFu;
+        if (e >= 31) return (uint16_t)(sign | 0x7C00u);
+        if (e <= 0) {
+            if (e < -10) return (uint16_t)sign;
+            mant |= 0x800000u;
+            const int shift = 14 - e;
+            uint32_t h = mant >> shift;
+            const uint32_t rem = mant & ((1u << shift) - 1u), half = 1u << (shift - 1);
+            if (rem > half || (rem == half && (h & 1u))) ++h;
+            return (uint16_t)(sign | h);
+        }
+        uint32_t h = ((uint32_t)e << 10) | (mant >> 13);
+        const uint32_t rem = mant & 0x1FFFu;
+        if (rem > 0x1000u || (rem == 0x1000u && (h & 1u))) ++h;
+        return (uint16_t)(sign | h);
+    }
+
+    // Tensor-core plan of a resample (k_resample_tc.cu): the widest tile of output columns
+    // whose staged source columns (from an even column, 4 f16 values each) fit N <= 256,
+    // and per band of 128 output rows the vertical weights as f16 band matrices, one
+    // 128 x 64 chunk per 64 source rows, laid out as the MMA reads them (K-major rows of
+    // 128 bytes, 16-byte chunk c of row m stored at chunk c ^ (m % 8)).
+    void plan_resample_tc(Pending &p, const std::vector<int32_t> &hf, const std::vector<int32_t> &hc,
+                          const std::vector<int32_t> &vf, const std::vector<int32_t> &vc, const std::vector<float> &vw,
+                          int vtaps, const Desc &d) {
+        const int dw = (int)d.width, dh = (int)d.height;
+        int tw = 0, span = 0;
+        for (int cand : {32, 16, 8}) {
+            int sp = 0;
+            for (int x0 = 0; x0 < dw; x0 += cand) {
+                const int x1 = std::min(x0 + cand, dw) - 1;
+                sp = std::max(sp, hf[x1] + hc[x1] - (hf[x0] & ~1));
+            }
+            if (sp * 4 <= 64 * ZS_TC_MAX_ATOMS) {
+                tw = cand;
+                span = sp;
+                break;
+            }
+        }
+        if (!tw) return;
+        const int bands = (dh + ZS_TC_M - 1) / ZS_TC_M;
+        std::vector<int32_t> index(2 * (size_t)bands);
+        std::vector<uint16_t> img;
+        for (int b = 0; b < bands; ++b) {
+            const int oy0 = b * ZS_TC_M, y1 = std::min(oy0 + ZS_TC_M, dh) - 1;
+            const int rbase = vf[oy0], rend = vf[y1] + vc[y1];
+            const int nk = (rend - rbase + ZS_TC_K - 1) / ZS_TC_K;
+            index[2 * b] = (int32_t)(img.size() / (ZS_TC_M * ZS_TC_K));
+            index[2 * b + 1] = nk;
+            for (int kc = 0; kc < nk; ++kc) {
+                const size_t base = img.size();
+                img.resize(base + (size_t)ZS_TC_M * ZS_TC_K, 0);
+                for (int m = 0; m < ZS_TC_M && oy0 + m <= y1; ++m) {
+                    const int oy = oy0 + m;
+                    for (int k = 0; k < ZS_TC_K; ++k) {
+                        const int t = rbase + ZS_TC_K * kc + k - vf[oy];
+                        if (t < 0 || t >= vc[oy]) continue;
+                        const size_t e = (size_t)m * ZS_TC_K + (size_t)((((k >> 3) ^ (m & 7)) << 3) | (k & 7));
+                        img[base + e] = f32_to_f16_bits(vw[(size_t)oy * vtaps + t]);
+                    }
+                }
+            }
+        }
+        p.vimg_slot = table_slot(img.data(), img.size() * 2);
+        p.vimg_index_slot = table_slot(index.data(), index.size() * 4);
+        p.a.tc_tw = tw;
+        p.a.tc_atoms = (span * 4 + 63) / 64;
+        p.label = "resample 2d [tensor cores: f16 band matrices, FP32 accumulation]";
     }
 
     void add_weights(Pending &p, uint32_t src_len, uint32_t dst_len, uint32_t filter) {
@@ -846,6 +929,7 @@ std::unique_ptr<Executable> lower(const Program &prog, const zs_capabilities &ca
     E->device = caps.device;
     E->mode = caps.mode;
     E->use_graph = caps.use_graph != 0;
+    E->flags = caps.flags;
     if (caps.mode > ZS_MODE_PER_OP_F16) fail(ZS_ERR_INVALID_ARG, "unknown lowering mode");
     Planner pl(prog, *E);
     pl.run();

@@ -162,6 +162,7 @@ struct Step {
     int dst_slot = -1;
     int idx_x_slot = -1, idx_y_slot = -1, weight_slot = -1;
     int vfirst_slot = -1, vcount_slot = -1, vweight_slot = -1;   // RESAMPLE_2D vertical tables
+    int vimg_slot = -1, vimg_index_slot = -1;                   // RESAMPLE_2D tensor-core band images
     uint64_t copy_bytes = 0;
     std::string label;
 };
@@ -170,6 +171,7 @@ struct Executable {
     int device = 0;
     uint32_t mode = ZS_MODE_FUSED;
     bool use_graph = false;
+    uint32_t flags = 0;                                // ZS_CAP_* bits
     int sm_count = 148;
     std::vector<Slot> slots;
     std::vector<Step> steps;

@@ -24,60 +24,14 @@
 // for the copies it still has in flight and returns.
 #include "zs_device.cuh"
 #include "zs_kernels.h"
+#include "zs_ptx.cuh"
 
 #define ZS_RS_THREADS 256
 #define ZS_RS_GROUPS (ZS_RS_THREADS / ZS_RS_TW)   // 4 row groups of 64 columns
-#define ZS_RS_WAIT_NS 1000000000ull               // one second
-static_assert(ZS_RS_RB == 2 * ZS_RS_GROUPS, "two filtered rows per thread and batch");
+#define ZS_RS_HP (ZS_RS_TW + 1)                   // filtered-row pitch (float4): no bank conflicts
+static_assert(ZS_RS_RB == 8 && ZS_RS_THREADS == 256 && ZS_RS_TW == 64, "8 warps x (8 rows x 8 columns)");
 
 namespace {
-
-__device__ __forceinline__ uint32_t zs_smem_addr(const void *p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void zs_mbar_init(uint32_t bar, uint32_t count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
-}
-
-__device__ __forceinline__ void zs_mbar_expect_tx(uint32_t bar, uint32_t bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ bool zs_mbar_try_wait(uint32_t bar, uint32_t parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(bar), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-__device__ __forceinline__ uint64_t zs_globaltimer() {
-    uint64_t t;
-    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-    return t;
-}
-
-// Bounded wait for the phase of `bar` with the given parity to complete.
-__device__ __forceinline__ bool zs_mbar_wait(uint32_t bar, uint32_t parity) {
-    if (zs_mbar_try_wait(bar, parity)) return true;
-    const uint64_t t0 = zs_globaltimer();
-    for (;;) {
-        if (zs_mbar_try_wait(bar, parity)) return true;
-        if (zs_globaltimer() - t0 > ZS_RS_WAIT_NS) return false;
-    }
-}
-
-__device__ __forceinline__ void zs_bulk_g2s(uint32_t dst, const void *src, uint32_t bytes, uint32_t bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(dst),
-        "l"(src), "r"(bytes), "r"(bar)
-        : "memory");
-}
 
 // Geometry of one output tile: its source column segment and source row range.
 struct RsTile {
@@ -113,6 +67,47 @@ __device__ __forceinline__ float4 zs_rs_texel(const uint8_t *p, const ZsFormat &
     return zs_decode_raw(f, zs_load_raw(p, f.bpp));
 }
 
+__device__ __forceinline__ void zs_rs_fma(float4 &h, float w, float4 v) {
+    h.x = fmaf(w, v.x, h.x); h.y = fmaf(w, v.y, h.y);
+    h.z = fmaf(w, v.z, h.z); h.w = fmaf(w, v.w, h.w);
+}
+
+__device__ __forceinline__ float4 zs_rs_h2f4(uint32_t lo, uint32_t hi) {
+    const float2 a = __half22float2(*reinterpret_cast<const __half2 *>(&lo));
+    const float2 b = __half22float2(*reinterpret_cast<const __half2 *>(&hi));
+    return make_float4(a.x, a.y, b.x, b.y);
+}
+
+// One horizontally filtered texel: taps p[0 .. cnt) (texels of `bpp` bytes) weighted by
+// w[0 .. cnt), accumulated in tap order.  RGBA16F reads two texels per 16-byte load once
+// the address is 16-byte aligned.
+template <int SK>
+__device__ __forceinline__ float4 zs_rs_hfilter(const uint8_t *p, const float *w, int cnt, const ZsFormat &f) {
+    float4 h = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (SK == ZS_RSK_F16X4) {
+        int k = 0;
+        if (cnt > 0 && ((uintptr_t)p & 15) != 0) {
+            const uint2 v = *(const uint2 *)p;
+            zs_rs_fma(h, w[0], zs_rs_h2f4(v.x, v.y));
+            k = 1;
+        }
+#pragma unroll 2
+        for (; k + 1 < cnt; k += 2) {
+            const uint4 v = *(const uint4 *)(p + k * 8);
+            zs_rs_fma(h, w[k], zs_rs_h2f4(v.x, v.y));
+            zs_rs_fma(h, w[k + 1], zs_rs_h2f4(v.z, v.w));
+        }
+        if (k < cnt) {
+            const uint2 v = *(const uint2 *)(p + k * 8);
+            zs_rs_fma(h, w[k], zs_rs_h2f4(v.x, v.y));
+        }
+        return h;
+    }
+    const int bpp = f.bpp;
+    for (int k = 0; k < cnt; ++k) zs_rs_fma(h, w[k], zs_rs_texel<SK>(p + k * bpp, f));
+    return h;
+}
+
 }  // namespace
 
 template <int RPT, int SK>
@@ -122,17 +117,24 @@ __global__ void __launch_bounds__(ZS_RS_THREADS, 2) zs_resample2d_kernel(const _
     const ZsSource &s0 = a.src[0];
     const int bpp = s0.fmt.bpp;
     const int NS = a.stages;
-    const int rowbytes = ((a.max_span * bpp + 15) & ~15) + 16;
+    const int rowbytes = ZS_RS_ROWBYTES(a.max_span, bpp);                        // = 16 (mod 128)
     const int hstride = a.taps | 1;                                               // odd: no bank conflicts
     uint8_t *stage_base = zs_rs_smem;                                             // [NS][RB][rowbytes]
-    float4 *hrow = (float4 *)(zs_rs_smem + (size_t)NS * ZS_RS_RB * rowbytes);     // [2][RB][TW]
-    float *hws = (float *)(hrow + 2 * ZS_RS_RB * ZS_RS_TW);                       // [TW][hstride]
+    float4 *hrow = (float4 *)(zs_rs_smem + (size_t)NS * ZS_RS_RB * rowbytes);     // [2][RB][HP]
+    float *hws = (float *)(hrow + 2 * ZS_RS_RB * ZS_RS_HP);                       // [TW][hstride]
     float *vws = hws + ((ZS_RS_TW * hstride + 3) & ~3);                           // [TH][vtaps]
     uint64_t *bars = (uint64_t *)(vws + ((TH * a.vtaps + 3) & ~3));               // [NS]
     const int tiles_x = (a.width + ZS_RS_TW - 1) / ZS_RS_TW;
     const int tiles = tiles_x * ((a.height + TH - 1) / TH);
+    // Vertical phase: one column and RPT output rows per thread.
     const int col = threadIdx.x % ZS_RS_TW;
     const int rgrp = threadIdx.x / ZS_RS_TW;
+    // Horizontal phase: a warp filters 8 rows x 8 columns, lane = (row, column group); the
+    // staged rows are 16 (mod 128) bytes apart, so the 8 rows of one column hit 8
+    // different bank groups.
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int hb = lane & 7;
+    const int hc0 = warp * 8 + (lane >> 3), hc1 = hc0 + 4;
     const bool bulk = ((uintptr_t)s0.ptr & 15) == 0 && (s0.stride & 15) == 0;
     const bool producer = threadIdx.x == 0;
 
@@ -185,10 +187,14 @@ __global__ void __launch_bounds__(ZS_RS_THREADS, 2) zs_resample2d_kernel(const _
         const int ox = t.x0 + col;
         const bool colok = ox <= t.x1;
         const int shift = bulk ? (int)(((int64_t)t.cs0 * bpp) & 15) : 0;
-        int hfirst = 0, hcount = 0;
-        if (colok) {
-            hfirst = a.index_x[ox] - t.cs0;
-            hcount = a.index_y[ox];
+        int hf0 = 0, hn0 = 0, hf1 = 0, hn1 = 0;
+        if (t.x0 + hc0 <= t.x1) {
+            hf0 = a.index_x[t.x0 + hc0] - t.cs0;
+            hn0 = a.index_y[t.x0 + hc0];
+        }
+        if (t.x0 + hc1 <= t.x1) {
+            hf1 = a.index_x[t.x0 + hc1] - t.cs0;
+            hn1 = a.index_y[t.x0 + hc1];
         }
         // The tile's filter weights, staged once (the previous tile's readers are done).
         __syncthreads();
@@ -229,36 +235,11 @@ __global__ void __launch_bounds__(ZS_RS_THREADS, 2) zs_resample2d_kernel(const _
                 }
                 __syncthreads();
             }
-            float4 *hr = hrow + (g & 1u) * (ZS_RS_RB * ZS_RS_TW);
-            if (!timed_out && colok) {
-                // Two rows per thread (rgrp, rgrp + GROUPS) share each weight load.
-                const float *wk = hws + col * hstride;
-                const uint8_t *p0 = sb + rgrp * rowbytes + shift + hfirst * bpp;
-                if (rgrp + ZS_RS_GROUPS < nb) {
-                    const uint8_t *p1 = p0 + ZS_RS_GROUPS * rowbytes;
-                    float4 h0 = make_float4(0.f, 0.f, 0.f, 0.f), h1 = h0;
-#pragma unroll 2
-                    for (int k = 0; k < hcount; ++k) {
-                        const float w = wk[k];
-                        const float4 v0 = zs_rs_texel<SK>(p0 + k * bpp, s0.fmt);
-                        const float4 v1 = zs_rs_texel<SK>(p1 + k * bpp, s0.fmt);
-                        h0.x = fmaf(w, v0.x, h0.x); h0.y = fmaf(w, v0.y, h0.y);
-                        h0.z = fmaf(w, v0.z, h0.z); h0.w = fmaf(w, v0.w, h0.w);
-                        h1.x = fmaf(w, v1.x, h1.x); h1.y = fmaf(w, v1.y, h1.y);
-                        h1.z = fmaf(w, v1.z, h1.z); h1.w = fmaf(w, v1.w, h1.w);
-                    }
-                    hr[rgrp * ZS_RS_TW + col] = h0;
-                    hr[(rgrp + ZS_RS_GROUPS) * ZS_RS_TW + col] = h1;
-                } else if (rgrp < nb) {
-                    float4 h0 = make_float4(0.f, 0.f, 0.f, 0.f);
-                    for (int k = 0; k < hcount; ++k) {
-                        const float w = wk[k];
-                        const float4 v0 = zs_rs_texel<SK>(p0 + k * bpp, s0.fmt);
-                        h0.x = fmaf(w, v0.x, h0.x); h0.y = fmaf(w, v0.y, h0.y);
-                        h0.z = fmaf(w, v0.z, h0.z); h0.w = fmaf(w, v0.w, h0.w);
-                    }
-                    hr[rgrp * ZS_RS_TW + col] = h0;
-                }
+            float4 *hr = hrow + (g & 1u) * (ZS_RS_RB * ZS_RS_HP);
+            if (!timed_out && hb < nb) {
+                const uint8_t *rp = sb + hb * rowbytes + shift;
+                if (hn0 > 0) hr[hb * ZS_RS_HP + hc0] = zs_rs_hfilter<SK>(rp + hf0 * bpp, hws + hc0 * hstride, hn0, s0.fmt);
+                if (hn1 > 0) hr[hb * ZS_RS_HP + hc1] = zs_rs_hfilter<SK>(rp + hf1 * bpp, hws + hc1 * hstride, hn1, s0.fmt);
             }
             if (__syncthreads_or(timed_out)) {
                 // Give up: record it, let the copies still in flight land, and return.
@@ -278,7 +259,7 @@ __global__ void __launch_bounds__(ZS_RS_THREADS, 2) zs_resample2d_kernel(const _
                     const float *vw = vws + (rgrp + j * ZS_RS_GROUPS) * a.vtaps;
                     for (int sy = lo; sy < hi; ++sy) {
                         const float w = vw[sy - vf[j]];
-                        const float4 h = hr[(sy - rs) * ZS_RS_TW + col];
+                        const float4 h = hr[(sy - rs) * ZS_RS_HP + col];
                         acc[j].x = fmaf(w, h.x, acc[j].x); acc[j].y = fmaf(w, h.y, acc[j].y);
                         acc[j].z = fmaf(w, h.z, acc[j].z); acc[j].w = fmaf(w, h.w, acc[j].w);
                     }
@@ -305,9 +286,9 @@ namespace {
 
 // Shared memory of one CTA for `stages` staged batches.
 size_t rs_smem_bytes(const ZsRasterArgs &a, int stages) {
-    const size_t rowbytes = (size_t)(((a.max_span * a.src[0].fmt.bpp + 15) & ~15) + 16);
+    const size_t rowbytes = (size_t)ZS_RS_ROWBYTES(a.max_span, a.src[0].fmt.bpp);
     const size_t hw = (size_t)((ZS_RS_TW * (a.taps | 1) + 3) & ~3), vw = (size_t)((a.tile_rows * a.vtaps + 3) & ~3);
-    return (size_t)stages * ZS_RS_RB * rowbytes + 2 * ZS_RS_RB * ZS_RS_TW * sizeof(float4) + (hw + vw) * sizeof(float) +
+    return (size_t)stages * ZS_RS_RB * rowbytes + 2 * ZS_RS_RB * ZS_RS_HP * sizeof(float4) + (hw + vw) * sizeof(float) +
            stages * sizeof(uint64_t);
 }
 
@@ -344,6 +325,7 @@ cudaError_t launch_rs_rows(const ZsRasterArgs &a, size_t smem, int sm_count, cud
 }  // namespace
 
 cudaError_t launch_resample2d(const ZsRasterArgs &args, int sm_count, cudaStream_t stream) {
+    if (resample_tc_usable(args)) return launch_resample_tc(args, sm_count, stream);
     ZsRasterArgs a = args;
     if (a.max_span < 1 || a.src[0].fmt.bpp < 1) return cudaErrorInvalidValue;
     const size_t one = rs_smem_bytes(a, 1) - rs_smem_bytes(a, 0);

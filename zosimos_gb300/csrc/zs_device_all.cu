@@ -4,6 +4,7 @@
 #include "zs_tables.cu"
 #include "k_raster.cu"
 #include "k_resample.cu"
+#include "k_resample_tc.cu"
 #include "k_chain.cu"
 #include "k_layers.cu"
 #include "k_batch.cu"

@@ -16,6 +16,10 @@ cudaError_t launch_raster(const ZsRasterArgs &args, int sm_count, cudaStream_t s
 // Both passes of a separable resample in one tiled launch (k_resample.cu); launch_raster
 // dispatches ZS_PR_RESAMPLE_2D here.
 cudaError_t launch_resample2d(const ZsRasterArgs &args, int sm_count, cudaStream_t stream);
+// The tensor-core form of RESAMPLE_2D (k_resample_tc.cu), usable when planned (tc_tw > 0),
+// the source is RGBA16F with 16-byte aligned rows and the TMA encoder is available.
+bool resample_tc_usable(const ZsRasterArgs &args);
+cudaError_t launch_resample_tc(const ZsRasterArgs &args, int sm_count, cudaStream_t stream);
 
 // Fused colour chain in canonical form, RGBA8 in / RGBA8 out (k_chain.cu).
 // Returns cudaErrorNotSupported when no specialisation exists for the formats.

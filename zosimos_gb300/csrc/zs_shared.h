@@ -121,6 +121,11 @@ struct ZsRasterArgs {
     int32_t max_span;         // widest source column span of one output tile
     int32_t tile_rows;        // output rows per tile: 8, 16 or 32
     int32_t stages;           // staged batches of source rows (set by the launcher)
+    // RESAMPLE_2D on the tensor cores (k_resample_tc.cu; tc_tw 0: not planned)
+    const uint8_t *vimg;          // vertical band matrices: [chunk][128 rows][64 f16], 128-byte swizzle
+    const int32_t *vimg_index;    // per band of 128 output rows: first chunk, chunk count
+    int32_t tc_tw;                // output columns per tile
+    int32_t tc_atoms;             // 64-element column blocks of source staged per tile (N = 64 * atoms)
     // destination
     uint8_t *dst;
     int64_t dst_stride;
@@ -136,8 +141,18 @@ struct ZsRasterArgs {
 #define ZS_RS_TW 64
 #define ZS_RS_TH 32
 #define ZS_RS_RB 8
+// Pitch of one staged source row: room for max_span texels plus the 16-byte alignment
+// remainder, rounded so that consecutive rows start 16 bytes apart modulo 128.
+#define ZS_RS_ROWBYTES(span, bpp) ((((span) * (bpp) + 16 + 127) & ~127) + 16)
 #define ZS_RS_MAX_SMEM (200 * 1024)
 #define ZS_RS_STAGE_BUDGET (96 * 1024)   // staged source rows of one CTA (2 CTAs per SM)
+
+// Tensor-core resample: bands of 128 output rows (the MMA's M), chunks of 64 source rows
+// (the K of one 128-byte swizzle atom), at most 4 atoms of 64 source elements (N <= 256).
+#define ZS_TC_M 128
+#define ZS_TC_K 64
+#define ZS_TC_MAX_ATOMS 4
+#define ZS_TC_CHUNK_BYTES (ZS_TC_M * ZS_TC_K * 2)
 
 // Bits of the device status word.
 #define ZS_DEVSTAT_WAIT_TIMEOUT 1u   // an mbarrier wait on a bulk copy exceeded its limit
