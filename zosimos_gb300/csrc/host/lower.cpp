@@ -758,9 +758,17 @@ struct Planner {
         auto p = new_pending(ZS_PR_RESAMPLE_2D, d.width, d.height, "resample 2d");
         set_src(*p, 0, op.a);
         p->a.tile_rows = th;
-        p->idx_x_slot = table_slot(hf.data(), hf.size() * 4);
-        p->idx_y_slot = table_slot(hc.data(), hc.size() * 4);
-        p->weight_slot = table_slot(hw.data(), hw.size() * 4);
+        // Horizontal tables padded with zero rows to a multiple of 32 output columns: the
+        // tensor-core kernel copies whole tiles of them into shared memory.
+        const size_t padded = (d.width + 31) / 32 * 32;
+        std::vector<int32_t> hfp(hf), hcp(hc);
+        std::vector<float> hwp(hw);
+        hfp.resize(padded, 0);
+        hcp.resize(padded, 0);
+        hwp.resize(padded * (size_t)htaps, 0.f);
+        p->idx_x_slot = table_slot(hfp.data(), hfp.size() * 4);
+        p->idx_y_slot = table_slot(hcp.data(), hcp.size() * 4);
+        p->weight_slot = table_slot(hwp.data(), hwp.size() * 4);
         p->vfirst_slot = table_slot(vf.data(), vf.size() * 4);
         p->vcount_slot = table_slot(vc.data(), vc.size() * 4);
         p->vweight_slot = table_slot(vw.data(), vw.size() * 4);
@@ -768,7 +776,8 @@ struct Planner {
         p->a.vtaps = vtaps;
         p->a.max_span = span;
         const Slot &ss = E.slots[vals[op.a].slot];
-        if (!(E.flags & ZS_CAP_SIMT_RESAMPLE) && vals[op.a].fmt.fast == ZS_FAST_F16X4 && ss.stride % 16 == 0)
+        if (!(E.flags & ZS_CAP_SIMT_RESAMPLE) && vals[op.a].fmt.fast == ZS_FAST_F16X4 && ss.stride % 16 == 0 &&
+            htaps <= 64)
             plan_resample_tc(*p, hf, hc, vf, vc, vw, vtaps, d);
         set_pending(r, std::move(p));
         return true;

@@ -17,7 +17,9 @@
 // Epilogue: every output row is one TMEM lane; 16 warps (four per lane quarter) take the
 // tile's output columns, read the horizontal taps of their column from TMEM
 // (tcgen05.ld 32x32b.x4 = the 4 channels of one source pixel), apply the FP32 horizontal
-// weights in tap order, run the fused pixel program and store.
+// weights in tap order, run the fused pixel program and store.  The tile's horizontal
+// weights and tap windows arrive in shared memory by bulk copy with the tile (one table
+// per accumulator buffer), so the epilogue issues no global loads.
 //
 // Roles: warp 0 lane 0 issues the copies (4-stage ring of {A chunk, B atoms}), warp 1
 // allocates TMEM and its lane 0 issues the MMAs, warps 2..17 are the epilogue.  All
@@ -40,7 +42,10 @@
 #define ZS_TC_STAGE_BYTES (ZS_TC_CHUNK_BYTES + ZS_TC_MAX_ATOMS * ZS_TC_ATOM_BYTES)
 #define ZS_TC_TMEM_COLS 512
 #define ZS_TC_ACC_COLS 256
-#define ZS_TC_SMEM (ZS_TC_STAGES * ZS_TC_STAGE_BYTES + 1024 + 256)
+// Per-tile horizontal tables (weights [tw][taps], first tap [tw], tap count [tw]) for tw <= 32,
+// taps <= 64, one per accumulator buffer.
+#define ZS_TC_TAB_BYTES ((32 * 64 + 2 * 32) * 4)
+#define ZS_TC_SMEM (ZS_TC_STAGES * ZS_TC_STAGE_BYTES + 2 * ZS_TC_TAB_BYTES + 1024 + 256)
 
 static_assert(ZS_TC_STAGE_BYTES % 1024 == 0, "stages stay 1024-byte aligned (128-byte swizzle atoms)");
 
@@ -116,11 +121,13 @@ __global__ void __launch_bounds__(ZS_TC_THREADS, 1)
     zs_resample_tc_kernel(const __grid_constant__ ZsRasterArgs a, const __grid_constant__ CUtensorMap tmap) {
     extern __shared__ __align__(1024) uint8_t zs_tc_smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)zs_tc_smem_raw + 1023) & ~(uintptr_t)1023);
-    uint64_t *full = (uint64_t *)(smem + ZS_TC_STAGES * ZS_TC_STAGE_BYTES);
+    uint8_t *tab = smem + ZS_TC_STAGES * ZS_TC_STAGE_BYTES;                // [2][ZS_TC_TAB_BYTES]
+    uint64_t *full = (uint64_t *)(tab + 2 * ZS_TC_TAB_BYTES);
     uint64_t *empty = full + ZS_TC_STAGES;
     uint64_t *tfull = empty + ZS_TC_STAGES;    // [2] accumulator ready
-    uint64_t *tempty = tfull + 2;              // [2] accumulator drained
-    uint64_t *drain = tempty + 2;
+    uint64_t *tempty = tfull + 2;              // [2] accumulator drained (and its tables free)
+    uint64_t *tabfull = tempty + 2;            // [2] tile tables landed
+    uint64_t *drain = tabfull + 2;
     uint32_t *tmem_slot = (uint32_t *)(drain + 1);
     volatile int *abort_flag = (volatile int *)(tmem_slot + 1);
 
@@ -137,6 +144,7 @@ __global__ void __launch_bounds__(ZS_TC_THREADS, 1)
         for (int b = 0; b < 2; ++b) {
             zs_mbar_init(zs_smem_addr(tfull + b), 1);
             zs_mbar_init(zs_smem_addr(tempty + b), ZS_TC_EPI_WARPS);
+            zs_mbar_init(zs_smem_addr(tabfull + b), 1);
         }
         zs_mbar_init(zs_smem_addr(drain), 1);
         *abort_flag = 0;
@@ -156,12 +164,25 @@ __global__ void __launch_bounds__(ZS_TC_THREADS, 1)
 
     if (warp == 0 && lane == 0) {
         // ---------------------------------------------------------------- copies
-        uint32_t it = 0;
+        uint32_t it = 0, lt = 0;
         const uint32_t tx = ZS_TC_CHUNK_BYTES + (uint32_t)atoms * ZS_TC_ATOM_BYTES;
-        for (int t = blockIdx.x; t < tiles && !*abort_flag; t += gridDim.x) {
+        const uint32_t wbytes = (uint32_t)(a.tc_tw * a.taps * 4), ibytes = (uint32_t)(a.tc_tw * 4);
+        for (int t = blockIdx.x; t < tiles && !*abort_flag; t += gridDim.x, ++lt) {
             const TcTile tt = tc_tile(a, t, tiles_x);
             const int first = a.vimg_index[2 * tt.band], nk = a.vimg_index[2 * tt.band + 1];
             const int rbase = a.vfirst[tt.band * ZS_TC_M];
+            // The tile's horizontal tables go to the buffer of its accumulator, free once the
+            // epilogue of the tile two before has finished.
+            const uint32_t ab = lt & 1u;
+            if (!tc_wait(zs_smem_addr(tempty + ab), ((lt >> 1) & 1u) ^ 1u, abort_flag)) break;
+            {
+                const uint32_t bar = zs_smem_addr(tabfull + ab);
+                const uint32_t tb = zs_smem_addr(tab + ab * ZS_TC_TAB_BYTES);
+                zs_mbar_expect_tx(bar, wbytes + 2 * ibytes);
+                zs_bulk_g2s(tb, a.weights + (int64_t)tt.x0 * a.taps, wbytes, bar);
+                zs_bulk_g2s(tb + wbytes, a.index_x + tt.x0, ibytes, bar);
+                zs_bulk_g2s(tb + wbytes + ibytes, a.index_y + tt.x0, ibytes, bar);
+            }
             bool ok = true;
             for (int kc = 0; kc < nk; ++kc, ++it) {
                 const int s = (int)(it % ZS_TC_STAGES);
@@ -184,6 +205,7 @@ __global__ void __launch_bounds__(ZS_TC_THREADS, 1)
             const uint32_t lo = it > ZS_TC_STAGES ? it - ZS_TC_STAGES : 0;
             for (uint32_t j = lo; j < it; ++j)
                 zs_mbar_wait(zs_smem_addr(full + (j % ZS_TC_STAGES)), (j / ZS_TC_STAGES) & 1u);
+            for (uint32_t j = lt > 2 ? lt - 2 : 0; j < lt; ++j) zs_mbar_wait(zs_smem_addr(tabfull + (j & 1u)), (j >> 1) & 1u);
         }
     } else if (warp == 1 && lane == 0) {
         // ---------------------------------------------------------------- MMAs
@@ -226,27 +248,36 @@ __global__ void __launch_bounds__(ZS_TC_THREADS, 1)
         // ---------------------------------------------------------------- epilogue
         const int e = warp - 2;
         const int quarter = warp & 3;      // TMEM lanes this warp may read
-        const int part = e >> 2;           // which of the 4 interleaved column subsets
+        const int part = e >> 2;           // this warp's outputs: x0 + part + 4 i
         const int m = quarter * 32 + lane;
         uint32_t lt = 0;
         for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++lt) {
             const TcTile tt = tc_tile(a, t, tiles_x);
             const uint32_t ab = lt & 1u;
+            if (!tc_wait(zs_smem_addr(tabfull + ab), (lt >> 1) & 1u, abort_flag)) break;
             if (!tc_wait(zs_smem_addr(tfull + ab), (lt >> 1) & 1u, abort_flag)) break;
             tc_fence_after();
+            const float *tw_w = (const float *)(tab + ab * ZS_TC_TAB_BYTES);
+            const int *tw_first = (const int *)(tw_w + a.tc_tw * a.taps);
+            const int *tw_cnt = tw_first + a.tc_tw;
             const int oy = tt.band * ZS_TC_M + m;
             const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16) + ab * ZS_TC_ACC_COLS;
             for (int ox = tt.x0 + part; ox < min(tt.x0 + a.tc_tw, a.width); ox += 4) {
-                const int cnt = a.index_y[ox];
-                const uint32_t col = (uint32_t)(a.index_x[ox] - tt.cs0) * 4u;
-                const float *w = a.weights + (int64_t)ox * a.taps;
-                float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+                const int oxl = ox - tt.x0;
+                const int cnt = tw_cnt[oxl];
+                const uint32_t col = (uint32_t)(tw_first[oxl] - tt.cs0) * 4u;
+                const float *w = tw_w + oxl * a.taps;
+                float2 a01 = make_float2(0.f, 0.f), a23 = make_float2(0.f, 0.f);
                 for (int k0 = 0; k0 < cnt; k0 += 8) {
                     const int n = min(8, cnt - k0);
                     uint32_t r[8][4];
+                    float wk[8];
 #pragma unroll
                     for (int j = 0; j < 8; ++j)
-                        if (j < n) tc_ld4(trow + col + 4u * (uint32_t)(k0 + j), r[j]);
+                        if (j < n) {
+                            tc_ld4(trow + col + 4u * (uint32_t)(k0 + j), r[j]);
+                            wk[j] = w[k0 + j];
+                        }
                     tc_wait_ld();
                     // Tie the loaded registers to the wait so that no use moves above it.
 #pragma unroll
@@ -256,15 +287,13 @@ __global__ void __launch_bounds__(ZS_TC_THREADS, 1)
 #pragma unroll
                     for (int j = 0; j < 8; ++j)
                         if (j < n) {
-                            const float wk = __ldg(w + k0 + j);
-                            acc.x = fmaf(wk, __uint_as_float(r[j][0]), acc.x);
-                            acc.y = fmaf(wk, __uint_as_float(r[j][1]), acc.y);
-                            acc.z = fmaf(wk, __uint_as_float(r[j][2]), acc.z);
-                            acc.w = fmaf(wk, __uint_as_float(r[j][3]), acc.w);
+                            const float2 w2 = make_float2(wk[j], wk[j]);
+                            a01 = __ffma2_rn(w2, make_float2(__uint_as_float(r[j][0]), __uint_as_float(r[j][1])), a01);
+                            a23 = __ffma2_rn(w2, make_float2(__uint_as_float(r[j][2]), __uint_as_float(r[j][3])), a23);
                         }
                 }
                 if (oy < a.height) {
-                    float4 r2 = make_float4(0.f, 0.f, 0.f, 0.f);
+                    float4 acc = make_float4(a01.x, a01.y, a23.x, a23.y), r2 = make_float4(0.f, 0.f, 0.f, 0.f);
                     zs_run_program(a.prog, a.fmts, acc, r2);
                     uint8_t *dp = a.dst + (int64_t)oy * a.dst_stride + (int64_t)ox * a.dst_fmt.bpp;
                     zs_store_raw(dp, a.dst_fmt.bpp, zs_encode_raw(a.dst_fmt, acc));
