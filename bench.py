@@ -391,12 +391,15 @@ def workload_resample(args, stream, sh):
         for factor in (2.0, 3.7, 8.0):
             ow = int(round(n / factor))
             c, _, _ = resample(n, n, ow, ow, filt)
-            exes = [zs.Linker.from_included().compile(c).lower_to(zs.Capabilities(mode=m))
-                    for m in (zs.Mode.Fused, zs.Mode.PerOpF32)]
+            caps = [zs.Capabilities(mode=zs.Mode.Fused), zs.Capabilities(mode=zs.Mode.PerOpF32),
+                    zs.Capabilities(mode=zs.Mode.Fused, simt_resample=True)]
+            exes = [zs.Linker.from_included().compile(c).lower_to(cp) for cp in caps]
             dst = zs.DeviceBuffer(ow * ow * 8)
             ms = [timed(lambda i, e=e: e.run_device([src.ptr], [dst.ptr], sh), steps, args.warmup) for e in exes]
+            tensor = "tensor cores" in exes[0].describe()
             _line(f"resample {fname} 8192^2 RGBA16F /{factor} -> {ow}^2", n * n, n * n * 8 + ow * ow * 8,
-                  ms[0], ms[1])
+                  ms[0], ms[1], {"kernel": "tcgen05 band MMA + TMEM epilogue" if tensor else "FP32 SIMT tiled",
+                                 "fused_simt_fp32_ms": round(ms[2], 4)})
             dst.free()
     c, _, _, _ = rotation(n, n, 17.0)
     exes = [zs.Linker.from_included().compile(c).lower_to(zs.Capabilities(mode=m))

@@ -21,8 +21,9 @@
 // weights and tap windows arrive in shared memory by bulk copy with the tile (one table
 // per accumulator buffer), so the epilogue issues no global loads.
 //
-// Roles: warp 0 lane 0 issues the copies (4-stage ring of {A chunk, B atoms}), warp 1
-// allocates TMEM and its lane 0 issues the MMAs, warps 2..17 are the epilogue.  All
+// Roles: warp 0 lane 0 issues the row copies (4-stage ring of {A chunk, B atoms}), warp 1
+// allocates TMEM and its lane 0 copies each tile's horizontal tables and issues the MMAs,
+// warps 2..17 are the epilogue.  All
 // mbarrier waits are bounded (one second); a wait that gives up raises an abort flag that
 // every role polls, sets ZS_DEVSTAT_WAIT_TIMEOUT, and the CTA drains its own copies and
 // MMAs (bounded) and frees its TMEM before returning.
@@ -164,25 +165,12 @@ __global__ void __launch_bounds__(ZS_TC_THREADS, 1)
 
     if (warp == 0 && lane == 0) {
         // ---------------------------------------------------------------- copies
-        uint32_t it = 0, lt = 0;
+        uint32_t it = 0;
         const uint32_t tx = ZS_TC_CHUNK_BYTES + (uint32_t)atoms * ZS_TC_ATOM_BYTES;
-        const uint32_t wbytes = (uint32_t)(a.tc_tw * a.taps * 4), ibytes = (uint32_t)(a.tc_tw * 4);
-        for (int t = blockIdx.x; t < tiles && !*abort_flag; t += gridDim.x, ++lt) {
+        for (int t = blockIdx.x; t < tiles && !*abort_flag; t += gridDim.x) {
             const TcTile tt = tc_tile(a, t, tiles_x);
             const int first = a.vimg_index[2 * tt.band], nk = a.vimg_index[2 * tt.band + 1];
             const int rbase = a.vfirst[tt.band * ZS_TC_M];
-            // The tile's horizontal tables go to the buffer of its accumulator, free once the
-            // epilogue of the tile two before has finished.
-            const uint32_t ab = lt & 1u;
-            if (!tc_wait(zs_smem_addr(tempty + ab), ((lt >> 1) & 1u) ^ 1u, abort_flag)) break;
-            {
-                const uint32_t bar = zs_smem_addr(tabfull + ab);
-                const uint32_t tb = zs_smem_addr(tab + ab * ZS_TC_TAB_BYTES);
-                zs_mbar_expect_tx(bar, wbytes + 2 * ibytes);
-                zs_bulk_g2s(tb, a.weights + (int64_t)tt.x0 * a.taps, wbytes, bar);
-                zs_bulk_g2s(tb + wbytes, a.index_x + tt.x0, ibytes, bar);
-                zs_bulk_g2s(tb + wbytes + ibytes, a.index_y + tt.x0, ibytes, bar);
-            }
             bool ok = true;
             for (int kc = 0; kc < nk; ++kc, ++it) {
                 const int s = (int)(it % ZS_TC_STAGES);
@@ -205,18 +193,29 @@ __global__ void __launch_bounds__(ZS_TC_THREADS, 1)
             const uint32_t lo = it > ZS_TC_STAGES ? it - ZS_TC_STAGES : 0;
             for (uint32_t j = lo; j < it; ++j)
                 zs_mbar_wait(zs_smem_addr(full + (j % ZS_TC_STAGES)), (j / ZS_TC_STAGES) & 1u);
-            for (uint32_t j = lt > 2 ? lt - 2 : 0; j < lt; ++j) zs_mbar_wait(zs_smem_addr(tabfull + (j & 1u)), (j >> 1) & 1u);
         }
     } else if (warp == 1 && lane == 0) {
         // ---------------------------------------------------------------- MMAs
-        uint32_t it = 0, lt = 0;
+        uint32_t it = 0, lt = 0, tabs = 0;
         const uint32_t idesc = tc_idesc(64 * atoms);
+        const uint32_t wbytes = (uint32_t)(a.tc_tw * a.taps * 4), ibytes = (uint32_t)(a.tc_tw * 4);
         for (int t = blockIdx.x; t < tiles && !*abort_flag; t += gridDim.x, ++lt) {
-            const int band = t / tiles_x;
-            const int nk = a.vimg_index[2 * band + 1];
+            const TcTile tt = tc_tile(a, t, tiles_x);
+            const int nk = a.vimg_index[2 * tt.band + 1];
             const uint32_t ab = lt & 1u;
             if (!tc_wait(zs_smem_addr(tempty + ab), ((lt >> 1) & 1u) ^ 1u, abort_flag)) break;
             tc_fence_after();
+            {
+                // The tile's horizontal weights and tap windows, into the table buffer of its
+                // accumulator (free now that the epilogue of the tile two before is done).
+                const uint32_t bar = zs_smem_addr(tabfull + ab);
+                const uint32_t tb = zs_smem_addr(tab + ab * ZS_TC_TAB_BYTES);
+                zs_mbar_expect_tx(bar, wbytes + 2 * ibytes);
+                zs_bulk_g2s(tb, a.weights + (int64_t)tt.x0 * a.taps, wbytes, bar);
+                zs_bulk_g2s(tb + wbytes, a.index_x + tt.x0, ibytes, bar);
+                zs_bulk_g2s(tb + wbytes + ibytes, a.index_y + tt.x0, ibytes, bar);
+                ++tabs;
+            }
             const uint32_t d = tmem + ab * ZS_TC_ACC_COLS;
             bool ok = true;
             for (int kc = 0; kc < nk; ++kc, ++it) {
@@ -241,9 +240,12 @@ __global__ void __launch_bounds__(ZS_TC_THREADS, 1)
             if (!ok) break;
             tc_commit(zs_smem_addr(tfull + ab));
         }
-        // Nothing of this thread's may still run when the TMEM is freed.
+        // Nothing of this thread's may still run when the TMEM and shared memory go.
         tc_commit(zs_smem_addr(drain));
         zs_mbar_wait(zs_smem_addr(drain), 0);
+        if (*abort_flag)
+            for (uint32_t j = tabs > 2 ? tabs - 2 : 0; j < tabs; ++j)
+                zs_mbar_wait(zs_smem_addr(tabfull + (j & 1u)), (j >> 1) & 1u);
     } else if (warp >= 2) {
         // ---------------------------------------------------------------- epilogue
         const int e = warp - 2;
@@ -267,17 +269,19 @@ __global__ void __launch_bounds__(ZS_TC_THREADS, 1)
                 const int cnt = tw_cnt[oxl];
                 const uint32_t col = (uint32_t)(tw_first[oxl] - tt.cs0) * 4u;
                 const float *w = tw_w + oxl * a.taps;
+                // Two accumulator pairs (even and odd taps) halve the FMA dependency chains.
                 float2 a01 = make_float2(0.f, 0.f), a23 = make_float2(0.f, 0.f);
+                float2 b01 = make_float2(0.f, 0.f), b23 = make_float2(0.f, 0.f);
                 for (int k0 = 0; k0 < cnt; k0 += 8) {
                     const int n = min(8, cnt - k0);
                     uint32_t r[8][4];
                     float wk[8];
 #pragma unroll
                     for (int j = 0; j < 8; ++j)
-                        if (j < n) {
-                            tc_ld4(trow + col + 4u * (uint32_t)(k0 + j), r[j]);
-                            wk[j] = w[k0 + j];
-                        }
+                        if (j < n) tc_ld4(trow + col + 4u * (uint32_t)(k0 + j), r[j]);
+#pragma unroll
+                    for (int j = 0; j < 8; ++j)
+                        if (j < n) wk[j] = w[k0 + j];
                     tc_wait_ld();
                     // Tie the loaded registers to the wait so that no use moves above it.
 #pragma unroll
@@ -288,12 +292,20 @@ __global__ void __launch_bounds__(ZS_TC_THREADS, 1)
                     for (int j = 0; j < 8; ++j)
                         if (j < n) {
                             const float2 w2 = make_float2(wk[j], wk[j]);
-                            a01 = __ffma2_rn(w2, make_float2(__uint_as_float(r[j][0]), __uint_as_float(r[j][1])), a01);
-                            a23 = __ffma2_rn(w2, make_float2(__uint_as_float(r[j][2]), __uint_as_float(r[j][3])), a23);
+                            const float2 v01 = make_float2(__uint_as_float(r[j][0]), __uint_as_float(r[j][1]));
+                            const float2 v23 = make_float2(__uint_as_float(r[j][2]), __uint_as_float(r[j][3]));
+                            if (j & 1) {
+                                b01 = __ffma2_rn(w2, v01, b01);
+                                b23 = __ffma2_rn(w2, v23, b23);
+                            } else {
+                                a01 = __ffma2_rn(w2, v01, a01);
+                                a23 = __ffma2_rn(w2, v23, a23);
+                            }
                         }
                 }
                 if (oy < a.height) {
-                    float4 acc = make_float4(a01.x, a01.y, a23.x, a23.y), r2 = make_float4(0.f, 0.f, 0.f, 0.f);
+                    float4 acc = make_float4(a01.x + b01.x, a01.y + b01.y, a23.x + b23.x, a23.y + b23.y);
+                    float4 r2 = make_float4(0.f, 0.f, 0.f, 0.f);
                     zs_run_program(a.prog, a.fmts, acc, r2);
                     uint8_t *dp = a.dst + (int64_t)oy * a.dst_stride + (int64_t)ox * a.dst_fmt.bpp;
                     zs_store_raw(dp, a.dst_fmt.bpp, zs_encode_raw(a.dst_fmt, acc));
