@@ -163,7 +163,8 @@ def test_resample_upscale():
 
 @pytest.mark.parametrize("filt", [zs.Filter.Lanczos3, zs.Filter.Box, zs.Filter.Triangle])
 @pytest.mark.parametrize("src,out", [((1024, 768), (512, 384)), ((1024, 768), (277, 208)), ((640, 300), (640, 131)),
-                                     ((200, 130), (317, 200)), ((518, 390), (129, 97))])
+                                     ((200, 130), (317, 200)), ((518, 390), (129, 97)), ((1024, 768), (128, 96)),
+                                     ((1040, 300), (130, 37))])
 def test_resample_tensor_cores(filt, src, out):
     # The vertical pass on the tensor cores (f16 band matrices, FP32 accumulation in TMEM),
     # against FP64, and against the FP32 SIMT kernel on the same input.
@@ -182,6 +183,7 @@ def test_resample_tensor_core_plan():
     # RGBA16F sources with 16-byte rows take the tensor-core kernel where the staged columns
     # of a tile fit one MMA; the SIMT flag and odd widths keep the FP32 SIMT kernel.
     assert "tensor cores" in P.resample_plan(1024, 768, (512, 384), zs.Filter.Lanczos3)
+    assert "tensor cores" in P.resample_plan(1024, 768, (128, 96), zs.Filter.Lanczos3)   # 8 atoms, one accumulator
     assert "tensor cores" not in P.resample_plan(1024, 768, (512, 384), zs.Filter.Lanczos3, simt_resample=True)
     assert "tensor cores" not in P.resample_plan(1023, 768, (512, 384), zs.Filter.Lanczos3)
 

@@ -816,18 +816,23 @@ struct Planner {
                           const std::vector<int32_t> &vf, const std::vector<int32_t> &vc, const std::vector<float> &vw,
                           int vtaps, const Desc &d) {
         const int dw = (int)d.width, dh = (int)d.height;
+        // Prefer tiles whose span fits 4 atoms (two accumulators: the epilogue of one tile
+        // overlaps the MMAs of the next), else up to 8 atoms (one 512-column accumulator).
         int tw = 0, span = 0;
-        for (int cand : {32, 16, 8}) {
-            int sp = 0;
-            for (int x0 = 0; x0 < dw; x0 += cand) {
-                const int x1 = std::min(x0 + cand, dw) - 1;
-                sp = std::max(sp, hf[x1] + hc[x1] - (hf[x0] & ~1));
+        for (int max_atoms : {4, ZS_TC_MAX_ATOMS}) {
+            for (int cand : {32, 16, 8}) {
+                int sp = 0;
+                for (int x0 = 0; x0 < dw; x0 += cand) {
+                    const int x1 = std::min(x0 + cand, dw) - 1;
+                    sp = std::max(sp, hf[x1] + hc[x1] - (hf[x0] & ~1));
+                }
+                if (sp * 4 <= 64 * max_atoms) {
+                    tw = cand;
+                    span = sp;
+                    break;
+                }
             }
-            if (sp * 4 <= 64 * ZS_TC_MAX_ATOMS) {
-                tw = cand;
-                span = sp;
-                break;
-            }
+            if (tw) break;
         }
         if (!tw) return;
         const int bands = (dh + ZS_TC_M - 1) / ZS_TC_M;

@@ -36,19 +36,24 @@
 #include "zs_kernels.h"
 #include "zs_ptx.cuh"
 
-#define ZS_TC_STAGES 4
+#define ZS_TC_STAGES 4                                                     // ring slots (narrow tiles)
 #define ZS_TC_EPI_WARPS 16
 #define ZS_TC_THREADS (64 + 32 * ZS_TC_EPI_WARPS)
 #define ZS_TC_ATOM_BYTES (ZS_TC_K * 128)                                   // 64 rows x 128 B
-#define ZS_TC_STAGE_BYTES (ZS_TC_CHUNK_BYTES + ZS_TC_MAX_ATOMS * ZS_TC_ATOM_BYTES)
+// Narrow tiles (<= 4 atoms): 4 stages of {A, 4 atoms}, two 256-column accumulators.
+// Wide tiles (5..8 atoms): 2 stages of {A, 8 atoms}, one 512-column accumulator filled by
+// two N <= 256 MMAs per K step.
+#define ZS_TC_STAGE_BYTES (ZS_TC_CHUNK_BYTES + 4 * ZS_TC_ATOM_BYTES)
+#define ZS_TC_WIDE_STAGE_BYTES (ZS_TC_CHUNK_BYTES + 8 * ZS_TC_ATOM_BYTES)
 #define ZS_TC_TMEM_COLS 512
-#define ZS_TC_ACC_COLS 256
 // Per-tile horizontal tables (weights [tw][taps], first tap [tw], tap count [tw]) for tw <= 32,
 // taps <= 64, one per accumulator buffer.
 #define ZS_TC_TAB_BYTES ((32 * 64 + 2 * 32) * 4)
 #define ZS_TC_SMEM (ZS_TC_STAGES * ZS_TC_STAGE_BYTES + 2 * ZS_TC_TAB_BYTES + 1024 + 256)
 
-static_assert(ZS_TC_STAGE_BYTES % 1024 == 0, "stages stay 1024-byte aligned (128-byte swizzle atoms)");
+static_assert(ZS_TC_STAGE_BYTES % 1024 == 0 && ZS_TC_WIDE_STAGE_BYTES % 1024 == 0,
+              "stages stay 1024-byte aligned (128-byte swizzle atoms)");
+static_assert(2 * ZS_TC_WIDE_STAGE_BYTES <= ZS_TC_STAGES * ZS_TC_STAGE_BYTES, "both rings fit the stage region");
 
 namespace {
 
@@ -136,6 +141,11 @@ __global__ void __launch_bounds__(ZS_TC_THREADS, 1)
     const int tiles_x = (a.width + a.tc_tw - 1) / a.tc_tw;
     const int tiles = tiles_x * ((a.height + ZS_TC_M - 1) / ZS_TC_M);
     const int atoms = a.tc_atoms;
+    const bool wide = atoms > 4;
+    const uint32_t NS = wide ? 2u : (uint32_t)ZS_TC_STAGES;                  // ring slots
+    const uint32_t SB = wide ? ZS_TC_WIDE_STAGE_BYTES : ZS_TC_STAGE_BYTES;   // bytes per slot
+    const uint32_t nbuf = wide ? 1u : 2u;                                     // accumulators
+    const uint32_t accw = ZS_TC_TMEM_COLS / nbuf;                            // columns each
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < ZS_TC_STAGES; ++s) {
@@ -173,13 +183,13 @@ __global__ void __launch_bounds__(ZS_TC_THREADS, 1)
             const int rbase = a.vfirst[tt.band * ZS_TC_M];
             bool ok = true;
             for (int kc = 0; kc < nk; ++kc, ++it) {
-                const int s = (int)(it % ZS_TC_STAGES);
-                if (!tc_wait(zs_smem_addr(empty + s), ((it / ZS_TC_STAGES) & 1u) ^ 1u, abort_flag)) {
+                const int s = (int)(it % NS);
+                if (!tc_wait(zs_smem_addr(empty + s), ((it / NS) & 1u) ^ 1u, abort_flag)) {
                     ok = false;
                     break;
                 }
                 const uint32_t bar = zs_smem_addr(full + s);
-                const uint32_t st = zs_smem_addr(smem + (size_t)s * ZS_TC_STAGE_BYTES);
+                const uint32_t st = zs_smem_addr(smem + (size_t)s * SB);
                 zs_mbar_expect_tx(bar, tx);
                 zs_bulk_g2s(st, a.vimg + (size_t)(first + kc) * ZS_TC_CHUNK_BYTES, ZS_TC_CHUNK_BYTES, bar);
                 for (int at = 0; at < atoms; ++at)
@@ -190,20 +200,19 @@ __global__ void __launch_bounds__(ZS_TC_THREADS, 1)
         }
         if (*abort_flag) {
             // Let this thread's copies land before the CTA (and its shared memory) goes.
-            const uint32_t lo = it > ZS_TC_STAGES ? it - ZS_TC_STAGES : 0;
-            for (uint32_t j = lo; j < it; ++j)
-                zs_mbar_wait(zs_smem_addr(full + (j % ZS_TC_STAGES)), (j / ZS_TC_STAGES) & 1u);
+            const uint32_t lo = it > NS ? it - NS : 0;
+            for (uint32_t j = lo; j < it; ++j) zs_mbar_wait(zs_smem_addr(full + (j % NS)), (j / NS) & 1u);
         }
     } else if (warp == 1 && lane == 0) {
         // ---------------------------------------------------------------- MMAs
         uint32_t it = 0, lt = 0, tabs = 0;
-        const uint32_t idesc = tc_idesc(64 * atoms);
+        const uint32_t idesc0 = tc_idesc(64 * (wide ? 4 : atoms)), idesc1 = tc_idesc(64 * (wide ? atoms - 4 : 4));
         const uint32_t wbytes = (uint32_t)(a.tc_tw * a.taps * 4), ibytes = (uint32_t)(a.tc_tw * 4);
         for (int t = blockIdx.x; t < tiles && !*abort_flag; t += gridDim.x, ++lt) {
             const TcTile tt = tc_tile(a, t, tiles_x);
             const int nk = a.vimg_index[2 * tt.band + 1];
-            const uint32_t ab = lt & 1u;
-            if (!tc_wait(zs_smem_addr(tempty + ab), ((lt >> 1) & 1u) ^ 1u, abort_flag)) break;
+            const uint32_t ab = lt % nbuf;
+            if (!tc_wait(zs_smem_addr(tempty + ab), ((lt / nbuf) & 1u) ^ 1u, abort_flag)) break;
             tc_fence_after();
             {
                 // The tile's horizontal weights and tap windows, into the table buffer of its
@@ -216,24 +225,26 @@ __global__ void __launch_bounds__(ZS_TC_THREADS, 1)
                 zs_bulk_g2s(tb + wbytes + ibytes, a.index_y + tt.x0, ibytes, bar);
                 ++tabs;
             }
-            const uint32_t d = tmem + ab * ZS_TC_ACC_COLS;
+            const uint32_t d = tmem + ab * accw;
             bool ok = true;
             for (int kc = 0; kc < nk; ++kc, ++it) {
-                const int s = (int)(it % ZS_TC_STAGES);
-                if (!tc_wait(zs_smem_addr(full + s), (it / ZS_TC_STAGES) & 1u, abort_flag)) {
+                const int s = (int)(it % NS);
+                if (!tc_wait(zs_smem_addr(full + s), (it / NS) & 1u, abort_flag)) {
                     ok = false;
                     break;
                 }
                 tc_fence_after();
-                const uint32_t sa = zs_smem_addr(smem + (size_t)s * ZS_TC_STAGE_BYTES);
+                const uint32_t sa = zs_smem_addr(smem + (size_t)s * SB);
                 const uint32_t sb = sa + ZS_TC_CHUNK_BYTES;
 #pragma unroll
                 for (int ks = 0; ks < ZS_TC_K / 16; ++ks) {
                     // A: K-major, 16 K-elements = 32 bytes further along each swizzled row.
                     // B: MN-major, 16 K-rows = two 1024-byte groups of 8 rows further.
                     const uint64_t ad = tc_desc(sa + 32 * ks, 16, 1024);
-                    const uint64_t bd = tc_desc(sb + 2048 * ks, ZS_TC_ATOM_BYTES, 1024);
-                    tc_mma(d, ad, bd, idesc, (kc | ks) != 0);
+                    tc_mma(d, ad, tc_desc(sb + 2048 * ks, ZS_TC_ATOM_BYTES, 1024), idesc0, (kc | ks) != 0);
+                    if (wide)   // atoms 4.. into accumulator columns 256..
+                        tc_mma(d + 256, ad, tc_desc(sb + 4 * ZS_TC_ATOM_BYTES + 2048 * ks, ZS_TC_ATOM_BYTES, 1024), idesc1,
+                               (kc | ks) != 0);
                 }
                 tc_commit(zs_smem_addr(empty + s));
             }
@@ -244,8 +255,8 @@ __global__ void __launch_bounds__(ZS_TC_THREADS, 1)
         tc_commit(zs_smem_addr(drain));
         zs_mbar_wait(zs_smem_addr(drain), 0);
         if (*abort_flag)
-            for (uint32_t j = tabs > 2 ? tabs - 2 : 0; j < tabs; ++j)
-                zs_mbar_wait(zs_smem_addr(tabfull + (j & 1u)), (j >> 1) & 1u);
+            for (uint32_t j = tabs > nbuf ? tabs - nbuf : 0; j < tabs; ++j)
+                zs_mbar_wait(zs_smem_addr(tabfull + (j % nbuf)), (j / nbuf) & 1u);
     } else if (warp >= 2) {
         // ---------------------------------------------------------------- epilogue
         const int e = warp - 2;
@@ -255,15 +266,15 @@ __global__ void __launch_bounds__(ZS_TC_THREADS, 1)
         uint32_t lt = 0;
         for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++lt) {
             const TcTile tt = tc_tile(a, t, tiles_x);
-            const uint32_t ab = lt & 1u;
-            if (!tc_wait(zs_smem_addr(tabfull + ab), (lt >> 1) & 1u, abort_flag)) break;
-            if (!tc_wait(zs_smem_addr(tfull + ab), (lt >> 1) & 1u, abort_flag)) break;
+            const uint32_t ab = lt % nbuf;
+            if (!tc_wait(zs_smem_addr(tabfull + ab), (lt / nbuf) & 1u, abort_flag)) break;
+            if (!tc_wait(zs_smem_addr(tfull + ab), (lt / nbuf) & 1u, abort_flag)) break;
             tc_fence_after();
             const float *tw_w = (const float *)(tab + ab * ZS_TC_TAB_BYTES);
             const int *tw_first = (const int *)(tw_w + a.tc_tw * a.taps);
             const int *tw_cnt = tw_first + a.tc_tw;
             const int oy = tt.band * ZS_TC_M + m;
-            const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16) + ab * ZS_TC_ACC_COLS;
+            const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16) + ab * accw;
             for (int ox = tt.x0 + part; ox < min(tt.x0 + a.tc_tw, a.width); ox += 4) {
                 const int oxl = ox - tt.x0;
                 const int cnt = tw_cnt[oxl];

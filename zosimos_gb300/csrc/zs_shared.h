@@ -148,10 +148,11 @@ struct ZsRasterArgs {
 #define ZS_RS_STAGE_BUDGET (96 * 1024)   // staged source rows of one CTA (2 CTAs per SM)
 
 // Tensor-core resample: bands of 128 output rows (the MMA's M), chunks of 64 source rows
-// (the K of one 128-byte swizzle atom), at most 4 atoms of 64 source elements (N <= 256).
+// (the K of one 128-byte swizzle atom), at most 8 atoms of 64 source elements (two MMAs of
+// N <= 256 into 512 TMEM columns).
 #define ZS_TC_M 128
 #define ZS_TC_K 64
-#define ZS_TC_MAX_ATOMS 4
+#define ZS_TC_MAX_ATOMS 8
 #define ZS_TC_CHUNK_BYTES (ZS_TC_M * ZS_TC_K * 2)
 
 // Bits of the device status word.
