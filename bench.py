@@ -443,7 +443,7 @@ def workload_layers(args, stream, sh):
     from zosimos_gb300.synthetic import layer_transforms, premultiplied_layer
     from zosimos_gb300.workloads import layer_stack
     timed = _timer(stream)
-    n, w = 32, 4096
+    n, w = (8, 4096) if args.profile else (32, 4096)
     distinct = 4      # four generated layers, bound cyclically to the 32 inputs
     layers = []
     for i in range(distinct):
@@ -456,6 +456,14 @@ def workload_layers(args, stream, sh):
             for m in (zs.Mode.Fused, zs.Mode.PerOpF32)]
     dst = zs.DeviceBuffer(w * w * 8)
     ins = [layers[i % distinct].ptr for i in range(n)]
+    if args.profile:
+        # A short, fixed sequence for ncu: one fused launch of an 8-layer stack (4 distinct
+        # 4096^2 RGBA16F layers bound cyclically, 512 MiB > L2).
+        import torch
+        exes[0].run_device(ins, [dst.ptr], sh)
+        torch.cuda.synchronize()
+        print("profile run done", flush=True)
+        return
     steps = max(3, args.steps // 40)
     ms = [timed(lambda i, e=e: e.run_device(ins, [dst.ptr], sh), steps, args.warmup) for e in exes]
     _line("layer stack 32 x 4096^2 premultiplied RGBA16F, affine + blend per layer", n * w * w,

@@ -164,8 +164,20 @@ struct Planner {
                 fail(ZS_ERR_UNIMPLEMENTED, "binary op after a layer stack");
             }
         }
+        // The specialised kernel: RGBA16F bilinear layers under affine (not projective)
+        // inverses, premultiplied operands, and only lossless FP32 quantisation.
+        bool fast = true;
+        for (int i = 0; i < L->nlayers; ++i) {
+            const ZsLayer &ly = L->layers[i];
+            const bool lossless_s = !ly.quant_sample || L->fmts[ly.quant_sample - 1].fast == ZS_FAST_F32X4;
+            const bool lossless_a = !ly.quant_acc || L->fmts[ly.quant_acc - 1].fast == ZS_FAST_F32X4;
+            fast = fast && ly.fmt.fast == ZS_FAST_F16X4 && ly.bilinear && !ly.straight && lossless_s && lossless_a &&
+                   ly.inv[6] == 0.f && ly.inv[7] == 0.f && ly.inv[8] == 1.f;
+        }
+        L->f16_bilinear = fast ? 1 : 0;
         st.layers = L;
-        st.label += " [fused layer stack, " + std::to_string(p.layers.size()) + " layers]";
+        st.label += " [fused layer stack, " + std::to_string(p.layers.size()) + " layers" +
+                    (fast ? ", RGBA16F bilinear kernel]" : "]");
         E.steps.push_back(st);
     }
 

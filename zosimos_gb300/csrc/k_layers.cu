@@ -40,11 +40,15 @@ __device__ __forceinline__ float4 zs_layer_sample(const ZsLayer &L, int x, int y
 }
 
 __global__ void __launch_bounds__(256) zs_layers_kernel(const __grid_constant__ ZsLayersArgs a) {
-    const int64_t n = (int64_t)a.width * a.height;
+    // 32 x 8 pixel tiles (8 x 4 per warp): each warp's samples of a layer fall into a
+    // compact footprint of that layer.
+    const int tiles_x = (a.width + 31) >> 5;
+    const int64_t n = (int64_t)tiles_x * ((a.height + 7) >> 3) * 256;
     const int64_t step = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += step) {
-        const int y = (int)(i / a.width);
-        const int x = (int)(i - (int64_t)y * a.width);
+        int x, y;
+        zs_tile_pixel(i, tiles_x, x, y);
+        if (x >= a.width || y >= a.height) continue;
         float4 acc = a.has_base ? zs_load_px(a.base, x, y)
                                 : make_float4(a.base_color[0], a.base_color[1], a.base_color[2], a.base_color[3]);
         for (int l = 0; l < a.nlayers; ++l) {
@@ -61,12 +65,93 @@ __global__ void __launch_bounds__(256) zs_layers_kernel(const __grid_constant__ 
     }
 }
 
+// The common stack: RGBA16F layers sampled bilinearly through affine inverses, premultiplied
+// operands, no lossy quantisation (FP32 quantisation is the identity).  Same arithmetic, in
+// the same order, as zs_layer_sample + zs_blend_px, without the per-tap format dispatch; each
+// thread takes two pixels four rows apart so that a layer's parameters are read once per
+// pair and two samples are in flight.  Tiles of 32 x 16 pixels, 8 x 8 per warp.
+__device__ __forceinline__ float4 zs_h4(uint2 v) {
+    const float2 lo = __half22float2(*reinterpret_cast<const __half2 *>(&v.x));
+    const float2 hi = __half22float2(*reinterpret_cast<const __half2 *>(&v.y));
+    return make_float4(lo.x, lo.y, hi.x, hi.y);
+}
+
+__global__ void __launch_bounds__(256) zs_layers_f16_kernel(const __grid_constant__ ZsLayersArgs a) {
+    const int tiles_x = (a.width + 31) >> 5;
+    const int64_t n = (int64_t)tiles_x * ((a.height + 15) >> 4) * 256;
+    const int64_t step = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += step) {
+        const int64_t tile = i >> 8;
+        const int t = (int)(i & 255), w = t >> 5, l = t & 31;
+        const int ty = (int)(tile / tiles_x), tx = (int)(tile - (int64_t)ty * tiles_x);
+        const int x = (tx << 5) + ((w & 3) << 3) + (l & 7);
+        const int y0 = (ty << 4) + ((w >> 2) << 3) + (l >> 3);
+        if (x >= a.width || y0 >= a.height) continue;
+        const bool two = y0 + 4 < a.height;
+        float4 acc[2];
+#pragma unroll
+        for (int p = 0; p < 2; ++p)
+            acc[p] = a.has_base ? zs_load_px(a.base, x, min(y0 + 4 * p, a.height - 1))
+                                : make_float4(a.base_color[0], a.base_color[1], a.base_color[2], a.base_color[3]);
+        const float cx = (float)x + 0.5f;
+        for (int li = 0; li < a.nlayers; ++li) {
+            const ZsLayer &L = a.layers[li];
+            const float i0 = L.inv[0], i1 = L.inv[1], i2 = L.inv[2], i3 = L.inv[3], i4 = L.inv[4], i5 = L.inv[5];
+            const float fw = (float)L.width, fh = (float)L.height;
+            const uint8_t *base = L.ptr;
+            const int64_t stride = L.stride;
+            float4 s[2];
+#pragma unroll
+            for (int p = 0; p < 2; ++p) {
+                const float cy = (float)(y0 + 4 * p) + 0.5f;
+                const float qx = fmaf(i0, cx, fmaf(i1, cy, i2));
+                const float qy = fmaf(i3, cx, fmaf(i4, cy, i5));
+                if (qx >= 0.0f && qx < fw && qy >= 0.0f && qy < fh) {
+                    const float txf = qx - 0.5f, tyf = qy - 0.5f;
+                    const float fx0 = floorf(txf), fy0 = floorf(tyf);
+                    const float fx = txf - fx0, fy = tyf - fy0;
+                    const int x0 = (int)fx0, y0i = (int)fy0;
+                    const int xa = zs_clampi(x0, 0, L.width - 1), xb = zs_clampi(x0 + 1, 0, L.width - 1);
+                    const int ya = zs_clampi(y0i, 0, L.height - 1), yb = zs_clampi(y0i + 1, 0, L.height - 1);
+                    const uint8_t *ra = base + (int64_t)ya * stride, *rb = base + (int64_t)yb * stride;
+                    const float4 t00 = zs_h4(__ldg((const uint2 *)(ra + (int64_t)xa * 8)));
+                    const float4 t01 = zs_h4(__ldg((const uint2 *)(ra + (int64_t)xb * 8)));
+                    const float4 t10 = zs_h4(__ldg((const uint2 *)(rb + (int64_t)xa * 8)));
+                    const float4 t11 = zs_h4(__ldg((const uint2 *)(rb + (int64_t)xb * 8)));
+                    s[p] = zs_lerp4(zs_lerp4(t00, t01, fx), zs_lerp4(t10, t11, fx), fy);
+                } else {
+                    s[p] = make_float4(L.canvas[0], L.canvas[1], L.canvas[2], L.canvas[3]);
+                }
+            }
+            const uint32_t mode = L.mode;
+            zs_blend_px(acc[0], s[0], mode, 0);
+            zs_blend_px(acc[1], s[1], mode, 0);
+        }
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+            if (p == 1 && !two) break;
+            const int y = y0 + 4 * p;
+            float4 r = acc[p], r2 = make_float4(0.f, 0.f, 0.f, 0.f);
+            zs_run_program(a.prog, a.fmts, r, r2);
+            uint8_t *dp = a.dst + (int64_t)y * a.dst_stride + (int64_t)x * a.dst_fmt.bpp;
+            zs_store_raw(dp, a.dst_fmt.bpp, zs_encode_raw(a.dst_fmt, r));
+        }
+    }
+}
+
 namespace zs {
 
 cudaError_t launch_layers(const ZsLayersArgs &args, int sm_count, cudaStream_t stream) {
-    const int64_t n = (int64_t)args.width * args.height;
-    if (n <= 0) return cudaSuccess;
-    int64_t blocks = (n + 255) / 256;
+    if (args.width <= 0 || args.height <= 0) return cudaSuccess;
+    if (args.f16_bilinear) {
+        int64_t blocks = (int64_t)((args.width + 31) / 32) * ((args.height + 15) / 16);
+        const int64_t cap = (int64_t)(sm_count > 0 ? sm_count : 148) * 8;
+        if (blocks > cap) blocks = cap;
+        zs_layers_f16_kernel<<<(unsigned)blocks, 256, 0, stream>>>(args);
+        g_kernel_launches.fetch_add(1);
+        return cudaGetLastError();
+    }
+    int64_t blocks = (int64_t)((args.width + 31) / 32) * ((args.height + 7) / 8);
     const int64_t cap = (int64_t)(sm_count > 0 ? sm_count : 148) * 8;
     if (blocks > cap) blocks = cap;
     zs_layers_kernel<<<(unsigned)blocks, 256, 0, stream>>>(args);

@@ -42,6 +42,16 @@ __device__ __forceinline__ void zs_affine_map(const float *inv, int x, int y, fl
     qy = Y;
 }
 
+// Pixel of work item i in 32 x 8 tiles of 256 items: warp w of the tile covers columns
+// 8 (w % 4) .. +8 and rows 4 (w / 4) .. +4, lane l column l % 8 and row l / 8.
+__device__ __forceinline__ void zs_tile_pixel(int64_t i, int tiles_x, int &x, int &y) {
+    const int64_t tile = i >> 8;
+    const int t = (int)(i & 255), w = t >> 5, l = t & 31;
+    const int ty = (int)(tile / tiles_x), tx = (int)(tile - (int64_t)ty * tiles_x);
+    x = (tx << 5) + ((w & 3) << 3) + (l & 7);
+    y = (ty << 3) + ((w >> 2) << 2) + (l >> 3);
+}
+
 __device__ __forceinline__ int zs_clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
 __device__ __forceinline__ float4 zs_lerp4(float4 a, float4 b, float t) {
@@ -50,11 +60,21 @@ __device__ __forceinline__ float4 zs_lerp4(float4 a, float4 b, float t) {
 }
 
 __global__ void __launch_bounds__(256) zs_raster_kernel(const __grid_constant__ ZsRasterArgs a) {
-    const int64_t n = (int64_t)a.width * a.height;
+    // Affine gathers walk 32 x 8 pixel tiles (8 x 4 per warp) so that a warp's samples
+    // fall into a compact source footprint; everything else walks rows.
+    const bool tiled = a.producer == ZS_PR_AFFINE;
+    const int tiles_x = (a.width + 31) >> 5;
+    const int64_t n = tiled ? (int64_t)tiles_x * ((a.height + 7) >> 3) * 256 : (int64_t)a.width * a.height;
     const int64_t step = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += step) {
-        const int y = (int)(i / a.width);
-        const int x = (int)(i - (int64_t)y * a.width);
+        int x, y;
+        if (tiled) {
+            zs_tile_pixel(i, tiles_x, x, y);
+            if (x >= a.width || y >= a.height) continue;
+        } else {
+            y = (int)(i / a.width);
+            x = (int)(i - (int64_t)y * a.width);
+        }
         float4 r = make_float4(0.f, 0.f, 0.f, 0.f), r2 = r;
         uint4 raw = make_uint4(0, 0, 0, 0);
         bool is_raw = false;

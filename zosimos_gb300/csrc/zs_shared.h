@@ -183,6 +183,9 @@ struct ZsLayersArgs {
     int32_t nlayers;
     int32_t width, height;
     int32_t has_base;      // 1: base buffer in `base`, 0: constant base_color
+    int32_t f16_bilinear;  // 1: every layer RGBA16F, bilinear, affine, premultiplied, no lossy
+                           // quantisation (the specialised kernel applies)
+    int32_t pad;
     ZsSource base;
     float base_color[4];
     ZsLayer layers[ZS_MAX_LAYERS];
