@@ -70,12 +70,6 @@ __global__ void __launch_bounds__(256) zs_layers_kernel(const __grid_constant__ 
 // the same order, as zs_layer_sample + zs_blend_px, without the per-tap format dispatch; each
 // thread takes two pixels four rows apart so that a layer's parameters are read once per
 // pair and two samples are in flight.  Tiles of 32 x 16 pixels, 8 x 8 per warp.
-__device__ __forceinline__ float4 zs_h4(uint2 v) {
-    const float2 lo = __half22float2(*reinterpret_cast<const __half2 *>(&v.x));
-    const float2 hi = __half22float2(*reinterpret_cast<const __half2 *>(&v.y));
-    return make_float4(lo.x, lo.y, hi.x, hi.y);
-}
-
 __global__ void __launch_bounds__(256) zs_layers_f16_kernel(const __grid_constant__ ZsLayersArgs a) {
     const int tiles_x = (a.width + 31) >> 5;
     const int64_t n = (int64_t)tiles_x * ((a.height + 15) >> 4) * 256;

@@ -345,6 +345,13 @@ __device__ inline uint4 zs_encode_raw(const ZsFormat &f, float4 c) {
     return r;
 }
 
+// One RGBA16F texel (8 bytes) as FP32.
+__device__ __forceinline__ float4 zs_h4(uint2 v) {
+    const float2 lo = __half22float2(*reinterpret_cast<const __half2 *>(&v.x));
+    const float2 hi = __half22float2(*reinterpret_cast<const __half2 *>(&v.y));
+    return make_float4(lo.x, lo.y, hi.x, hi.y);
+}
+
 __device__ __forceinline__ float4 zs_load_px(const ZsSource &s, int x, int y) {
     const uint8_t *p = s.ptr + (int64_t)y * s.stride + (int64_t)x * s.fmt.bpp;
     return zs_decode_raw(s.fmt, zs_load_raw(p, s.fmt.bpp));
