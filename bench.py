@@ -417,6 +417,8 @@ def workload_thumbnails(args, stream, sh):
     from zosimos_gb300.workloads import color_chain, rgba_bytes
     timed = _timer(stream)
     ws, hs = thumbnail_sizes(1024, seed=4)
+    if args.profile:
+        ws, hs = ws[:256], hs[:256]     # a short, fixed sequence for ncu: one batch of 256 images
     # Sources: top-left crops of one seeded 4096^2 image, each in its own tight buffer.
     atlas = rgba_bytes(srgb_gradient_noise(4096, 4096, seed=4))
     bufs = []
@@ -429,6 +431,12 @@ def workload_thumbnails(args, stream, sh):
     out = zs.DeviceBuffer(1024 * 256 * 256 * 4)
     ptrs, wl, hl = [b.ptr for b in bufs], [int(w) for w in ws], [int(h) for h in hs]
     run = lambda i: exe.batch_thumbnails(ptrs, wl, hl, 256, out.ptr, sh)
+    if args.profile:
+        import torch
+        run(0)
+        torch.cuda.synchronize()
+        print("profile run done", flush=True)
+        return
     ms = timed(run, max(3, args.steps // 20), args.warmup)
     src_px = int(sum(int(w) * int(h) for w, h in zip(ws, hs)))
     _line("thumbnails 1024 uneven RGBA8 -> colour chain -> box fit 256 -> centred 256^2", src_px,

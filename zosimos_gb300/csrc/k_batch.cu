@@ -5,19 +5,20 @@
 // Per image: decode -> the fused colour chain of a lowered Program (canonical form
 // M_a, [cbrt], M_b, [cube], M_c, [clamp], M_d, linear result) -> box (area coverage)
 // fit-resize so the long side is `canvas` -> centred inscribe on a transparent
-// canvas x canvas image -> exact sRGB8 encode.  The canvas of image i is cut into
-// work items of ZS_BATCH_ROWS rows; CTAs pull items with one atomicAdd each (no
-// spinning, no inter-CTA waits), so the uneven cost of the images balances itself.
-// Each thread computes output pixels directly from their source window: the box
-// weights are separable and every source pixel in the window is decoded and pushed
-// through the chain in FP32 registers.
+// canvas x canvas image -> exact sRGB8 encode.  The canvases are zero-filled (the
+// transparent margins) by one memset; the fitted pixels are cut into work items of 32
+// adjacent pixels of one row, one item per warp, so the 32 lanes have windows of the
+// same size.  Warps take items by static striding over all images (a prefix table and a
+// binary search find the image of an item), which spreads every image's cost over all
+// warps without atomics or barriers.  Each lane computes its output pixel from its source
+// window: the box weights are separable, the source texels of a window row go through
+// the colour chain two at a time in FP32x2 registers.
 #include <vector>
 
 #include "host/zs_host.hpp"
 #include "zs_device.cuh"
 #include "zs_kernels.h"
 
-#define ZS_BATCH_ROWS 4
 #define ZS_BATCH_THREADS 256
 
 struct ZsBatchImage {
@@ -31,13 +32,14 @@ struct ZsBatchImage {
 
 struct ZsBatchArgs {
     const ZsBatchImage *images;
-    uint32_t *counter;         // work-queue head, zeroed before the launch
+    const int32_t *prefix;     // [n + 1]: first work item of each image, total at [n]
     uint8_t *out;
     int32_t n;
     int32_t canvas;
-    int32_t items_per_image;
     int32_t flags;
+    int32_t pad;
     float m[4][9];
+    float m2[4][9][2];         // the same matrices with every coefficient duplicated (f32x2 operands)
 };
 
 __device__ __forceinline__ void zs_batch_m3(const float *m, float &r, float &g, float &b) {
@@ -61,6 +63,35 @@ __device__ __forceinline__ float4 zs_batch_chain(uint32_t w, const ZsBatchArgs &
     return make_float4(r, g, b, (float)(w >> 24) / 255.0f);
 }
 
+// The same chain on two texels at once: FP32x2 matrix products, MUFU cube roots.
+__device__ __forceinline__ void zs_batch_chain2(uint32_t w0, uint32_t w1, const ZsBatchArgs &a, float2 &r, float2 &g,
+                                                float2 &b) {
+    r = make_float2(zs_srgb_decode_lut[w0 & 255u], zs_srgb_decode_lut[w1 & 255u]);
+    g = make_float2(zs_srgb_decode_lut[(w0 >> 8) & 255u], zs_srgb_decode_lut[(w1 >> 8) & 255u]);
+    b = make_float2(zs_srgb_decode_lut[(w0 >> 16) & 255u], zs_srgb_decode_lut[(w1 >> 16) & 255u]);
+    zs_m3x2<false>(a.m2[0], r, g, b);
+    if (a.flags & ZS_CHAIN_CBRT) {
+        if (a.flags & ZS_CHAIN_CBRT_NONNEG) {
+            zs_cbrt2(r);
+            zs_cbrt2(g);
+            zs_cbrt2(b);
+        } else {
+            r = make_float2(zs_cbrt1<false>(r.x), zs_cbrt1<false>(r.y));
+            g = make_float2(zs_cbrt1<false>(g.x), zs_cbrt1<false>(g.y));
+            b = make_float2(zs_cbrt1<false>(b.x), zs_cbrt1<false>(b.y));
+        }
+    }
+    zs_m3x2<false>(a.m2[1], r, g, b);
+    if (a.flags & ZS_CHAIN_CUBE) {
+        r = __fmul2_rn(__fmul2_rn(r, r), r);
+        g = __fmul2_rn(__fmul2_rn(g, g), g);
+        b = __fmul2_rn(__fmul2_rn(b, b), b);
+    }
+    if (a.flags & ZS_CHAIN_CLAMP) zs_m3x2<true>(a.m2[2], r, g, b);
+    else zs_m3x2<false>(a.m2[2], r, g, b);
+    zs_m3x2<false>(a.m2[3], r, g, b);
+}
+
 // Box (area coverage) window of output index u along one axis.
 __device__ __forceinline__ void zs_box_window(int u, float s, float f, int len, int &j0, int &j1, float &lo, float &hi) {
     const float c = ((float)u + 0.5f) * s;
@@ -71,54 +102,60 @@ __device__ __forceinline__ void zs_box_window(int u, float s, float f, int len, 
 }
 
 __global__ void __launch_bounds__(ZS_BATCH_THREADS) zs_batch_kernel(const __grid_constant__ ZsBatchArgs a) {
-    __shared__ uint32_t item;
-    const int total = a.n * a.items_per_image;
-    const int cpx = a.canvas * ZS_BATCH_ROWS;
-    for (;;) {
-        if (threadIdx.x == 0) item = atomicAdd(a.counter, 1u);
-        __syncthreads();
-        const int it = (int)item;
-        __syncthreads();
-        if (it >= total) break;
-        const int img = it / a.items_per_image;
-        const int band = it - img * a.items_per_image;
-        const ZsBatchImage I = a.images[img];
-        uint32_t *out = reinterpret_cast<uint32_t *>(a.out + (size_t)img * a.canvas * a.canvas * 4);
-        for (int p = threadIdx.x; p < cpx; p += blockDim.x) {
-            const int oy = band * ZS_BATCH_ROWS + p / a.canvas;
-            const int ox = p % a.canvas;
-            if (oy >= a.canvas) continue;
-            const int u = ox - I.x0, v = oy - I.y0;
-            uint32_t code = 0;   // transparent canvas
-            if (u >= 0 && v >= 0 && u < I.tw && v < I.th) {
-                int jx0, jx1, jy0, jy1;
-                float lox, hix, loy, hiy;
-                zs_box_window(u, I.sx, I.fx, I.width, jx0, jx1, lox, hix);
-                zs_box_window(v, I.sy, I.fy, I.height, jy0, jy1, loy, hiy);
-                float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-                float wsum = 0.f;
-                for (int jy = jy0; jy < jy1; ++jy) {
-                    const float wy = fminf(hiy, (float)jy + 1.f) - fmaxf(loy, (float)jy);
-                    if (wy <= 0.f) continue;
-                    const uint32_t *row = reinterpret_cast<const uint32_t *>(I.ptr + (size_t)jy * I.width * 4);
-                    for (int jx = jx0; jx < jx1; ++jx) {
-                        const float wx = fminf(hix, (float)jx + 1.f) - fmaxf(lox, (float)jx);
-                        if (wx <= 0.f) continue;
-                        const float wgt = wx * wy;
-                        const float4 c = zs_batch_chain(__ldg(row + jx), a);
-                        acc.x = fmaf(wgt, c.x, acc.x);
-                        acc.y = fmaf(wgt, c.y, acc.y);
-                        acc.z = fmaf(wgt, c.z, acc.z);
-                        acc.w = fmaf(wgt, c.w, acc.w);
-                        wsum += wgt;
-                    }
-                }
-                const float inv = wsum > 0.f ? 1.0f / wsum : 0.f;
-                code = zs_enc_srgb8(zs_srgb_encode_tab, acc.x * inv) | (zs_enc_srgb8(zs_srgb_encode_tab, acc.y * inv) << 8) |
-                       (zs_enc_srgb8(zs_srgb_encode_tab, acc.z * inv) << 16) | (zs_unorm8(acc.w * inv) << 24);
-            }
-            out[(size_t)oy * a.canvas + ox] = code;
+    const int lane = threadIdx.x & 31;
+    const int warps = (int)(gridDim.x * (blockDim.x >> 5));
+    const int total = a.prefix[a.n];
+    for (int it = (int)(blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)); it < total; it += warps) {
+        int lo = 0, hi = a.n - 1;           // last image whose first item is <= it
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (a.prefix[mid] <= it) lo = mid;
+            else hi = mid - 1;
         }
+        const ZsBatchImage I = a.images[lo];
+        const int segs = (I.tw + 31) >> 5, local = it - a.prefix[lo];
+        const int v = local / segs, u = (local - v * segs) * 32 + lane;
+        if (u >= I.tw) continue;
+        uint32_t *out = reinterpret_cast<uint32_t *>(a.out + (size_t)lo * a.canvas * a.canvas * 4);
+        int jx0, jx1, jy0, jy1;
+        float lox, hix, loy, hiy;
+        zs_box_window(u, I.sx, I.fx, I.width, jx0, jx1, lox, hix);
+        zs_box_window(v, I.sy, I.fy, I.height, jy0, jy1, loy, hiy);
+        // Weight sums once per output; per row, source texels go through the
+        // chain two at a time (the odd tail pairs with itself at weight 0).
+        float wsx = 0.f, wsy = 0.f;
+        for (int jx = jx0; jx < jx1; ++jx) wsx += fmaxf(fminf(hix, (float)jx + 1.f) - fmaxf(lox, (float)jx), 0.f);
+        for (int jy = jy0; jy < jy1; ++jy) wsy += fmaxf(fminf(hiy, (float)jy + 1.f) - fmaxf(loy, (float)jy), 0.f);
+        const float wsum = wsx * wsy;
+        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int jy = jy0; jy < jy1; ++jy) {
+            const float wy = fminf(hiy, (float)jy + 1.f) - fmaxf(loy, (float)jy);
+            if (wy <= 0.f) continue;
+            const uint32_t *row = reinterpret_cast<const uint32_t *>(I.ptr + (size_t)jy * I.width * 4);
+            float2 sr = make_float2(0.f, 0.f), sg = sr, sb = sr, sa = sr;
+            for (int jx = jx0; jx < jx1; jx += 2) {
+                const bool two = jx + 1 < jx1;
+                const uint32_t w0 = __ldg(row + jx), w1 = two ? __ldg(row + jx + 1) : w0;
+                const float2 wx = make_float2(
+                    fmaxf(fminf(hix, (float)jx + 1.f) - fmaxf(lox, (float)jx), 0.f),
+                    two ? fmaxf(fminf(hix, (float)jx + 2.f) - fmaxf(lox, (float)jx + 1.f), 0.f) : 0.f);
+                float2 r, g, b;
+                zs_batch_chain2(w0, w1, a, r, g, b);
+                const float2 al = make_float2((float)(w0 >> 24) * (1.0f / 255.0f), (float)(w1 >> 24) * (1.0f / 255.0f));
+                sr = __ffma2_rn(wx, r, sr);
+                sg = __ffma2_rn(wx, g, sg);
+                sb = __ffma2_rn(wx, b, sb);
+                sa = __ffma2_rn(wx, al, sa);
+            }
+            acc.x = fmaf(wy, sr.x + sr.y, acc.x);
+            acc.y = fmaf(wy, sg.x + sg.y, acc.y);
+            acc.z = fmaf(wy, sb.x + sb.y, acc.z);
+            acc.w = fmaf(wy, sa.x + sa.y, acc.w);
+        }
+        const float inv = wsum > 0.f ? 1.0f / wsum : 0.f;
+        const uint32_t code = zs_enc_srgb8(zs_srgb_encode_tab, acc.x * inv) | (zs_enc_srgb8(zs_srgb_encode_tab, acc.y * inv) << 8) |
+                              (zs_enc_srgb8(zs_srgb_encode_tab, acc.z * inv) << 16) | (zs_unorm8(acc.w * inv) << 24);
+        out[(size_t)(I.y0 + v) * a.canvas + I.x0 + u] = code;
     }
 }
 
@@ -163,8 +200,19 @@ int batch_thumbnails(Executable *chain, const void *const *images, const uint32_
         I.fx = I.sx > 1.f ? I.sx : 1.f;
         I.fy = I.sy > 1.f ? I.sy : 1.f;
     }
-    // Scratch: image table + work-queue counter, kept with the executable.
-    const size_t bytes = sizeof(ZsBatchImage) * n + 256;
+    // Work items: 32 adjacent fitted pixels of one row.
+    std::vector<int32_t> prefix(n + 1, 0);
+    for (uint32_t i = 0; i < n; ++i) {
+        const int64_t items = (int64_t)host[i].th * ((host[i].tw + 31) / 32);
+        if ((int64_t)prefix[i] + items > INT32_MAX) {
+            set_last_error("zs_batch_thumbnails: too many output pixels in one batch");
+            return ZS_ERR_INVALID_ARG;
+        }
+        prefix[i + 1] = prefix[i] + (int32_t)items;
+    }
+    // Scratch: image table + item prefix table, kept with the executable.
+    const size_t table_bytes = (sizeof(ZsBatchImage) * n + 255) & ~(size_t)255;
+    const size_t bytes = table_bytes + sizeof(int32_t) * (n + 1);
     if (chain->batch_bytes < bytes) {
         if (chain->batch_scratch) cudaFree(chain->batch_scratch);
         chain->batch_scratch = nullptr;
@@ -177,10 +225,13 @@ int batch_thumbnails(Executable *chain, const void *const *images, const uint32_
         chain->batch_bytes = bytes;
     }
     uint8_t *scratch = (uint8_t *)chain->batch_scratch;
-    uint32_t *counter = (uint32_t *)scratch;
-    ZsBatchImage *table = (ZsBatchImage *)(scratch + 256);
+    ZsBatchImage *table = (ZsBatchImage *)scratch;
+    int32_t *dprefix = (int32_t *)(scratch + table_bytes);
     cudaError_t e = cudaMemcpyAsync(table, host.data(), sizeof(ZsBatchImage) * n, cudaMemcpyHostToDevice, stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(dprefix, prefix.data(), sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice, stream);
+    // Transparent margins: zero every canvas, the kernel writes the fitted pixels.
+    if (e == cudaSuccess) e = cudaMemsetAsync(out, 0, (size_t)n * canvas * canvas * 4, stream);
     if (e != cudaSuccess) {
         set_last_error(std::string("zs_batch_thumbnails: ") + cudaGetErrorString(e));
         return ZS_ERR_DEVICE;
@@ -188,19 +239,20 @@ int batch_thumbnails(Executable *chain, const void *const *images, const uint32_
     ZsBatchArgs a;
     std::memset(&a, 0, sizeof(a));
     a.images = table;
-    a.counter = counter;
+    a.prefix = dprefix;
     a.out = (uint8_t *)out;
     a.n = (int)n;
     a.canvas = (int)canvas;
-    a.items_per_image = ((int)canvas + ZS_BATCH_ROWS - 1) / ZS_BATCH_ROWS;
     a.flags = cs->chain.flags;
     std::memcpy(a.m, cs->chain.m, sizeof(a.m));
+    std::memcpy(a.m2, cs->chain.m2, sizeof(a.m2));
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, zs_batch_kernel, ZS_BATCH_THREADS, 0);
     if (per_sm < 1) per_sm = 1;
     long long blocks = (long long)chain->sm_count * per_sm;
-    const long long items = (long long)n * a.items_per_image;
-    if (blocks > items) blocks = items;
+    const long long need = ((long long)prefix[n] + ZS_BATCH_THREADS / 32 - 1) / (ZS_BATCH_THREADS / 32);
+    if (blocks > need) blocks = need;
+    if (blocks < 1) return ZS_OK;
     zs_batch_kernel<<<(unsigned)blocks, ZS_BATCH_THREADS, 0, stream>>>(a);
     g_kernel_launches.fetch_add(1);
     e = cudaGetLastError();
