@@ -73,6 +73,25 @@ def test_chain_run_host_and_device_agree():
     assert maxdiff(out_h, P.oracle_chain(img)) <= LSB
 
 
+def test_chain_run_host_striped():
+    # 2048 x 2050 RGBA8 (16.4 MiB): run_host splits the pixel-local chain into row stripes on
+    # three streams; the result must equal the one-launch device path byte for byte.
+    w, h = 2048, 2050
+    img = srgb_gradient_noise(w, h, seed=6)
+    c, _, _ = P.chain_commands(w, h)
+    exe = zs.Linker.from_included().compile(c).lower_to()
+    out_h = np.empty((h, w * 4), np.uint8)
+    exe.run_host([P.rgba_bytes(img)], [out_h])
+    src = zs.DeviceBuffer(img.nbytes)
+    dst = zs.DeviceBuffer(img.nbytes)
+    src.upload(P.rgba_bytes(img))
+    exe.run_device([src.ptr], [dst.ptr])
+    zs.device_synchronize()
+    out_d = dst.download(np.empty_like(out_h))
+    assert (out_h == out_d).all()
+    assert maxdiff(out_h[:64], P.oracle_chain(img[:64])) <= LSB
+
+
 def test_composed(background, foreground, goldens):
     ours = P.ours_composed(background, foreground)
     assert (ours == P.oracle_composed(background, foreground)).all()

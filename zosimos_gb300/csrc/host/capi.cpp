@@ -33,12 +33,19 @@ using namespace zs;
 struct zs_pool { Pool p; };
 struct zs_cmd { Command c; };
 struct zs_program { Program p; };
-struct zs_executable { std::unique_ptr<Executable> e; cudaStream_t stream = nullptr; ~zs_executable(); };
+struct zs_executable {
+    std::unique_ptr<Executable> e;
+    cudaStream_t stream = nullptr;
+    cudaStream_t stripes[3] = {nullptr, nullptr, nullptr};   // striped host round trips
+    ~zs_executable();
+};
 struct zs_environment { Environment env; };
 struct zs_execution { Execution x; std::vector<int> kinds; std::vector<int> args; };
 
 zs_executable::~zs_executable() {
     if (stream) cudaStreamDestroy(stream);
+    for (cudaStream_t t : stripes)
+        if (t) cudaStreamDestroy(t);
 }
 
 static void note_graph_launch(const Executable &E) {
@@ -550,6 +557,42 @@ static cudaStream_t exe_stream(zs_executable *exe) {
     return exe->stream;
 }
 
+// A lone fused colour chain is pixel local: its host round trip runs in row stripes on
+// three rotating streams, so that the upload of one stripe, the kernel of the previous and
+// the download of the one before overlap (both copy directions at once).
+static bool run_host_striped(zs_executable *exe, const void *const *inputs, void *const *outputs) {
+    Executable &E = *exe->e;
+    if (E.steps.size() != 1 || E.steps[0].kind != StepKind::Chain || E.input_slot.size() != 1 ||
+        E.output_slot.size() != 1)
+        return false;
+    const Step &st = E.steps[0];
+    if (st.src_slot[0] != E.input_slot[0] || st.dst_slot != E.output_slot[0]) return false;
+    const int64_t npx = st.chain.npx;
+    const int64_t bytes = npx * 4;
+    if (bytes < (int64_t)(16 << 20)) return false;               // small images: one round trip
+    const int kStripes = 8;
+    const int64_t per = ((npx + kStripes - 1) / kStripes + 1023) & ~(int64_t)1023;   // 4 KiB multiples
+    for (cudaStream_t &t : exe->stripes)
+        if (!t) check_cuda(cudaStreamCreateWithFlags(&t, cudaStreamNonBlocking), "stream");
+    uint8_t *din = (uint8_t *)E.dev_buffers[st.src_slot[0]], *dout = (uint8_t *)E.dev_buffers[st.dst_slot];
+    const uint8_t *hin = (const uint8_t *)inputs[0];
+    uint8_t *hout = (uint8_t *)outputs[0];
+    int k = 0;
+    for (int64_t p0 = 0; p0 < npx; p0 += per, ++k) {
+        const int64_t n = std::min(per, npx - p0);
+        cudaStream_t t = exe->stripes[k % 3];
+        check_cuda(cudaMemcpyAsync(din + p0 * 4, hin + p0 * 4, n * 4, cudaMemcpyHostToDevice, t), "h2d");
+        ZsChainArgs c = st.chain;
+        c.src = din + p0 * 4;
+        c.dst = dout + p0 * 4;
+        c.npx = n;
+        check_cuda(launch_chain(c, st.chain_src_fast, st.chain_dst_fast, E.sm_count, t), st.label.c_str());
+        check_cuda(cudaMemcpyAsync(hout + p0 * 4, dout + p0 * 4, n * 4, cudaMemcpyDeviceToHost, t), "d2h");
+    }
+    for (cudaStream_t t : exe->stripes) check_cuda(cudaStreamSynchronize(t), "synchronize");
+    return true;
+}
+
 int zs_run_host(zs_executable *exe, const void *const *inputs, uint32_t n_inputs, void *const *outputs,
                 uint32_t n_outputs) {
     return guarded([&] {
@@ -557,7 +600,10 @@ int zs_run_host(zs_executable *exe, const void *const *inputs, uint32_t n_inputs
         Executable &E = *exe->e;
         if (n_inputs != E.input_regs.size() || n_outputs != E.output_regs.size())
             fail(ZS_ERR_INVALID_ARG, "wrong number of inputs or outputs");
+        for (uint32_t i = 0; i < n_inputs; ++i) NEED(inputs[i]);
+        for (uint32_t j = 0; j < n_outputs; ++j) NEED(outputs[j]);
         E.ensure_buffers();
+        if (run_host_striped(exe, inputs, outputs)) return;
         cudaStream_t s = exe_stream(exe);
         std::vector<void *> ptrs = E.dev_buffers;
         for (uint32_t i = 0; i < n_inputs; ++i) {
