@@ -307,6 +307,13 @@ uint64_t zs_kernel_launch_count(void);
  * No counterpart in the reference (wgpu reports device loss through its own callbacks). */
 int zs_device_status(int device, uint32_t *flags);
 
+/* Diagnostic for the failure detection above: launches one warp whose mbarrier wait nothing
+ * completes, through the same bounded-wait routine as the pipelined kernels but with a limit
+ * of `limit_us` microseconds (1..1000000), and synchronises.  The kernel gives up and sets
+ * bit 0 of the device status word, which zs_device_status then reports.  No counterpart in
+ * the reference. */
+int zs_selftest_wait_timeout(int device, uint32_t limit_us);
+
 #ifdef __cplusplus
 }
 #endif

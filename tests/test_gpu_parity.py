@@ -275,3 +275,17 @@ def test_blend_resize_plan():
     fused = zs.Linker.from_included().compile(c).lower_to()
     plain = zs.Linker.from_included().compile(c).lower_to(zs.Capabilities(mode=zs.Mode.PerOpF32))
     assert fused.kernel_count() < plain.kernel_count()
+
+
+def test_bounded_wait_timeout_is_reported():
+    # Failure detection without a GPU fault: a wait that nothing completes gives up after its
+    # limit, the status word reports it once (reading clears it), and the context still works.
+    import time
+    assert zs.device_status(0) == 0
+    t0 = time.perf_counter()
+    zs.selftest_wait_timeout(0, 2000)
+    assert time.perf_counter() - t0 < 5.0
+    assert zs.device_status(0) == 1
+    assert zs.device_status(0) == 0
+    img = srgb_gradient_noise(64, 48, seed=1)
+    assert maxdiff(P.ours_chain(img), P.oracle_chain(img)) <= LSB

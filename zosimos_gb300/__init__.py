@@ -164,6 +164,7 @@ def _lib():
             "zs_device_free": ([P], None), "zs_memcpy_h2d": ([P, P, U64], I32), "zs_memcpy_d2h": ([P, P, U64], I32),
             "zs_device_synchronize": ([], I32), "zs_kernel_launch_count": ([], U64),
             "zs_device_status": ([ctypes.c_int32, pU32], I32),
+            "zs_selftest_wait_timeout": ([ctypes.c_int32, U32], I32),
             "zs_descriptor_is_consistent": ([pD], I32), "zs_descriptor_byte_len": ([pD], U64),
             "zs_texel_bytes": ([U32], U32),
             "zs_batch_thumbnails": ([P, P, P, P, U32, U32, P, P], I32),
@@ -184,6 +185,12 @@ def _check(rc: int) -> None:
 
 def kernel_launch_count() -> int:
     return int(_lib().zs_kernel_launch_count())
+
+
+def selftest_wait_timeout(device: int = 0, limit_us: int = 2000) -> None:
+    """Run a kernel whose bounded wait nothing completes (it gives up after `limit_us` and
+    sets bit 0 of the device status word, as a real timeout would)."""
+    _check(_lib().zs_selftest_wait_timeout(device, limit_us))
 
 
 def device_status(device: int = 0) -> int:

@@ -719,6 +719,14 @@ int zs_batch_thumbnails(zs_executable *chain, const void *const *images, const u
 
 uint64_t zs_kernel_launch_count(void) { return kernel_launch_count(); }
 
+int zs_selftest_wait_timeout(int device, uint32_t limit_us) {
+    return guarded([&] {
+        if (limit_us == 0 || limit_us > 1000000) fail(ZS_ERR_INVALID_ARG, "limit_us out of range");
+        check_cuda(init_device_tables(device), "device tables");
+        check_cuda(wait_selftest(device, limit_us), "wait self test");
+    });
+}
+
 int zs_device_status(int device, uint32_t *flags) {
     return guarded([&] {
         NEED(flags);

@@ -9,3 +9,4 @@
 #include "k_layers.cu"
 #include "k_batch.cu"
 #include "k_noalloc.cu"
+#include "k_selftest.cu"

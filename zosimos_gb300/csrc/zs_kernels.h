@@ -29,6 +29,9 @@ cudaError_t launch_chain(const ZsChainArgs &args, uint8_t src_fast, uint8_t dst_
 // A stack of affine-transformed layers blended in one pass (k_layers.cu).
 cudaError_t launch_layers(const ZsLayersArgs &args, int sm_count, cudaStream_t stream);
 
+// Runs the bounded-wait self test on `device` (k_selftest.cu): a wait that nothing
+// completes gives up after `limit_us` and sets ZS_DEVSTAT_WAIT_TIMEOUT.
+cudaError_t wait_selftest(int device, uint32_t limit_us);
 // Device status word (ZS_DEVSTAT_* bits) of `device`, optionally cleared after reading.
 cudaError_t read_device_status(int device, uint32_t *flags, bool clear);
 // Number of kernel launches issued since process start (instrumentation for the bench).

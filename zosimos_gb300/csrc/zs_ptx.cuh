@@ -35,13 +35,14 @@ __device__ __forceinline__ uint64_t zs_globaltimer() {
     return t;
 }
 
-// Bounded wait for the phase of `bar` with the given parity to complete.
-__device__ __forceinline__ bool zs_mbar_wait(uint32_t bar, uint32_t parity) {
+// Bounded wait for the phase of `bar` with the given parity to complete; false when
+// `limit_ns` of global time passed first.
+__device__ __forceinline__ bool zs_mbar_wait(uint32_t bar, uint32_t parity, uint64_t limit_ns = ZS_WAIT_NS) {
     if (zs_mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = zs_globaltimer();
     for (;;) {
         if (zs_mbar_try_wait(bar, parity)) return true;
-        if (zs_globaltimer() - t0 > ZS_WAIT_NS) return false;
+        if (zs_globaltimer() - t0 > limit_ns) return false;
     }
 }
 
