@@ -63,15 +63,17 @@ __device__ __forceinline__ float4 zs_batch_chain(uint32_t w, const ZsBatchArgs &
     return make_float4(r, g, b, (float)(w >> 24) / 255.0f);
 }
 
-// The same chain on two texels at once: FP32x2 matrix products, MUFU cube roots.
-__device__ __forceinline__ void zs_batch_chain2(uint32_t w0, uint32_t w1, const ZsBatchArgs &a, float2 &r, float2 &g,
-                                                float2 &b) {
-    r = make_float2(zs_srgb_decode_lut[w0 & 255u], zs_srgb_decode_lut[w1 & 255u]);
-    g = make_float2(zs_srgb_decode_lut[(w0 >> 8) & 255u], zs_srgb_decode_lut[(w1 >> 8) & 255u]);
-    b = make_float2(zs_srgb_decode_lut[(w0 >> 16) & 255u], zs_srgb_decode_lut[(w1 >> 16) & 255u]);
+// The same chain on two texels at once: decode through the lane-replicated shared table
+// of the chain kernel, FP32x2 matrix products, MUFU cube roots.
+template <bool NONNEG>
+__device__ __forceinline__ void zs_batch_chain2(uint32_t w0, uint32_t w1, const unsigned char *lut, uint32_t lane4,
+                                                const ZsBatchArgs &a, float2 &r, float2 &g, float2 &b) {
+    r = make_float2(zs_dec<0>(lut, w0, lane4), zs_dec<0>(lut, w1, lane4));
+    g = make_float2(zs_dec<1>(lut, w0, lane4), zs_dec<1>(lut, w1, lane4));
+    b = make_float2(zs_dec<2>(lut, w0, lane4), zs_dec<2>(lut, w1, lane4));
     zs_m3x2<false>(a.m2[0], r, g, b);
     if (a.flags & ZS_CHAIN_CBRT) {
-        if (a.flags & ZS_CHAIN_CBRT_NONNEG) {
+        if (NONNEG) {
             zs_cbrt2(r);
             zs_cbrt2(g);
             zs_cbrt2(b);
@@ -101,8 +103,14 @@ __device__ __forceinline__ void zs_box_window(int u, float s, float f, int len, 
     j1 = min((int)ceilf(hi), len);
 }
 
+template <bool NONNEG>
 __global__ void __launch_bounds__(ZS_BATCH_THREADS) zs_batch_kernel(const __grid_constant__ ZsBatchArgs a) {
+    extern __shared__ __align__(16) float zs_batch_lut[];      // [code][64], lanes 32..63 unused
+    for (int i = threadIdx.x; i < 256 * 32; i += blockDim.x) zs_batch_lut[(i >> 5) * 64 + (i & 31)] = zs_srgb_decode_lut[i >> 5];
+    __syncthreads();
+    const unsigned char *lut = reinterpret_cast<const unsigned char *>(zs_batch_lut);
     const int lane = threadIdx.x & 31;
+    const uint32_t lane4 = (uint32_t)lane << 2;
     const int warps = (int)(gridDim.x * (blockDim.x >> 5));
     const int total = a.prefix[a.n];
     for (int it = (int)(blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)); it < total; it += warps) {
@@ -140,7 +148,7 @@ __global__ void __launch_bounds__(ZS_BATCH_THREADS) zs_batch_kernel(const __grid
                     fmaxf(fminf(hix, (float)jx + 1.f) - fmaxf(lox, (float)jx), 0.f),
                     two ? fmaxf(fminf(hix, (float)jx + 2.f) - fmaxf(lox, (float)jx + 1.f), 0.f) : 0.f);
                 float2 r, g, b;
-                zs_batch_chain2(w0, w1, a, r, g, b);
+                zs_batch_chain2<NONNEG>(w0, w1, lut, lane4, a, r, g, b);
                 const float2 al = make_float2((float)(w0 >> 24) * (1.0f / 255.0f), (float)(w1 >> 24) * (1.0f / 255.0f));
                 sr = __ffma2_rn(wx, r, sr);
                 sg = __ffma2_rn(wx, g, sg);
@@ -246,14 +254,21 @@ int batch_thumbnails(Executable *chain, const void *const *images, const uint32_
     a.flags = cs->chain.flags;
     std::memcpy(a.m, cs->chain.m, sizeof(a.m));
     std::memcpy(a.m2, cs->chain.m2, sizeof(a.m2));
+    auto kernel = (a.flags & ZS_CHAIN_CBRT_NONNEG) ? zs_batch_kernel<true> : zs_batch_kernel<false>;
+    const size_t smem = 256 * 64 * sizeof(float);
+    e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, zs_batch_kernel, ZS_BATCH_THREADS, 0);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, ZS_BATCH_THREADS, smem);
+    if (e != cudaSuccess) {
+        set_last_error(std::string("zs_batch_thumbnails: ") + cudaGetErrorString(e));
+        return ZS_ERR_DEVICE;
+    }
     if (per_sm < 1) per_sm = 1;
     long long blocks = (long long)chain->sm_count * per_sm;
     const long long need = ((long long)prefix[n] + ZS_BATCH_THREADS / 32 - 1) / (ZS_BATCH_THREADS / 32);
     if (blocks > need) blocks = need;
     if (blocks < 1) return ZS_OK;
-    zs_batch_kernel<<<(unsigned)blocks, ZS_BATCH_THREADS, 0, stream>>>(a);
+    kernel<<<(unsigned)blocks, ZS_BATCH_THREADS, smem, stream>>>(a);
     g_kernel_launches.fetch_add(1);
     e = cudaGetLastError();
     if (e != cudaSuccess) {
