@@ -28,6 +28,9 @@ struct Pending {
     int vfirst_slot = -1, vcount_slot = -1, vweight_slot = -1;
     int vimg_slot = -1, vimg_index_slot = -1;
     HProgram prog;
+    // virt1: the gathered image's producer sources and program (evaluated per tap)
+    int vsrc_slot[2] = {-1, -1};
+    HProgram vprog;
     std::string label;
     // ZS_PR_LAYERS: base (src_slot[0] when has_below, else a.cons[0..3]) and the layers.
     std::vector<LayerRef> layers;
@@ -210,7 +213,7 @@ struct Planner {
         // Pixel program: FP64 host program -> FP32 parameters.
         ZsPixelProgram &pp = st.raster.prog;
         std::memset(&pp, 0, sizeof(pp));
-        int nf = 0, np = 0;
+        int nf = 0;
         auto fmt_id = [&](const ZsFormat &f) -> uint8_t {
             for (int i = 0; i < nf; ++i)
                 if (format_equal(st.raster.fmts[i], f)) return (uint8_t)i;
@@ -218,30 +221,42 @@ struct Planner {
             st.raster.fmts[nf] = f;
             return (uint8_t)nf++;
         };
-        for (const HInstr &hi : p.prog.ins) {
-            if (pp.n >= ZS_MAX_INSTR) fail(ZS_ERR_UNIMPLEMENTED, "fused program too long");
-            ZsPInstr &o = pp.ins[pp.n++];
-            o.op = hi.op;
-            o.a = hi.a;
-            o.b = hi.b;
-            o.p = (uint16_t)np;
-            if (hi.op == ZS_P_MAT3) {
-                if (np + 9 > ZS_MAX_PARAMS) fail(ZS_ERR_UNIMPLEMENTED, "too many parameters");
-                for (int k = 0; k < 9; ++k) pp.prm[np++] = (float)hi.mat.m[k];
-            } else if (hi.op == ZS_P_INJECT) {
-                if (np + 8 > ZS_MAX_PARAMS) fail(ZS_ERR_UNIMPLEMENTED, "too many parameters");
-                for (int k = 0; k < 8; ++k) pp.prm[np++] = (float)hi.v[k];
-            } else if (hi.op == ZS_P_QUANT) {
-                o.a = fmt_id(hi.fa);
-            } else if (hi.op == ZS_P_TRANSMUTE) {
-                o.a = fmt_id(hi.fa);
-                o.b = fmt_id(hi.fb);
+        auto compile = [&](const HProgram &hp, ZsPixelProgram &out) {
+            int np = 0;
+            for (const HInstr &hi : hp.ins) {
+                if (out.n >= ZS_MAX_INSTR) fail(ZS_ERR_UNIMPLEMENTED, "fused program too long");
+                ZsPInstr &o = out.ins[out.n++];
+                o.op = hi.op;
+                o.a = hi.a;
+                o.b = hi.b;
+                o.p = (uint16_t)np;
+                if (hi.op == ZS_P_MAT3) {
+                    if (np + 9 > ZS_MAX_PARAMS) fail(ZS_ERR_UNIMPLEMENTED, "too many parameters");
+                    for (int k = 0; k < 9; ++k) out.prm[np++] = (float)hi.mat.m[k];
+                } else if (hi.op == ZS_P_INJECT) {
+                    if (np + 8 > ZS_MAX_PARAMS) fail(ZS_ERR_UNIMPLEMENTED, "too many parameters");
+                    for (int k = 0; k < 8; ++k) out.prm[np++] = (float)hi.v[k];
+                } else if (hi.op == ZS_P_QUANT) {
+                    o.a = fmt_id(hi.fa);
+                } else if (hi.op == ZS_P_TRANSMUTE) {
+                    o.a = fmt_id(hi.fa);
+                    o.b = fmt_id(hi.fb);
+                }
             }
+        };
+        compile(p.prog, pp);
+        if (p.a.virt1) {
+            HProgram vp = p.vprog;
+            vp.optimise();
+            std::memset(&st.raster.vprog, 0, sizeof(st.raster.vprog));
+            compile(vp, st.raster.vprog);
+            st.vsrc_slot[0] = p.vsrc_slot[0];
+            st.vsrc_slot[1] = p.vsrc_slot[1];
         }
         // Gathers with no program between equal formats copy texel bytes verbatim.
         const uint8_t pr = p.a.producer;
-        if (pp.n == 0 && (pr == ZS_PR_QUAD || (pr == ZS_PR_AFFINE && !p.a.bilinear) || pr == ZS_PR_PALETTE ||
-                          pr == ZS_PR_INDEX)) {
+        if (pp.n == 0 && !p.a.virt1 &&
+            (pr == ZS_PR_QUAD || (pr == ZS_PR_AFFINE && !p.a.bilinear) || pr == ZS_PR_PALETTE || pr == ZS_PR_INDEX)) {
             bool same = true;
             const int gather_src = (pr == ZS_PR_QUAD || pr == ZS_PR_AFFINE) ? 1 : 0;
             same = format_equal(p.a.src[gather_src].fmt, d.fmt) && p.a.src[gather_src].fmt.bpp == d.fmt.bpp;
@@ -345,6 +360,46 @@ struct Planner {
         return p;
     }
 
+    // A pixel-aligned pending value (LOAD or BLEND producer and its program) that only this
+    // gather reads is not stored: the gather evaluates it at every tap (fused mode).  Plain
+    // decodes of one buffer are left to need(), which forwards the buffer itself.
+    bool attach_virtual(Pending &p, uint32_t reg) {
+        if (E.mode != ZS_MODE_FUSED) return false;
+        Val &v = vals[reg];
+        if (v.materialized || !v.pend || remaining[reg] != 0 || out_slot_of[reg] >= 0) return false;
+        const Pending &q = *v.pend;
+        if ((q.a.producer != ZS_PR_LOAD && q.a.producer != ZS_PR_BLEND) || q.a.nsrc < 1 || q.a.nsrc > 2) return false;
+        if (q.a.producer == ZS_PR_LOAD && q.a.nsrc == 1) {
+            HProgram t = q.prog;
+            t.optimise();
+            if (t.ins.empty()) return false;
+        }
+        p.a.virt1 = 1;
+        p.a.vproducer = q.a.producer;
+        p.a.vmode = q.a.blend_mode;
+        p.a.vstraight = q.a.straight;
+        p.a.vnsrc = q.a.nsrc;
+        p.a.vrect[0] = q.a.rect[0];
+        p.a.vrect[1] = q.a.rect[1];
+        for (int i = 0; i < 2; ++i) {
+            p.a.vsrc[i] = q.a.src[i];
+            p.vsrc_slot[i] = q.src_slot[i];
+        }
+        p.vprog = q.prog;
+        const Desc &d = desc(reg);
+        p.a.src[1].width = (int)d.width;
+        p.a.src[1].height = (int)d.height;
+        p.a.src[1].fmt = format_of(d);
+        p.a.src[1].stride = 0;
+        p.src_slot[1] = -1;
+        if (p.a.nsrc < 2) p.a.nsrc = 2;
+        p.label += " [evaluates " + q.label + " per tap]";
+        v.pend.reset();
+        v.materialized = true;     // consumed by the gather
+        v.slot = -1;
+        return true;
+    }
+
     // A source operand must be readable from a buffer.  A pending value that is just the
     // decode of one buffer (LOAD with an empty program, e.g. sRGB8 -> linear FP32 whose
     // matrix folded to the identity) is forwarded to that buffer instead of being stored.
@@ -388,7 +443,7 @@ struct Planner {
     bool try_layer(uint32_t r, const Op &op) {
         if (E.mode != ZS_MODE_FUSED || op.rect.x != 0 || op.rect.y != 0) return false;
         Val &tv = vals[op.b];
-        if (tv.materialized || !tv.pend || tv.pend->a.producer != ZS_PR_AFFINE || tv.pend->a.has_below ||
+        if (tv.materialized || !tv.pend || tv.pend->a.producer != ZS_PR_AFFINE || tv.pend->a.has_below || tv.pend->a.virt1 ||
             remaining[op.b] != 0 || out_slot_of[op.b] >= 0)
             return false;
         const Desc &d = P.ops[r].desc;
@@ -607,8 +662,9 @@ struct Planner {
             case OpKind::Affine: {
                 use(op.a);
                 use(op.b);
-                need(op.b);
                 auto p = new_pending(ZS_PR_AFFINE, d.width, d.height, op.u0 ? "affine bilinear" : "affine nearest");
+                const bool virt = attach_virtual(*p, op.b);
+                if (!virt) need(op.b);
                 float solid[4];
                 if (solid_value(op.a, solid)) {
                     // Painting onto a constant canvas: the canvas is never stored.
@@ -621,7 +677,7 @@ struct Planner {
                     set_src(*p, 0, op.a);
                     p->a.has_below = 1;
                 }
-                set_src(*p, 1, op.b);
+                if (!virt) set_src(*p, 1, op.b);
                 p->a.bilinear = (uint8_t)op.u0;
                 Mat3 fwd{};
                 for (int k = 0; k < 9; ++k) fwd.m[k] = op.fparams[k];

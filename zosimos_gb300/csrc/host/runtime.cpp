@@ -123,6 +123,8 @@ void Executable::record_range(cudaStream_t stream, const std::vector<void *> &pt
             a.vweights = st.vweight_slot >= 0 ? (const float *)ptrs[st.vweight_slot] : nullptr;
             a.vimg = st.vimg_slot >= 0 ? (const uint8_t *)ptrs[st.vimg_slot] : nullptr;
             a.vimg_index = st.vimg_index_slot >= 0 ? (const int32_t *)ptrs[st.vimg_index_slot] : nullptr;
+            for (int i = 0; i < 2; ++i)
+                a.vsrc[i].ptr = st.vsrc_slot[i] >= 0 ? (const uint8_t *)ptrs[st.vsrc_slot[i]] : nullptr;
             check_cuda(launch_raster(a, sm_count, stream), st.label.c_str());
         } break;
         }

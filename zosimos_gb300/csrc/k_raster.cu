@@ -59,6 +59,22 @@ __device__ __forceinline__ float4 zs_lerp4(float4 a, float4 b, float t) {
                        a.w + (b.w - a.w) * t);
 }
 
+// The gathered image of an AFFINE launch at (x, y): a stored texel, or (virt1) its
+// pixel-aligned producer and program evaluated here.
+__device__ __forceinline__ float4 zs_src1_px(const ZsRasterArgs &a, int x, int y) {
+    if (!a.virt1) return zs_load_px(a.src[1], x, y);
+    float4 r = zs_load_px(a.vsrc[0], x, y), r2 = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (a.vproducer == ZS_PR_BLEND) {
+        const int ax = x - a.vrect[0], ay = y - a.vrect[1];
+        if (ax >= 0 && ay >= 0 && ax < a.vsrc[1].width && ay < a.vsrc[1].height)
+            zs_blend_px(r, zs_load_px(a.vsrc[1], ax, ay), a.vmode, a.vstraight);
+    } else if (a.vnsrc > 1) {
+        r2 = zs_load_px(a.vsrc[1], x, y);
+    }
+    zs_run_program(a.vprog, a.fmts, r, r2);
+    return r;
+}
+
 __global__ void __launch_bounds__(256) zs_raster_kernel(const __grid_constant__ ZsRasterArgs a) {
     // Affine gathers walk 32 x 8 pixel tiles (8 x 4 per warp) so that a warp's samples
     // fall into a compact source footprint; everything else walks rows.
@@ -138,7 +154,7 @@ __global__ void __launch_bounds__(256) zs_raster_kernel(const __grid_constant__ 
                     raw = zs_load_raw(s1.ptr + (int64_t)iy * s1.stride + (int64_t)ix * s1.fmt.bpp, s1.fmt.bpp);
                     is_raw = true;
                 } else {
-                    r = zs_load_px(s1, ix, iy);
+                    r = zs_src1_px(a, ix, iy);
                 }
             } else if (inside) {
                 float tx = qx - 0.5f, ty = qy - 0.5f;
@@ -147,8 +163,8 @@ __global__ void __launch_bounds__(256) zs_raster_kernel(const __grid_constant__ 
                 int x0 = (int)fx0, y0 = (int)fy0;
                 int xa = zs_clampi(x0, 0, s1.width - 1), xb = zs_clampi(x0 + 1, 0, s1.width - 1);
                 int ya = zs_clampi(y0, 0, s1.height - 1), yb = zs_clampi(y0 + 1, 0, s1.height - 1);
-                float4 top = zs_lerp4(zs_load_px(s1, xa, ya), zs_load_px(s1, xb, ya), fx);
-                float4 bot = zs_lerp4(zs_load_px(s1, xa, yb), zs_load_px(s1, xb, yb), fx);
+                float4 top = zs_lerp4(zs_src1_px(a, xa, ya), zs_src1_px(a, xb, ya), fx);
+                float4 bot = zs_lerp4(zs_src1_px(a, xa, yb), zs_src1_px(a, xb, yb), fx);
                 r = zs_lerp4(top, bot, fy);
             } else if (a.has_below) {
                 if (a.raw_copy) {
@@ -295,7 +311,8 @@ cudaError_t launch_raster(const ZsRasterArgs &args, int sm_count, cudaStream_t s
     const int64_t n = (int64_t)args.width * args.height;
     if (n <= 0) return cudaSuccess;
     if (args.producer == ZS_PR_RESAMPLE_2D) return launch_resample2d(args, sm_count, stream);
-    if (args.producer == ZS_PR_AFFINE && args.bilinear && !args.raw_copy && args.src[1].fmt.fast == ZS_FAST_F16X4 &&
+    if (args.producer == ZS_PR_AFFINE && args.bilinear && !args.raw_copy && !args.virt1 &&
+        args.src[1].fmt.fast == ZS_FAST_F16X4 &&
         args.aff[6] == 0.f && args.aff[7] == 0.f && args.aff[8] == 1.f) {
         int64_t blocks = (int64_t)((args.width + 31) / 32) * ((args.height + 15) / 16);
         const int64_t cap = (int64_t)(sm_count > 0 ? sm_count : 148) * 8;

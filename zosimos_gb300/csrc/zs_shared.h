@@ -102,7 +102,7 @@ struct ZsRasterArgs {
     uint8_t bilinear;     // AFFINE: bilinear sampling
     uint8_t blend_mode;
     uint8_t straight;
-    uint8_t pad0;
+    uint8_t virt1;        // AFFINE: src1 is evaluated per tap (vsrc / vprog below), not stored
     ZsSource src[ZS_MAX_SRCS];
     int32_t rect[4];      // QUAD target rect / BLEND offset rect
     int32_t sel[4];       // QUAD selection rect in src1
@@ -131,8 +131,16 @@ struct ZsRasterArgs {
     int64_t dst_stride;
     int32_t width, height;
     ZsFormat dst_fmt;
-    ZsFormat fmts[ZS_MAX_FMTS];   // formats referenced by QUANT / TRANSMUTE
+    ZsFormat fmts[ZS_MAX_FMTS];   // formats referenced by QUANT / TRANSMUTE (both programs)
     ZsPixelProgram prog;
+    // virt1: the pixel-aligned producer of the gathered image -- LOAD of vsrc (r = vsrc[0],
+    // r2 = vsrc[1]) or BLEND of vsrc[1] at offset vrect over vsrc[0] -- and its program, run
+    // at every tap instead of materialising the image.
+    ZsSource vsrc[2];
+    int32_t vrect[2];
+    uint8_t vproducer, vmode, vstraight, vnsrc;
+    int32_t pad3;
+    ZsPixelProgram vprog;
 };
 
 // RESAMPLE_2D output tile (columns x rows; the rows per launch are 8, 16 or ZS_RS_TH) and
