@@ -108,6 +108,27 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
+def max_over_ranks(dist, value: float, device: str = "cuda") -> float:
+    """The slowest rank's figure: every rank contributes its own, every rank gets the max
+    (no data path collective: only the timings are exchanged)."""
+    if not dist:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_seed(rank: int) -> int:
+    """Each rank runs its own replica: a different seeded image of the same shape."""
+    return 1 + rank
+
+
+def aggregate_mpix(world: int, npx: int, seconds: float) -> float:
+    """Whole-job throughput: the pixels all ranks processed per second of the slowest rank."""
+    return world * npx / seconds / 1e6
+
+
 def cpu_baseline(seconds: float = 10.0, threads: int = 0):
     """The plain per-op FP32 CPU pipeline (oracle port) on a bounded sample: 1024 rows
     of the 4096-wide image, repeated until `seconds` have passed."""
@@ -182,7 +203,7 @@ def run_ours(args, rank, world, dist):
     stream = torch.cuda.Stream()          # a real stream: graphs cannot capture the legacy default stream
     sh = stream.cuda_stream
 
-    img = srgb_gradient_noise(W, H, seed=1 + rank)
+    img = srgb_gradient_noise(W, H, seed=replica_seed(rank))
     host_in = rgba_bytes(img)
 
     def lowered(mode):
@@ -232,11 +253,7 @@ def run_ours(args, rank, world, dist):
         e1.record(stream)
         torch.cuda.synchronize()
         launches = zs.kernel_launch_count() - k0
-        ms = e0.elapsed_time(e1)
-        if dist:
-            t = torch.tensor([ms], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            ms = float(t.item())
+        ms = max_over_ranks(dist, e0.elapsed_time(e1))
         return ms / steps, launches
 
     with ClockSampler(dev) as clocks:
@@ -258,18 +275,14 @@ def run_ours(args, rank, world, dist):
     t0 = time.perf_counter()
     for _ in range(args.steps):
         zs._check(lib.zs_run_host(fused._h, inp, 1, outp, 1))
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    if dist:
-        t = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = max_over_ranks(dist, (time.perf_counter() - t0) / args.steps)
     lib.zs_host_free(hin)
     lib.zs_host_free(hout)
 
     if rank != 0:
         return
     peak, peak_kind = _peaks()
-    mpix = world * NPX / (ms_fused * 1e-3) / 1e6
+    mpix = aggregate_mpix(world, NPX, ms_fused * 1e-3)
     achieved = ALGO_BYTES / (ms_fused * 1e-3) / 1e9
     traffic = _profiled_traffic()
     line = {
@@ -280,9 +293,9 @@ def run_ours(args, rank, world, dist):
                                "4096x4096 RGBA8 sRGB per GPU, seeded gradient+noise",
                    "l2": "4 rotating input/output buffer pairs (536 MB) > 129 MB L2",
                    "parallelism": f"replicas x{world}", "graph": "CUDA graph replay"},
-        "plain_per_op_fp32": {"value": round(world * NPX / (ms_plain * 1e-3) / 1e6, 1), "unit": "Mpix/s",
+        "plain_per_op_fp32": {"value": round(aggregate_mpix(world, NPX, ms_plain * 1e-3), 1), "unit": "Mpix/s",
                               "ms_per_step": round(ms_plain, 4), "kernels": plain.kernel_count()},
-        "per_op_fp16": {"value": round(world * NPX / (ms_plain16 * 1e-3) / 1e6, 1), "unit": "Mpix/s",
+        "per_op_fp16": {"value": round(aggregate_mpix(world, NPX, ms_plain16 * 1e-3), 1), "unit": "Mpix/s",
                         "ms_per_step": round(ms_plain16, 4), "kernels": plain16.kernel_count()},
         "speedup_vs_plain_fp32": round(ms_plain / ms_fused, 2),
         "max_lsb_vs_plain_fp32": max_lsb,
@@ -290,7 +303,7 @@ def run_ours(args, rank, world, dist):
                      "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": ALGO_BYTES,
                      "traffic": traffic},
-        "e2e": {"value": round(world * NPX / e2e_s / 1e6, 1), "unit": "Mpix/s",
+        "e2e": {"value": round(aggregate_mpix(world, NPX, e2e_s), 1), "unit": "Mpix/s",
                 "h2d_bytes_per_step": NPX * 4, "d2h_bytes_per_step": NPX * 4, "ms_per_step": round(e2e_s * 1e3, 3)},
         "gpu_launches": launches,
         "clocks": clocks.summary(),
