@@ -289,3 +289,15 @@ def test_bounded_wait_timeout_is_reported():
     assert zs.device_status(0) == 0
     img = srgb_gradient_noise(64, 48, seed=1)
     assert maxdiff(P.ours_chain(img), P.oracle_chain(img)) <= LSB
+
+
+@pytest.mark.parametrize("src,out", [((4, 2), (1, 1)), ((6, 7), (2, 3)), ((2, 2), (9, 5)), ((3, 2), (1, 1)),
+                                     ((5, 7), (2, 3)), ((16, 1), (3, 1)), ((2, 300), (2, 7))])
+@pytest.mark.parametrize("simt", [False, True])
+def test_resample_tiny(src, out, simt):
+    # Images smaller than one tile, one TMA box or one 16-byte row; 1 x 1 results.
+    from zosimos_gb300.synthetic import linear_gradient_gauss
+    img = linear_gradient_gauss(src[0], src[1], seed=17)
+    for filt in (zs.Filter.Lanczos3, zs.Filter.Box, zs.Filter.Triangle):
+        ours = P.ours_resample(img, out, filt, simt_resample=simt)
+        assert np.abs(ours - P.oracle_resample(img, out, filt)).max() <= F16_TOL
