@@ -113,13 +113,9 @@ __global__ void __launch_bounds__(ZS_BATCH_THREADS) zs_batch_kernel(const __grid
     const uint32_t lane4 = (uint32_t)lane << 2;
     const int warps = (int)(gridDim.x * (blockDim.x >> 5));
     const int total = a.prefix[a.n];
+    int lo = 0;   // image of the current item: items only move forward, so scan from the last one
     for (int it = (int)(blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)); it < total; it += warps) {
-        int lo = 0, hi = a.n - 1;           // last image whose first item is <= it
-        while (lo < hi) {
-            const int mid = (lo + hi + 1) >> 1;
-            if (a.prefix[mid] <= it) lo = mid;
-            else hi = mid - 1;
-        }
+        while (a.prefix[lo + 1] <= it) ++lo;
         const ZsBatchImage I = a.images[lo];
         const int segs = (I.tw + 31) >> 5, local = it - a.prefix[lo];
         const int v = local / segs, u = (local - v * segs) * 32 + lane;
@@ -129,12 +125,10 @@ __global__ void __launch_bounds__(ZS_BATCH_THREADS) zs_batch_kernel(const __grid
         float lox, hix, loy, hiy;
         zs_box_window(u, I.sx, I.fx, I.width, jx0, jx1, lox, hix);
         zs_box_window(v, I.sy, I.fy, I.height, jy0, jy1, loy, hiy);
-        // Weight sums once per output; per row, source texels go through the
-        // chain two at a time (the odd tail pairs with itself at weight 0).
-        float wsx = 0.f, wsy = 0.f;
-        for (int jx = jx0; jx < jx1; ++jx) wsx += fmaxf(fminf(hix, (float)jx + 1.f) - fmaxf(lox, (float)jx), 0.f);
-        for (int jy = jy0; jy < jy1; ++jy) wsy += fmaxf(fminf(hiy, (float)jy + 1.f) - fmaxf(loy, (float)jy), 0.f);
-        const float wsum = wsx * wsy;
+        // The weights of a window sum to its length clipped to the image; per row, source
+        // texels go through the chain two at a time (the odd tail pairs with itself at weight 0).
+        const float wsum = fmaxf(fminf(hix, (float)jx1) - fmaxf(lox, (float)jx0), 0.f) *
+                           fmaxf(fminf(hiy, (float)jy1) - fmaxf(loy, (float)jy0), 0.f);
         float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
         for (int jy = jy0; jy < jy1; ++jy) {
             const float wy = fminf(hiy, (float)jy + 1.f) - fmaxf(loy, (float)jy);
