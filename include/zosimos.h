@@ -184,6 +184,13 @@ int zs_cmd_resize(zs_cmd *cmd, uint32_t src, uint32_t width, uint32_t height, ui
 /* Extension of resize with a filter: 0 Box (area), 1 Lanczos-3, 2 Triangle. */
 int zs_cmd_resize_filtered(zs_cmd *cmd, uint32_t src, uint32_t width, uint32_t height,
                            uint32_t filter, uint32_t *reg);
+/* CommandBuffer::derivative (command.rs:1493): first derivative by a 3x3 operator along the
+ * width or height (box3.frag, command.rs:3343-3409); the result keeps the descriptor of
+ * `src`, its alpha is 1.  Methods (DerivativeMethod order): 0 Roberts, 1 Prewitt, 2 Sobel,
+ * 3 Scharr3, 4 Scharr4, 5 Scharr5, 6 Scharr3To4Bit, 7 Scharr5Tab, 8 Scharr3To8Bit; Roberts,
+ * Scharr4, Scharr5 and Scharr5Tab fail in zs_compile with ZS_ERR_UNIMPLEMENTED as in the
+ * reference.  direction: 0 Width, 1 Height. */
+int zs_cmd_derivative(zs_cmd *cmd, uint32_t src, uint32_t method, uint32_t direction, uint32_t *reg);
 /* CommandBuffer::blend (command.rs:1509, UNIMPLEMENTED upstream, built here):
  * mode 0 Alpha/over, 1 multiply, 2 screen, 3 add; `above` placed at rect.x/rect.y. */
 int zs_cmd_blend(zs_cmd *cmd, uint32_t below, const zs_rect *rect, uint32_t above,

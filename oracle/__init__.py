@@ -235,6 +235,34 @@ def resample(src, width, height, filt="Lanczos3", f32=False):
 # ---------------------------------------------------------------- matrices
 
 
+DERIVATIVE = dict(Roberts=0, Prewitt=1, Sobel=2, Scharr3=3, Scharr4=4, Scharr5=5, Scharr3To4Bit=6, Scharr5Tab=7,
+                  Scharr3To8Bit=8)
+# Smoothing vectors of the implemented 3x3 operators (command.rs:3343-3409); the derivative
+# vector is [0.5, 0, -0.5] for all of them.
+DERIVATIVE_SMOOTHING = dict(Prewitt=(1 / 3, 1 / 3, 1 / 3), Sobel=(1 / 4, 1 / 2, 1 / 4),
+                            Scharr3=(46.84 / 256, 162.32 / 256, 46.84 / 256),
+                            Scharr3To4Bit=(3 / 16, 10 / 16, 3 / 16), Scharr3To8Bit=(47 / 256, 162 / 256, 47 / 256))
+
+
+def derivative_matrix(method: str, width: bool = True) -> np.ndarray:
+    """Row-major 3x3 of the operator as the reference builds it: the f32 outer product of
+    smoothing and derivative vectors (RowMatrix::with_outer_product), transposed along the
+    height (Direction::adjust_vertical_box)."""
+    a = np.float32(DERIVATIVE_SMOOTHING[method])
+    b = np.float32((0.5, 0.0, -0.5))
+    m = (a[:, None] * b[None, :]).astype(np.float32)
+    return (m if width else m.T).astype(np.float64)
+
+
+def box3(src, m, f32=False):
+    src = np.ascontiguousarray(src, dtype=_dtype(f32))
+    h, w = src.shape[:2]
+    out = np.empty_like(src)
+    m, pm = _d9(m)
+    getattr(lib(), _prefix(f32) + "box3")(_p(src), ctypes.c_int32(w), ctypes.c_int32(h), _p(out), pm)
+    return out
+
+
 def rgb_to_xyz(primaries="Bt709", whitepoint="D65") -> np.ndarray:
     out = np.zeros(9)
     lib().zo_rgb_to_xyz(ctypes.c_int32(PRIMARIES[primaries]), ctypes.c_int32(WHITEPOINT[whitepoint]), _p(out))

@@ -428,3 +428,21 @@ def oracle_layer_stack(layers16, transforms):
         O.affine(placed, img.astype(np.float64), inv3_f32(layer_affine(w, h, deg, s).transformation), True)
         O.blend(acc, placed, (0, 0), BLEND_CYCLE[i % 4], straight=False)
     return acc
+
+
+# ---------------------------------------------------------------- blend.rs:577-620 derivative
+
+
+def ours_derivative(bg, method, direction=zs.Direction.Width, mode=zs.Mode.Fused):
+    pool = Pool()
+    kb = pool.insert_srgb(bg)
+    c = CommandBuffer()
+    i = c.input(pool.descriptor(kb))
+    o, _ = c.output(c.derivative(i, method, direction))
+    return run(c, pool, [(i, kb)], [o], mode)[0]
+
+
+def oracle_derivative(bg, method: str, width=True):
+    h, w = bg.shape[:2]
+    lin = O.decode(O.SRGB_RGBA8, rgba_bytes(bg), w, h)
+    return O.encode(O.SRGB_RGBA8, O.box3(lin, O.derivative_matrix(method, width)))

@@ -301,3 +301,15 @@ def test_resample_tiny(src, out, simt):
     for filt in (zs.Filter.Lanczos3, zs.Filter.Box, zs.Filter.Triangle):
         ours = P.ours_resample(img, out, filt, simt_resample=simt)
         assert np.abs(ours - P.oracle_resample(img, out, filt)).max() <= F16_TOL
+
+
+@pytest.mark.parametrize("method", ["Prewitt", "Sobel", "Scharr3", "Scharr3To4Bit", "Scharr3To8Bit"])
+@pytest.mark.parametrize("mode", [zs.Mode.Fused, zs.Mode.PerOpF32])
+def test_derivative(background, goldens, method, mode):
+    # tests/blend.rs:577-620 (width), plus the height direction against the oracle.
+    m = getattr(zs.DerivativeMethod, method)
+    ours = P.ours_derivative(background, m, zs.Direction.Width, mode)
+    assert maxdiff(ours, P.oracle_derivative(background, method, True)) <= LSB
+    assert blockhash256(ours.reshape(512, 512, 4)) in goldens["derived_" + method]
+    ours_h = P.ours_derivative(background, m, zs.Direction.Height, mode)
+    assert maxdiff(ours_h, P.oracle_derivative(background, method, False)) <= LSB

@@ -178,3 +178,18 @@ def test_noalloc_rejects_oversized_without_device():
                    ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p]
     fn.restype = ctypes.c_int32
     assert fn(ctypes.c_void_p(16), 8192, 8192, ctypes.c_void_p(16), 4096, 4096, 1, None) == 10
+
+
+def test_derivative_plan_and_unimplemented_methods():
+    c = CommandBuffer()
+    i = c.input(Descriptor.srgb_rgba8(64, 64))
+    c.output(c.derivative(i, zs.DerivativeMethod.Sobel, zs.Direction.Height))
+    assert Linker.from_included().compile(c).lower_to().kernel_count() == 1
+    for m in (zs.DerivativeMethod.Roberts, zs.DerivativeMethod.Scharr4, zs.DerivativeMethod.Scharr5,
+              zs.DerivativeMethod.Scharr5Tab):
+        c = CommandBuffer()
+        i = c.input(Descriptor.srgb_rgba8(8, 8))
+        c.output(c.derivative(i, m))                 # the command is accepted ...
+        with pytest.raises(ZosimosError) as e:
+            Linker.from_included().compile(c)       # ... compiling it is NotYetImplemented
+        assert e.value.code == 2

@@ -131,3 +131,11 @@ def test_chain_oracle_fp32_close_to_fp64():
     a = P.oracle_chain(img).astype(int)
     b = P.oracle_chain(img, f32=True).astype(int)
     assert np.abs(a - b).max() <= 1
+
+
+@pytest.mark.parametrize("method", ["Prewitt", "Sobel", "Scharr3", "Scharr3To4Bit", "Scharr3To8Bit"])
+def test_derivative_goldens(background, goldens, method):
+    # tests/blend.rs:577-620: derivative along the width of background.png, stored as sRGB8.
+    lin = O.decode(O.SRGB_RGBA8, background.reshape(512, 2048), 512, 512)
+    out = O.encode(O.SRGB_RGBA8, O.box3(lin, O.derivative_matrix(method))).reshape(512, 512, 4)
+    assert blockhash256(out) in goldens["derived_" + method]

@@ -74,6 +74,15 @@ class Filter:
     Box, Lanczos3, Triangle = range(3)
 
 
+class DerivativeMethod:
+    """command.rs DerivativeMethod (Roberts, Scharr4, Scharr5, Scharr5Tab: not yet implemented)."""
+    Roberts, Prewitt, Sobel, Scharr3, Scharr4, Scharr5, Scharr3To4Bit, Scharr5Tab, Scharr3To8Bit = range(9)
+
+
+class Direction:
+    Width, Height = range(2)
+
+
 class Mode:
     Fused, PerOpF32, PerOpF16 = range(3)
 
@@ -150,6 +159,7 @@ def _lib():
             "zs_cmd_affine": ([P, U32, P, U32, U32, pU32], I32), "zs_cmd_resize": ([P, U32, U32, U32, pU32], I32),
             "zs_cmd_resize_filtered": ([P, U32, U32, U32, U32, pU32], I32),
             "zs_cmd_blend": ([P, U32, pR, U32, U32, pU32], I32), "zs_cmd_color_matrix": ([P, U32, P, pU32], I32),
+            "zs_cmd_derivative": ([P, U32, U32, U32, pU32], I32),
             "zs_cmd_output": ([P, U32, pU32, pD], I32), "zs_cmd_describe": ([P, U32, pD], I32),
             "zs_compile": ([P, ctypes.POINTER(P)], I32), "zs_program_free": ([P], None),
             "zs_lower": ([P, ctypes.POINTER(_CCaps), ctypes.POINTER(P)], I32), "zs_executable_free": ([P], None),
@@ -478,6 +488,9 @@ class CommandBuffer:
 
     def resize_filtered(self, src: int, size, filt: int) -> int:
         return self._reg(_lib().zs_cmd_resize_filtered, src, size[0], size[1], filt)
+
+    def derivative(self, src: int, method: int, direction: int = Direction.Width) -> int:
+        return self._reg(_lib().zs_cmd_derivative, src, method, direction)
 
     def blend(self, below: int, rect: Rectangle, above: int, mode: int) -> int:
         return self._reg(_lib().zs_cmd_blend, below, ctypes.byref(rect._c()), above, mode)

@@ -23,6 +23,7 @@ uint32_t cmd_solid(Command &c, const Desc &d, const float color[4]);
 uint32_t cmd_affine(Command &c, uint32_t below, const float m[9], uint32_t sampling, uint32_t above);
 uint32_t cmd_resize(Command &c, uint32_t src, uint32_t w, uint32_t h, bool filtered, uint32_t filter);
 uint32_t cmd_blend(Command &c, uint32_t below, const zs_rect &rect, uint32_t above, uint32_t mode);
+uint32_t cmd_derivative(Command &c, uint32_t src, uint32_t method, uint32_t direction);
 uint32_t cmd_output(Command &c, uint32_t src, Desc *outformat);
 int batch_thumbnails(Executable *chain, const void *const *images, const uint32_t *widths, const uint32_t *heights,
                      uint32_t n, uint32_t canvas, void *out, cudaStream_t stream);
@@ -325,6 +326,9 @@ int zs_cmd_resize_filtered(zs_cmd *cmd, uint32_t src, uint32_t width, uint32_t h
                            uint32_t *reg) {
     CMD_BODY(cmd_resize(cmd->c, src, width, height, true, filter));
 }
+int zs_cmd_derivative(zs_cmd *cmd, uint32_t src, uint32_t method, uint32_t direction, uint32_t *reg) {
+    return guarded([&] { NEED(cmd); NEED(reg); *reg = cmd_derivative(cmd->c, src, method, direction); });
+}
 int zs_cmd_blend(zs_cmd *cmd, uint32_t below, const zs_rect *rect, uint32_t above, uint32_t mode, uint32_t *reg) {
     return guarded([&] { NEED(cmd); NEED(rect); NEED(reg); *reg = cmd_blend(cmd->c, below, *rect, above, mode); });
 }
@@ -358,6 +362,13 @@ int zs_compile(const zs_cmd *cmd, zs_program **out) {
                 break;
             case OpKind::Bilinear:
             case OpKind::Solid: break;
+            case OpKind::Derivative:
+                // DerivativeMethod::to_shader: Roberts, Scharr4, Scharr5, Scharr5Tab are
+                // CompileError::NotYetImplemented (command.rs:3397-3402).
+                if (op.u0 == 0 || op.u0 == 4 || op.u0 == 5 || op.u0 == 7)
+                    fail(ZS_ERR_UNIMPLEMENTED, "derivative method not yet implemented");
+                p.uses[op.a]++;
+                break;
             case OpKind::Inject:
             case OpKind::Inscribe:
             case OpKind::InscribePlaced:

@@ -271,6 +271,38 @@ uint32_t cmd_affine(Command &c, uint32_t below, const float m[9], uint32_t sampl
     return c.push(op);
 }
 
+// CommandBuffer::derivative (command.rs:1493-1507) with the operator of
+// DerivativeMethod::to_shader (command.rs:3343-3409): the f32 outer product of a smoothing
+// and the derivative vector [0.5, 0, -0.5], transposed along the height.
+uint32_t cmd_derivative(Command &c, uint32_t src, uint32_t method, uint32_t direction) {
+    const Desc s = c.describe(src);
+    if (method > 8) fail(ZS_ERR_INVALID_ARG, "unknown derivative method");
+    if (direction > 1) fail(ZS_ERR_INVALID_ARG, "unknown derivative direction");
+    static const float smooth[9][3] = {
+        {0.f, 0.f, 0.f},                                    // Roberts (not yet implemented)
+        {1.f / 3.f, 1.f / 3.f, 1.f / 3.f},                  // Prewitt
+        {1.f / 4.f, 1.f / 2.f, 1.f / 4.f},                  // Sobel
+        {46.84f / 256.f, 162.32f / 256.f, 46.84f / 256.f},  // Scharr3
+        {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f},                   // Scharr4, Scharr5 (not yet implemented)
+        {3.f / 16.f, 10.f / 16.f, 3.f / 16.f},              // Scharr3To4Bit
+        {0.f, 0.f, 0.f},                                    // Scharr5Tab (not yet implemented)
+        {47.f / 256.f, 162.f / 256.f, 47.f / 256.f},        // Scharr3To8Bit
+    };
+    const float d[3] = {0.5f, 0.0f, -0.5f};
+    Op op{OpKind::Derivative};
+    op.a = src;
+    op.desc = s;
+    op.desc.row_stride = 0;
+    for (int j = 0; j < 3; ++j)
+        for (int i = 0; i < 3; ++i) {
+            const float v = smooth[method][j] * d[i];          // row j, column i
+            op.fparams[direction == 0 ? 3 * j + i : 3 * i + j] = v;
+        }
+    op.u0 = method;
+    op.u1 = direction;
+    return c.push(op);
+}
+
 uint32_t cmd_resize(Command &c, uint32_t src, uint32_t w, uint32_t h, bool filtered, uint32_t filter) {
     const Desc s = c.describe(src);
     if (w == 0 || h == 0) fail(ZS_ERR_OTHER, "empty resize");

@@ -742,6 +742,14 @@ struct Planner {
                 add_weights(*v, sd.height, d.height, op.u0);
                 set_pending(r, std::move(v));
             } break;
+            case OpKind::Derivative: {
+                use(op.a);
+                need(op.a);
+                auto p = new_pending(ZS_PR_BOX3, d.width, d.height, "derivative");
+                set_src(*p, 0, op.a);
+                for (int k = 0; k < 9; ++k) p->a.cons[k] = op.fparams[k];
+                set_pending(r, std::move(p));
+            } break;
             case OpKind::Blend: {
                 use(op.a);
                 use(op.b);

@@ -13,6 +13,7 @@
 //   INDEX     resize through a nearest index table                    gather
 //   BLEND     blend of `above` at an offset over `below`              (new op)
 //   RESAMPLE  one separable filter pass (FP64-normalised weights)      (new op)
+//   BOX3      3x3 stencil: the derivative operators                   box3.frag:12-53
 // Gathers whose source and destination formats agree and that carry no fused
 // program copy texel bytes verbatim (integer-exact).
 #include <atomic>
@@ -212,6 +213,29 @@ __global__ void __launch_bounds__(256) zs_raster_kernel(const __grid_constant__ 
                 float4 s = zs_load_px(s1, ax, ay);
                 zs_blend_px(r, s, a.blend_mode, a.straight);
             }
+        } break;
+        case ZS_PR_BOX3: {
+            // box3.frag:12-53: clamp-to-edge nearest taps (the default sampler); each row of
+            // the component-wise product is summed, then the three row sums; alpha 1.
+            float rows[3][3];
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                const int yy = zs_clampi(y + j - 1, 0, s0.height - 1);
+                float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+                for (int i = 0; i < 3; ++i) {
+                    const float w = a.cons[3 * j + i];
+                    const float4 v = zs_load_px(s0, zs_clampi(x + i - 1, 0, s0.width - 1), yy);
+                    acc.x = fmaf(w, v.x, acc.x);
+                    acc.y = fmaf(w, v.y, acc.y);
+                    acc.z = fmaf(w, v.z, acc.z);
+                }
+                rows[j][0] = acc.x;
+                rows[j][1] = acc.y;
+                rows[j][2] = acc.z;
+            }
+            r = make_float4(rows[0][0] + rows[1][0] + rows[2][0], rows[0][1] + rows[1][1] + rows[2][1],
+                            rows[0][2] + rows[1][2] + rows[2][2], 1.0f);
         } break;
         case ZS_PR_RESAMPLE_H: {
             int first = a.index_x[x], cnt = a.index_y[x];

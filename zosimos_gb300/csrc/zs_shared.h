@@ -83,7 +83,8 @@ enum ZsProducer : uint8_t {
     ZS_PR_RESAMPLE_H,   // horizontal filter pass over src0 rows
     ZS_PR_RESAMPLE_V,   // vertical filter pass over src0 columns
     ZS_PR_LAYERS,       // planner only: a layer stack, launched by k_layers.cu
-    ZS_PR_RESAMPLE_2D   // both separable passes in one tiled launch (k_resample.cu)
+    ZS_PR_RESAMPLE_2D,  // both separable passes in one tiled launch (k_resample.cu)
+    ZS_PR_BOX3          // 3x3 stencil of src0, weights in cons[0..8]   (box3.frag)
 };
 
 struct ZsSource {
@@ -107,7 +108,7 @@ struct ZsRasterArgs {
     int32_t rect[4];      // QUAD target rect / BLEND offset rect
     int32_t sel[4];       // QUAD selection rect in src1
     float aff[9];         // AFFINE inverse matrix (f32, applied with a fixed fmaf order)
-    float cons[24];       // BILINEAR params / SOLID colour / PALETTE channel weights (8)
+    float cons[24];       // BILINEAR params / SOLID colour / PALETTE channel weights (8) / BOX3 weights (9)
     const int32_t *index_x;   // INDEX producer / RESAMPLE first-tap table
     const int32_t *index_y;   // INDEX producer / RESAMPLE tap-count table
     const float *weights;     // RESAMPLE weights [dst][taps]
