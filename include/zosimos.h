@@ -191,6 +191,14 @@ int zs_cmd_resize_filtered(zs_cmd *cmd, uint32_t src, uint32_t width, uint32_t h
  * Scharr4, Scharr5 and Scharr5Tab fail in zs_compile with ZS_ERR_UNIMPLEMENTED as in the
  * reference.  direction: 0 Width, 1 Height. */
 int zs_cmd_derivative(zs_cmd *cmd, uint32_t src, uint32_t method, uint32_t direction, uint32_t *reg);
+/* CommandBuffer::distribution_normal2d (command.rs; shaders/distribution_normal2d.rs,
+ * distribution_normal2d.frag): an image of the normal density
+ * exp(-0.5 pos.(C+ pos)) / sqrt(pdet), pos = 2 (uv - 0.5) - mu at pixel centres, in all three
+ * colour channels, alpha 1.  params = [mu0, mu1, C+00, C+01, C+10, C+11, pdet].  The two
+ * constructors of DistributionNormal2d fill `params` as the reference does (f32). */
+int zs_cmd_distribution_normal2d(zs_cmd *cmd, const zs_descriptor *desc, const float params[7], uint32_t *reg);
+int zs_normal2d_with_diagonal(float var0, float var1, float params[7]);
+int zs_normal2d_with_direction(float x, float y, float params[7]);
 /* CommandBuffer::blend (command.rs:1509, UNIMPLEMENTED upstream, built here):
  * mode 0 Alpha/over, 1 multiply, 2 screen, 3 add; `above` placed at rect.x/rect.y. */
 int zs_cmd_blend(zs_cmd *cmd, uint32_t below, const zs_rect *rect, uint32_t above,

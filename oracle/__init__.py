@@ -263,6 +263,58 @@ def box3(src, m, f32=False):
     return out
 
 
+def normal2d_with_diagonal(var0: float, var1: float) -> np.ndarray:
+    """Parameters [mu0, mu1, inv00, inv01, inv10, inv11, pseudo_det] of a centred normal
+    distribution with diagonal covariance, in f32 as shaders/distribution_normal2d.rs:24-38."""
+    f = np.float32
+    pi = f(np.pi)
+    d0 = f(0) if var0 == 0 else f(1) / f(var0)
+    d1 = f(0) if var1 == 0 else f(1) / f(var1)
+    f0 = f(1) if var0 == 0 else f(2) * pi * f(var0)
+    f1 = f(1) if var1 == 0 else f(2) * pi * f(var1)
+    return np.array([0, 0, d0, 0, 0, d1, f0 * f1], np.float32)
+
+
+def normal2d_with_direction(x: float, y: float) -> np.ndarray:
+    """A 1-D normal distribution along `dir` (shaders/distribution_normal2d.rs:40-94): the
+    pseudo inverse dir^T dir / |dir|^4 by the reference's reformulated f32 expressions."""
+    f = np.float32
+    x, y = f(x), f(y)
+    length_sq = f(float(x) * float(x) + float(y) * float(y))
+
+    def symmetric(a, b):
+        hyp = f(np.hypot(a, b))
+        up = (f(1) / hyp) * (a / hyp)
+        low = a + b * (b / a)
+        return f(up / low)
+
+    def asymmetric(a, b):
+        a, b = min(a, b), max(a, b)
+        hyp = f(np.hypot(a, b))
+        inner = f(float(a) * float(a / b) + float(b))      # mul_add: one rounding
+        return f(((a / hyp) / inner) / hyp)
+
+    inv = [symmetric(x, x), asymmetric(x, y), asymmetric(y, x), symmetric(y, y)]
+    return np.array([0, 0, *inv, f(2) * f(np.pi) * length_sq], np.float32)
+
+
+def normal2d(width: int, height: int, params) -> np.ndarray:
+    """distribution_normal2d.frag: v = exp(-0.5 pos . (C^+ pos)) / sqrt(pseudo_det) at pixel
+    centres, pos = 2 (uv - 0.5) - mu; (v, v, v, 1), FP64."""
+    p = np.asarray(params, np.float64)
+    u = (np.arange(width) + 0.5) / width
+    v = (np.arange(height) + 0.5) / height
+    px = 2.0 * (u[None, :] - 0.5) - p[0]
+    py = 2.0 * (v[:, None] - 0.5) - p[1]
+    # GLSL mat2 columns are (inv00, inv01) and (inv10, inv11) of the uploaded row-major data.
+    q = px * (p[2] * px + p[4] * py) + py * (p[3] * px + p[5] * py)
+    val = np.exp(-0.5 * q) / np.sqrt(p[6])
+    out = np.empty((height, width, 4))
+    out[..., 0] = out[..., 1] = out[..., 2] = val
+    out[..., 3] = 1.0
+    return out
+
+
 def rgb_to_xyz(primaries="Bt709", whitepoint="D65") -> np.ndarray:
     out = np.zeros(9)
     lib().zo_rgb_to_xyz(ctypes.c_int32(PRIMARIES[primaries]), ctypes.c_int32(WHITEPOINT[whitepoint]), _p(out))

@@ -313,3 +313,32 @@ def test_derivative(background, goldens, method, mode):
     assert blockhash256(ours.reshape(512, 512, 4)) in goldens["derived_" + method]
     ours_h = P.ours_derivative(background, m, zs.Direction.Height, mode)
     assert maxdiff(ours_h, P.oracle_derivative(background, method, False)) <= LSB
+
+
+@pytest.mark.parametrize("case", ["normal2d", "normal1d", "u8"])
+def test_distribution_normal2d(goldens, case):
+    # tests/blend.rs:227-311.
+    import oracle as O
+    from imgutil import luma_alpha16_to_rgba8
+    params = zs.normal2d_with_diagonal(0.2, 0.2) if case == "normal2d" else zs.normal2d_with_direction(0.04998, 0.0501)
+    if case == "u8":
+        d = zs.Descriptor(400, 400, zs.Bits.UInt8, zs.Parts.Luma, zs.ColorKind.Rgb, zs.Primaries.Bt709,
+                          zs.Transfer.Srgb, zs.Whitepoint.D65)
+        f = O.Format(O.BITS["UInt8"], O.PARTS["Luma"], O.TRANSFER["Srgb"], False)
+    else:
+        d = P.luma_alpha16_desc(400, 400)
+        f = O.Format(O.BITS["UInt16x2"], O.PARTS["LumaA"], O.TRANSFER["Srgb"], False)
+    c = zs.CommandBuffer()
+    o, _ = c.output(c.distribution_normal2d(d, params))
+    ours = np.frombuffer(P.run(c, zs.Pool(), [], [o])[0], np.uint8).reshape(400, -1)
+    want = O.encode(f, O.normal2d(400, 400, params))
+    # within one code of the FP64 oracle (truncating quantisation of FP32 against FP64)
+    fl = O.Format(f.bits, f.parts, O.TRANSFER["Linear"], False)
+    got_c, want_c = O.decode(fl, ours, 400, 400), O.decode(fl, want, 400, 400)
+    assert np.abs(got_c - want_c).max() <= (1.0001 / 255 if case == "u8" else 1.0001 / 65535)
+    if case == "u8":
+        rgba = np.stack([ours, ours, ours, np.full_like(ours, 255)], -1)
+        h = blockhash256(rgba)
+        assert min(bin(int(h, 16) ^ int(a, 16)).count("1") for a in goldens["distribution_u8"]) <= 3
+    else:
+        assert blockhash256(luma_alpha16_to_rgba8(ours)) in goldens["distribution_" + case]

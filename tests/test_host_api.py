@@ -193,3 +193,12 @@ def test_derivative_plan_and_unimplemented_methods():
         with pytest.raises(ZosimosError) as e:
             Linker.from_included().compile(c)       # ... compiling it is NotYetImplemented
         assert e.value.code == 2
+
+
+def test_normal2d_parameters_follow_the_reference_constructors():
+    import oracle as O
+    assert (zs.normal2d_with_diagonal(0.2, 0.2) == O.normal2d_with_diagonal(0.2, 0.2)).all()
+    assert (zs.normal2d_with_direction(0.04998, 0.0501) == O.normal2d_with_direction(0.04998, 0.0501)).all()
+    c = CommandBuffer()
+    c.output(c.distribution_normal2d(Descriptor.srgb_rgba8(32, 16), zs.normal2d_with_diagonal(0.2, 0.2)))
+    assert Linker.from_included().compile(c).lower_to().kernel_count() == 1

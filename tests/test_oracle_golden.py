@@ -139,3 +139,23 @@ def test_derivative_goldens(background, goldens, method):
     lin = O.decode(O.SRGB_RGBA8, background.reshape(512, 2048), 512, 512)
     out = O.encode(O.SRGB_RGBA8, O.box3(lin, O.derivative_matrix(method))).reshape(512, 512, 4)
     assert blockhash256(out) in goldens["derived_" + method]
+
+
+LA16_SRGB = O.Format(O.BITS["UInt16x2"], O.PARTS["LumaA"], O.TRANSFER["Srgb"], False)
+L8_SRGB = O.Format(O.BITS["UInt8"], O.PARTS["Luma"], O.TRANSFER["Srgb"], False)
+
+
+def _hamming(h, accepted):
+    return min(bin(int(h, 16) ^ int(a, 16)).count("1") for a in accepted)
+
+
+def test_distribution_normal_goldens(goldens):
+    # tests/blend.rs:227-311: 400 x 400 LumaA16 / Luma8 images of the normal density.
+    img = O.normal2d(400, 400, O.normal2d_with_diagonal(0.2, 0.2))
+    assert blockhash256(luma_alpha16_to_rgba8(O.encode(LA16_SRGB, img))) in goldens["distribution_normal2d"]
+    img = O.normal2d(400, 400, O.normal2d_with_direction(0.04998, 0.0501))
+    assert blockhash256(luma_alpha16_to_rgba8(O.encode(LA16_SRGB, img))) in goldens["distribution_normal1d"]
+    l8 = O.encode(L8_SRGB, img).reshape(400, 400)
+    rgba = np.stack([l8, l8, l8, np.full_like(l8, 255)], -1)
+    # The two accepted hashes of the reference differ from each other by more than this.
+    assert _hamming(blockhash256(rgba), goldens["distribution_u8"]) <= 3

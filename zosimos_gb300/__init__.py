@@ -160,6 +160,9 @@ def _lib():
             "zs_cmd_resize_filtered": ([P, U32, U32, U32, U32, pU32], I32),
             "zs_cmd_blend": ([P, U32, pR, U32, U32, pU32], I32), "zs_cmd_color_matrix": ([P, U32, P, pU32], I32),
             "zs_cmd_derivative": ([P, U32, U32, U32, pU32], I32),
+            "zs_cmd_distribution_normal2d": ([P, pD, P, pU32], I32),
+            "zs_normal2d_with_diagonal": ([ctypes.c_float, ctypes.c_float, P], I32),
+            "zs_normal2d_with_direction": ([ctypes.c_float, ctypes.c_float, P], I32),
             "zs_cmd_output": ([P, U32, pU32, pD], I32), "zs_cmd_describe": ([P, U32, pD], I32),
             "zs_compile": ([P, ctypes.POINTER(P)], I32), "zs_program_free": ([P], None),
             "zs_lower": ([P, ctypes.POINTER(_CCaps), ctypes.POINTER(P)], I32), "zs_executable_free": ([P], None),
@@ -201,6 +204,20 @@ def selftest_wait_timeout(device: int = 0, limit_us: int = 2000) -> None:
     """Run a kernel whose bounded wait nothing completes (it gives up after `limit_us` and
     sets bit 0 of the device status word, as a real timeout would)."""
     _check(_lib().zs_selftest_wait_timeout(device, limit_us))
+
+
+def normal2d_with_diagonal(var0: float, var1: float) -> np.ndarray:
+    """DistributionNormal2d::with_diagonal: parameters of a centred normal density."""
+    p = np.zeros(7, np.float32)
+    _check(_lib().zs_normal2d_with_diagonal(var0, var1, p.ctypes.data))
+    return p
+
+
+def normal2d_with_direction(x: float, y: float) -> np.ndarray:
+    """DistributionNormal2d::with_direction: a 1-D normal density along (x, y)."""
+    p = np.zeros(7, np.float32)
+    _check(_lib().zs_normal2d_with_direction(x, y, p.ctypes.data))
+    return p
 
 
 def device_status(device: int = 0) -> int:
@@ -488,6 +505,11 @@ class CommandBuffer:
 
     def resize_filtered(self, src: int, size, filt: int) -> int:
         return self._reg(_lib().zs_cmd_resize_filtered, src, size[0], size[1], filt)
+
+    def distribution_normal2d(self, desc: Descriptor, params) -> int:
+        """params: the 7 floats of normal2d_with_diagonal / normal2d_with_direction."""
+        p = np.ascontiguousarray(np.asarray(params, dtype=np.float32).reshape(7))
+        return self._reg(_lib().zs_cmd_distribution_normal2d, ctypes.byref(desc._c()), p.ctypes.data)
 
     def derivative(self, src: int, method: int, direction: int = Direction.Width) -> int:
         return self._reg(_lib().zs_cmd_derivative, src, method, direction)

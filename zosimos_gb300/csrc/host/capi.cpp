@@ -24,6 +24,9 @@ uint32_t cmd_affine(Command &c, uint32_t below, const float m[9], uint32_t sampl
 uint32_t cmd_resize(Command &c, uint32_t src, uint32_t w, uint32_t h, bool filtered, uint32_t filter);
 uint32_t cmd_blend(Command &c, uint32_t below, const zs_rect &rect, uint32_t above, uint32_t mode);
 uint32_t cmd_derivative(Command &c, uint32_t src, uint32_t method, uint32_t direction);
+uint32_t cmd_normal2d(Command &c, const Desc &d, const float params[7]);
+void normal2d_with_diagonal(float var0, float var1, float p[7]);
+void normal2d_with_direction(float x, float y, float p[7]);
 uint32_t cmd_output(Command &c, uint32_t src, Desc *outformat);
 int batch_thumbnails(Executable *chain, const void *const *images, const uint32_t *widths, const uint32_t *heights,
                      uint32_t n, uint32_t canvas, void *out, cudaStream_t stream);
@@ -326,6 +329,15 @@ int zs_cmd_resize_filtered(zs_cmd *cmd, uint32_t src, uint32_t width, uint32_t h
                            uint32_t *reg) {
     CMD_BODY(cmd_resize(cmd->c, src, width, height, true, filter));
 }
+int zs_cmd_distribution_normal2d(zs_cmd *cmd, const zs_descriptor *desc, const float params[7], uint32_t *reg) {
+    return guarded([&] { NEED(cmd); NEED(desc); NEED(params); NEED(reg); *reg = cmd_normal2d(cmd->c, *desc, params); });
+}
+int zs_normal2d_with_diagonal(float var0, float var1, float params[7]) {
+    return guarded([&] { NEED(params); normal2d_with_diagonal(var0, var1, params); });
+}
+int zs_normal2d_with_direction(float x, float y, float params[7]) {
+    return guarded([&] { NEED(params); normal2d_with_direction(x, y, params); });
+}
 int zs_cmd_derivative(zs_cmd *cmd, uint32_t src, uint32_t method, uint32_t direction, uint32_t *reg) {
     return guarded([&] { NEED(cmd); NEED(reg); *reg = cmd_derivative(cmd->c, src, method, direction); });
 }
@@ -361,6 +373,7 @@ int zs_compile(const zs_cmd *cmd, zs_program **out) {
                 p.uses[op.a]++;
                 break;
             case OpKind::Bilinear:
+            case OpKind::Normal2d:
             case OpKind::Solid: break;
             case OpKind::Derivative:
                 // DerivativeMethod::to_shader: Roberts, Scharr4, Scharr5, Scharr5Tab are

@@ -271,6 +271,49 @@ uint32_t cmd_affine(Command &c, uint32_t below, const float m[9], uint32_t sampl
     return c.push(op);
 }
 
+// CommandBuffer::distribution_normal2d: a generator with the descriptor given.
+uint32_t cmd_normal2d(Command &c, const Desc &d, const float params[7]) {
+    if (!is_consistent(d)) fail(ZS_ERR_TYPE, "inconsistent descriptor: " + describe(d));
+    Op op{OpKind::Normal2d};
+    op.desc = d;
+    op.desc.row_stride = 0;
+    for (int k = 0; k < 7; ++k) op.fparams[k] = params[k];
+    return c.push(op);
+}
+
+// DistributionNormal2d::with_diagonal (shaders/distribution_normal2d.rs:24-38), in f32.
+void normal2d_with_diagonal(float var0, float var1, float p[7]) {
+    const float pi = 3.14159265358979323846f;
+    const float d0 = var0 == 0.f ? 0.f : 1.f / var0, d1 = var1 == 0.f ? 0.f : 1.f / var1;
+    const float f0 = var0 == 0.f ? 1.f : 2.f * pi * var0, f1 = var1 == 0.f ? 1.f : 2.f * pi * var1;
+    const float out[7] = {0.f, 0.f, d0, 0.f, 0.f, d1, f0 * f1};
+    for (int k = 0; k < 7; ++k) p[k] = out[k];
+}
+
+// DistributionNormal2d::with_direction (shaders/distribution_normal2d.rs:40-94): the pseudo
+// inverse dir^T dir / |dir|^4 through the reference's reformulated f32 expressions.
+void normal2d_with_direction(float x, float y, float p[7]) {
+    const double xt = x, yt = y;
+    const float length_sq = (float)(xt * xt + yt * yt);
+    if (!std::isfinite(length_sq)) fail(ZS_ERR_INVALID_ARG, "direction length is not finite");
+    auto symmetric = [](float a, float b) {
+        const float hyp = std::hypot(a, b);
+        const float up = (1.0f / hyp) * (a / hyp);
+        const float low = a + b * (b / a);
+        return up / low;
+    };
+    auto asymmetric = [](float a, float b) {
+        const float lo = std::min(a, b), hi = std::max(a, b);
+        const float hyp = std::hypot(lo, hi);
+        const float inner = std::fma(lo, lo / hi, hi);
+        return ((lo / hyp) / inner) / hyp;
+    };
+    const float pi = 3.14159265358979323846f;
+    const float out[7] = {0.f, 0.f, symmetric(x, x), asymmetric(x, y), asymmetric(y, x), symmetric(y, y),
+                          2.0f * pi * length_sq};
+    for (int k = 0; k < 7; ++k) p[k] = out[k];
+}
+
 // CommandBuffer::derivative (command.rs:1493-1507) with the operator of
 // DerivativeMethod::to_shader (command.rs:3343-3409): the f32 outer product of a smoothing
 // and the derivative vector [0.5, 0, -0.5], transposed along the height.

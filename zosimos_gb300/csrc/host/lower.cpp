@@ -742,6 +742,11 @@ struct Planner {
                 add_weights(*v, sd.height, d.height, op.u0);
                 set_pending(r, std::move(v));
             } break;
+            case OpKind::Normal2d: {
+                auto p = new_pending(ZS_PR_NORMAL2D, d.width, d.height, "distribution normal2d");
+                for (int k = 0; k < 7; ++k) p->a.cons[k] = op.fparams[k];
+                set_pending(r, std::move(p));
+            } break;
             case OpKind::Derivative: {
                 use(op.a);
                 need(op.a);

@@ -14,6 +14,7 @@
 //   BLEND     blend of `above` at an offset over `below`              (new op)
 //   RESAMPLE  one separable filter pass (FP64-normalised weights)      (new op)
 //   BOX3      3x3 stencil: the derivative operators                   box3.frag:12-53
+//   NORMAL2D  normal density generator                                distribution_normal2d.frag
 // Gathers whose source and destination formats agree and that carry no fused
 // program copy texel bytes verbatim (integer-exact).
 #include <atomic>
@@ -213,6 +214,16 @@ __global__ void __launch_bounds__(256) zs_raster_kernel(const __grid_constant__ 
                 float4 s = zs_load_px(s1, ax, ay);
                 zs_blend_px(r, s, a.blend_mode, a.straight);
             }
+        } break;
+        case ZS_PR_NORMAL2D: {
+            // distribution_normal2d.frag: pos = 2 (uv - 0.5) - mu at the pixel centre; the
+            // GLSL mat2 columns are (C+00, C+01) and (C+10, C+11).
+            const float *c = a.cons;
+            const float u = __fdiv_rn((float)x + 0.5f, (float)a.width), v = __fdiv_rn((float)y + 0.5f, (float)a.height);
+            const float px = 2.0f * (u - 0.5f) - c[0], py = 2.0f * (v - 0.5f) - c[1];
+            const float q = px * (c[2] * px + c[4] * py) + py * (c[3] * px + c[5] * py);
+            const float val = expf(-0.5f * q) / sqrtf(c[6]);
+            r = make_float4(val, val, val, 1.0f);
         } break;
         case ZS_PR_BOX3: {
             // box3.frag:12-53: clamp-to-edge nearest taps (the default sampler); each row of
