@@ -1,8 +1,10 @@
 """Build libzosimos_gb300.so in-tree with nvcc for sm_103a (no cmake, no torch).
 
-The device code is one translation unit (csrc/zs_device_all.cu); the host side
-(csrc/host/*.cpp) is plain C++17 compiled by nvcc's host compiler.  Objects are
-compiled in parallel and linked against the CUDA runtime.
+Each kernel file (csrc/*.cu) is its own translation unit without relocatable device
+code: the few device variables they share (the sRGB tables, the status word) are
+per-file copies that csrc/zs_tables.cu fills and reads through per-file host hooks.
+The host side (csrc/host/*.cpp) is plain C++17 compiled by nvcc's host compiler.
+Objects are compiled in parallel and linked against the CUDA runtime.
 """
 from __future__ import annotations
 
@@ -27,7 +29,7 @@ def _nvcc() -> str:
 
 
 def _sources():
-    cu = [os.path.join(CSRC, "zs_device_all.cu")]
+    cu = sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cu"))
     host = sorted(os.path.join(CSRC, "host", f) for f in os.listdir(os.path.join(CSRC, "host")) if f.endswith(".cpp"))
     return cu, host
 
@@ -68,7 +70,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
             raise RuntimeError("compile failed: " + " ".join(cmd) + "\n" + r.stdout + r.stderr)
         return r.stdout + r.stderr
 
-    with cf.ThreadPoolExecutor(max_workers=min(8, os.cpu_count() or 4)) as ex:
+    # The slowest object (k_raster.cu) goes first so that it overlaps the rest.
+    jobs.sort(key=lambda c: not c[-3].endswith("k_raster.cu"))
+    with cf.ThreadPoolExecutor(max_workers=min(len(jobs), max(4, os.cpu_count() or 4))) as ex:
         logs = list(ex.map(run, jobs))
     if verbose:
         for log in logs:

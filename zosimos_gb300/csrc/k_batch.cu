@@ -13,9 +13,11 @@
 // warps without atomics or barriers.  Each lane computes its output pixel from its source
 // window: the box weights are separable, the source texels of a window row go through
 // the colour chain two at a time in FP32x2 registers.
+#include <cstring>
 #include <vector>
 
 #include "host/zs_host.hpp"
+#include "zs_chain.cuh"
 #include "zs_device.cuh"
 #include "zs_kernels.h"
 
@@ -273,3 +275,5 @@ int batch_thumbnails(Executable *chain, const void *const *images, const uint32_
 }
 
 }  // namespace zs
+
+ZS_TU_HOOKS(batch)

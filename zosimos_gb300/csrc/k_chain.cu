@@ -19,21 +19,19 @@
 //    the matrix coefficients read as 64-bit constant operands;
 //  * cube roots as ex2(lg2(x)/3) on the MUFU pipe (the sign fix-up is dropped when the
 //    host proves M_a keeps [0,1]^3 non-negative);
-//  * clamps as saturating adds on the FMA pipe;
+//  * clamps folded into the last FMA of each matrix row (fma.sat on the FMA pipe), the
+//    encode shift added to a pixel pair by one packed add;
+//  * the first loads issued before the shared tables are staged;
 //  * exact round-to-nearest sRGB encode from a bucketed threshold table replicated 4x
 //    across lanes (entry + float bits carries the code into byte 3), packed with PRMT;
 //  * alpha bytes passed through (unorm8 alpha decode + encode is the identity).
 #include <atomic>
 
+#include "zs_chain.cuh"
 #include "zs_device.cuh"
 #include "zs_kernels.h"
 
-namespace zs {
-extern std::atomic<uint64_t> g_kernel_launches;
-}
-
 #define ZS_CHAIN_THREADS 512
-#define ZS_ENC_REP 4
 
 // Decode rows are 256 bytes apart so that the byte offset of (code, lane) is
 // (code << 8) | (lane << 2): one PRMT builds it from the packed texel.
@@ -41,69 +39,6 @@ struct ZsChainSmem {
     float lut[256 * 64];                         // [code][lane], lanes 32..63 unused
     uint32_t enc[ZS_ENCS_ENTRIES * ZS_ENC_REP];   // [bucket][lane & 3], shifted domain
 };
-
-__device__ __forceinline__ float zs_ex2(float x) {
-    float y;
-    asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-__device__ __forceinline__ float zs_lg2(float x) {
-    float y;
-    asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-    return y;
-}
-
-template <bool NONNEG>
-__device__ __forceinline__ float zs_cbrt1(float x) {
-    if (NONNEG) return zs_ex2(zs_lg2(x) * (1.0f / 3.0f));
-    return copysignf(zs_ex2(zs_lg2(fabsf(x)) * (1.0f / 3.0f)), x);
-}
-
-// saturate(x) as a saturating add on the FMA pipe (the ALU pipe is the busier one).
-__device__ __forceinline__ float zs_sat(float x) {
-    float y;
-    asm("add.rn.sat.f32 %0, %1, 0f00000000;" : "=f"(y) : "f"(x));
-    return y;
-}
-
-__device__ __forceinline__ float2 zs_sat2(float2 v) { return make_float2(zs_sat(v.x), zs_sat(v.y)); }
-
-// rgb' = M rgb on a pixel pair; SAT saturates the results to [0, 1].
-template <bool SAT>
-__device__ __forceinline__ void zs_m3x2(const float (*m)[2], float2 &r, float2 &g, float2 &b) {
-    const float2 *c = reinterpret_cast<const float2 *>(m);
-    const float2 x = r, y = g, z = b;
-    r = __ffma2_rn(c[0], x, __ffma2_rn(c[1], y, __fmul2_rn(c[2], z)));
-    g = __ffma2_rn(c[3], x, __ffma2_rn(c[4], y, __fmul2_rn(c[5], z)));
-    b = __ffma2_rn(c[6], x, __ffma2_rn(c[7], y, __fmul2_rn(c[8], z)));
-    if (SAT) {
-        r = zs_sat2(r);
-        g = zs_sat2(g);
-        b = zs_sat2(b);
-    }
-}
-
-// x in [0, 1] -> table entry + bits of x + 2^-12; the sRGB8 code is byte 3 of the
-// result.  The shift keeps the argument inside the table without an integer clamp.
-__device__ __forceinline__ uint32_t zs_enc_q(const uint32_t *enc_lane, float x) {
-    const uint32_t b = __float_as_uint(x + (1.0f / 4096.0f));
-    return enc_lane[((b >> 16) - ZS_ENCS_BASE) * ZS_ENC_REP] + b;
-}
-
-// Decoded value of byte K of texel w for this lane: (code << 8) | (lane << 2) is the
-// byte offset of the lane-replicated table entry, built by one byte permute.
-template <int K>
-__device__ __forceinline__ float zs_dec(const unsigned char *lut, uint32_t w, uint32_t lane4) {
-    const uint32_t off = __byte_perm(w, lane4, 0x5504u | (K << 4));
-    return *reinterpret_cast<const float *>(lut + off);
-}
-
-__device__ __forceinline__ void zs_cbrt2(float2 &v) {
-    // NONNEG: both arguments are >= 0 (the MUFU log of 0 is -inf, its exp2 is 0).
-    float2 l = make_float2(zs_lg2(v.x), zs_lg2(v.y));
-    l = __fmul2_rn(l, make_float2(1.0f / 3.0f, 1.0f / 3.0f));
-    v = make_float2(zs_ex2(l.x), zs_ex2(l.y));
-}
 
 template <bool CBRT, bool CUBE, bool CLAMP, bool NONNEG>
 __device__ __forceinline__ void zs_chain_pair(uint32_t &wp, uint32_t &wq, const unsigned char *lut,
@@ -132,6 +67,10 @@ __device__ __forceinline__ void zs_chain_pair(uint32_t &wp, uint32_t &wq, const 
     }
     zs_m3x2<CLAMP>(a.m2[2], r, g, b);
     zs_m3x2<true>(a.m2[3], r, g, b);
+    const float2 sh = make_float2(1.0f / 4096.0f, 1.0f / 4096.0f);
+    r = __fadd2_rn(r, sh);
+    g = __fadd2_rn(g, sh);
+    b = __fadd2_rn(b, sh);
     const uint32_t rp = zs_enc_q(enc_lane, r.x), gp = zs_enc_q(enc_lane, g.x), bp = zs_enc_q(enc_lane, b.x);
     const uint32_t rq = zs_enc_q(enc_lane, r.y), gq = zs_enc_q(enc_lane, g.y), bq = zs_enc_q(enc_lane, b.y);
     wp = __byte_perm(__byte_perm(rp, gp, 0x0073), __byte_perm(bp, wp, 0x0073), 0x5410);
@@ -142,24 +81,38 @@ template <bool CBRT, bool CUBE, bool CLAMP, bool NONNEG>
 __global__ void __launch_bounds__(ZS_CHAIN_THREADS, 2) zs_chain_srgb8_kernel(const __grid_constant__ ZsChainArgs a) {
     extern __shared__ __align__(16) unsigned char zs_smem_raw[];
     ZsChainSmem &sm = *reinterpret_cast<ZsChainSmem *>(zs_smem_raw);
-    for (int i = threadIdx.x; i < 256 * 32; i += blockDim.x) sm.lut[(i >> 5) * 64 + (i & 31)] = zs_srgb_decode_lut[i >> 5];
-    for (int i = threadIdx.x; i < ZS_ENCS_ENTRIES * ZS_ENC_REP; i += blockDim.x)
-        sm.enc[i] = zs_srgb_encode_tab_shifted[i / ZS_ENC_REP];
+    const uint4 *in = reinterpret_cast<const uint4 *>(a.src);
+    uint4 *out = reinterpret_cast<uint4 *>(a.dst);
+    const int64_t nvec = a.npx >> 2;
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    // The first two vectors are requested before the tables are staged, so that their
+    // DRAM latency overlaps the table fill.
+    const bool piped = v + stride < nvec;
+    uint4 w0 = make_uint4(0, 0, 0, 0), w1 = w0;
+    if (piped) {
+        w0 = __ldcs(in + v);
+        w1 = __ldcs(in + v + stride);
+    }
+    // Tables: one 16-byte store writes four lane copies of an entry.
+    for (int i = threadIdx.x; i < 256 * 8; i += blockDim.x) {
+        const float d = zs_srgb_decode_lut[i >> 3];
+        reinterpret_cast<float4 *>(sm.lut)[(i >> 3) * 16 + (i & 7)] = make_float4(d, d, d, d);
+    }
+    static_assert(ZS_ENC_REP == 4, "one uint4 per encode bucket");
+    for (int i = threadIdx.x; i < ZS_ENCS_ENTRIES; i += blockDim.x) {
+        const uint32_t e = zs_srgb_encode_tab_shifted[i];
+        reinterpret_cast<uint4 *>(sm.enc)[i] = make_uint4(e, e, e, e);
+    }
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const unsigned char *lut = reinterpret_cast<const unsigned char *>(sm.lut);
     const uint32_t lane4 = (uint32_t)lane << 2;
     const uint32_t *enc_lane = sm.enc + (lane & (ZS_ENC_REP - 1));
 
-    const uint4 *in = reinterpret_cast<const uint4 *>(a.src);
-    uint4 *out = reinterpret_cast<uint4 *>(a.dst);
-    const int64_t nvec = a.npx >> 2;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (v + stride < nvec) {
+    if (piped) {
         // Software pipeline: the next two vectors are in flight while the current two are
         // computed, so each thread keeps 32 bytes of reads outstanding at all times.
-        uint4 w0 = __ldcs(in + v), w1 = __ldcs(in + v + stride);
         for (;;) {
             const int64_t nx = v + 2 * stride;
             const bool more = nx + stride < nvec;
@@ -245,3 +198,5 @@ cudaError_t launch_chain(const ZsChainArgs &args, uint8_t src_fast, uint8_t dst_
 }
 
 }  // namespace zs
+
+ZS_TU_HOOKS(chain)

@@ -154,3 +154,5 @@ cudaError_t launch_layers(const ZsLayersArgs &args, int sm_count, cudaStream_t s
 }
 
 }  // namespace zs
+
+ZS_TU_HOOKS(layers)

@@ -244,3 +244,5 @@ extern "C" int zs_resample_rgba16f_noalloc(const void *src, uint32_t src_width, 
     }
     return ZS_OK;
 }
+
+ZS_TU_HOOKS(noalloc)

@@ -28,39 +28,6 @@ uint64_t kernel_launch_count() { return g_kernel_launches.load(); }
 void add_kernel_launches(uint64_t n) { g_kernel_launches.fetch_add(n); }
 }  // namespace zs
 
-__device__ __forceinline__ int zs_quad_src(int p, int t0, int t1, int s0, int s1) {
-    // floor(s0 + (p - t0 + 0.5) * (s1 - s0) / (t1 - t0)) in exact integer arithmetic.
-    long long num = (2LL * (p - t0) + 1) * (long long)(s1 - s0);
-    return s0 + (int)(num / (2LL * (t1 - t0)));
-}
-
-__device__ __forceinline__ void zs_affine_map(const float *inv, int x, int y, float &qx, float &qy) {
-    float cx = (float)x + 0.5f, cy = (float)y + 0.5f;
-    float X = fmaf(inv[0], cx, fmaf(inv[1], cy, inv[2]));
-    float Y = fmaf(inv[3], cx, fmaf(inv[4], cy, inv[5]));
-    float Z = fmaf(inv[6], cx, fmaf(inv[7], cy, inv[8]));
-    if (Z != 1.0f) { X = __fdiv_rn(X, Z); Y = __fdiv_rn(Y, Z); }
-    qx = X;
-    qy = Y;
-}
-
-// Pixel of work item i in 32 x 8 tiles of 256 items: warp w of the tile covers columns
-// 8 (w % 4) .. +8 and rows 4 (w / 4) .. +4, lane l column l % 8 and row l / 8.
-__device__ __forceinline__ void zs_tile_pixel(int64_t i, int tiles_x, int &x, int &y) {
-    const int64_t tile = i >> 8;
-    const int t = (int)(i & 255), w = t >> 5, l = t & 31;
-    const int ty = (int)(tile / tiles_x), tx = (int)(tile - (int64_t)ty * tiles_x);
-    x = (tx << 5) + ((w & 3) << 3) + (l & 7);
-    y = (ty << 3) + ((w >> 2) << 2) + (l >> 3);
-}
-
-__device__ __forceinline__ int zs_clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
-
-__device__ __forceinline__ float4 zs_lerp4(float4 a, float4 b, float t) {
-    return make_float4(a.x + (b.x - a.x) * t, a.y + (b.y - a.y) * t, a.z + (b.z - a.z) * t,
-                       a.w + (b.w - a.w) * t);
-}
-
 // The gathered image of an AFFINE launch at (x, y): a stored texel, or (virt1) its
 // pixel-aligned producer and program evaluated here.
 __device__ __forceinline__ float4 zs_src1_px(const ZsRasterArgs &a, int x, int y) {
@@ -365,3 +332,5 @@ cudaError_t launch_raster(const ZsRasterArgs &args, int sm_count, cudaStream_t s
 }
 
 }  // namespace zs
+
+ZS_TU_HOOKS(raster)

@@ -339,3 +339,5 @@ cudaError_t launch_resample2d(const ZsRasterArgs &args, int sm_count, cudaStream
 }
 
 }  // namespace zs
+
+ZS_TU_HOOKS(resample)

@@ -387,3 +387,5 @@ cudaError_t launch_resample_tc(const ZsRasterArgs &a, int sm_count, cudaStream_t
 }
 
 }  // namespace zs
+
+ZS_TU_HOOKS(resample_tc)

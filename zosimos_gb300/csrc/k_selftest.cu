@@ -35,3 +35,5 @@ cudaError_t wait_selftest(int device, uint32_t limit_us) {
 }
 
 }  // namespace zs
+
+ZS_TU_HOOKS(selftest)

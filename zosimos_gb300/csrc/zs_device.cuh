@@ -15,13 +15,46 @@
 
 // sRGB8 -> linear f32 (correctly rounded from FP64) and the bucketed rounding
 // thresholds of linear f32 -> sRGB8 (built by zs_tables.cu, uploaded once per
-// device).  All device code is one translation unit (zs_device_all.cu).
-__device__ float zs_srgb_decode_lut[256];
-__device__ uint32_t zs_srgb_encode_tab[ZS_ENC_ENTRIES];
-__device__ uint32_t zs_srgb_encode_tab_shifted[ZS_ENCS_ENTRIES];
+// device).  Each kernel file is its own translation unit (compiled in parallel, no
+// relocatable device code), so every one holds its own copy of these variables;
+// ZS_TU_HOOKS at the end of each file exports the host functions that fill its tables
+// and read its status word, and zs_tables.cu calls them all.
+static __device__ float zs_srgb_decode_lut[256];
+static __device__ uint32_t zs_srgb_encode_tab[ZS_ENC_ENTRIES];
+static __device__ uint32_t zs_srgb_encode_tab_shifted[ZS_ENCS_ENTRIES];
 // Sticky error bits set by kernels whose bounded waits gave up (ZS_DEVSTAT_*); the host
 // reads and clears them after synchronising.
-__device__ unsigned int zs_device_status_word;
+static __device__ unsigned int zs_device_status_word;
+
+// The kernel files, one translation unit each (ZS_TU_HOOKS(name) in every one).
+#define ZS_DEVICE_TUS(X) X(raster) X(resample) X(resample_tc) X(chain) X(layers) X(batch) X(noalloc) X(selftest)
+
+#define ZS_TU_DECLARE_HOOKS(NAME)                                                                   \
+    cudaError_t tu_upload_tables_##NAME(const float *dec, const uint32_t *enc, const uint32_t *encs); \
+    cudaError_t tu_device_status_##NAME(unsigned int *flags, bool clear);
+
+// Host functions of this translation unit: upload the sRGB tables into its copies, and
+// read (and optionally clear) its status word.  The current device must be selected.
+#define ZS_TU_HOOKS(NAME)                                                                            \
+    namespace zs {                                                                                   \
+    cudaError_t tu_upload_tables_##NAME(const float *dec, const uint32_t *enc, const uint32_t *encs) { \
+        cudaError_t e = cudaMemcpyToSymbol(zs_srgb_decode_lut, dec, sizeof(zs_srgb_decode_lut));     \
+        if (e == cudaSuccess) e = cudaMemcpyToSymbol(zs_srgb_encode_tab, enc, sizeof(zs_srgb_encode_tab)); \
+        if (e == cudaSuccess)                                                                        \
+            e = cudaMemcpyToSymbol(zs_srgb_encode_tab_shifted, encs, sizeof(zs_srgb_encode_tab_shifted)); \
+        return e;                                                                                    \
+    }                                                                                                \
+    cudaError_t tu_device_status_##NAME(unsigned int *flags, bool clear) {                          \
+        unsigned int v = 0;                                                                          \
+        cudaError_t e = cudaMemcpyFromSymbol(&v, zs_device_status_word, sizeof(v));                  \
+        if (e == cudaSuccess && clear && v) {                                                        \
+            const unsigned int zero = 0;                                                             \
+            e = cudaMemcpyToSymbol(zs_device_status_word, &zero, sizeof(zero));                      \
+        }                                                                                            \
+        *flags = v;                                                                                  \
+        return e;                                                                                    \
+    }                                                                                                \
+    }
 
 // ---------------------------------------------------------------- transfer functions
 
@@ -464,4 +497,39 @@ __device__ inline void zs_run_program(const ZsPixelProgram &P, const ZsFormat *f
         default: break;
         }
     }
+}
+
+// ---------------------------------------------------------------- geometry (raster and layer kernels)
+
+__device__ __forceinline__ int zs_quad_src(int p, int t0, int t1, int s0, int s1) {
+    // floor(s0 + (p - t0 + 0.5) * (s1 - s0) / (t1 - t0)) in exact integer arithmetic.
+    long long num = (2LL * (p - t0) + 1) * (long long)(s1 - s0);
+    return s0 + (int)(num / (2LL * (t1 - t0)));
+}
+
+__device__ __forceinline__ void zs_affine_map(const float *inv, int x, int y, float &qx, float &qy) {
+    float cx = (float)x + 0.5f, cy = (float)y + 0.5f;
+    float X = fmaf(inv[0], cx, fmaf(inv[1], cy, inv[2]));
+    float Y = fmaf(inv[3], cx, fmaf(inv[4], cy, inv[5]));
+    float Z = fmaf(inv[6], cx, fmaf(inv[7], cy, inv[8]));
+    if (Z != 1.0f) { X = __fdiv_rn(X, Z); Y = __fdiv_rn(Y, Z); }
+    qx = X;
+    qy = Y;
+}
+
+// Pixel of work item i in 32 x 8 tiles of 256 items: warp w of the tile covers columns
+// 8 (w % 4) .. +8 and rows 4 (w / 4) .. +4, lane l column l % 8 and row l / 8.
+__device__ __forceinline__ void zs_tile_pixel(int64_t i, int tiles_x, int &x, int &y) {
+    const int64_t tile = i >> 8;
+    const int t = (int)(i & 255), w = t >> 5, l = t & 31;
+    const int ty = (int)(tile / tiles_x), tx = (int)(tile - (int64_t)ty * tiles_x);
+    x = (tx << 5) + ((w & 3) << 3) + (l & 7);
+    y = (ty << 3) + ((w >> 2) << 2) + (l >> 3);
+}
+
+__device__ __forceinline__ int zs_clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
+
+__device__ __forceinline__ float4 zs_lerp4(float4 a, float4 b, float t) {
+    return make_float4(a.x + (b.x - a.x) * t, a.y + (b.y - a.y) * t, a.z + (b.z - a.z) * t,
+                       a.w + (b.w - a.w) * t);
 }

@@ -3,9 +3,14 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
 #include "zs_shared.h"
 
 namespace zs {
+
+// Kernel launches issued since process start (defined in k_raster.cu).
+extern std::atomic<uint64_t> g_kernel_launches;
 
 // Exact sRGB8 tables (zs_tables.cu).
 void build_srgb_tables(float *decode, uint32_t *encode, uint32_t *encode_shifted);

@@ -23,6 +23,8 @@
 
 namespace zs {
 
+ZS_DEVICE_TUS(ZS_TU_DECLARE_HOOKS)
+
 static double eotf_srgb(double v) {
     if (v < -0.04045) return -std::pow((-v + 0.055) / 1.055, 2.4);
     if (v <= 0.04045) return v / 12.92;
@@ -83,9 +85,10 @@ cudaError_t init_device_tables(int device) {
     cudaError_t e = cudaGetDevice(&prev);
     if (e != cudaSuccess) return e;
     if (prev != device && (e = cudaSetDevice(device)) != cudaSuccess) return e;
-    e = cudaMemcpyToSymbol(zs_srgb_decode_lut, dec, sizeof(dec));
-    if (e == cudaSuccess) e = cudaMemcpyToSymbol(zs_srgb_encode_tab, enc, sizeof(enc));
-    if (e == cudaSuccess) e = cudaMemcpyToSymbol(zs_srgb_encode_tab_shifted, encs, sizeof(encs));
+#define ZS_UPLOAD(NAME) \
+    if (e == cudaSuccess) e = tu_upload_tables_##NAME(dec, enc, encs);
+    ZS_DEVICE_TUS(ZS_UPLOAD)
+#undef ZS_UPLOAD
     if (prev != device) cudaSetDevice(prev);
     if (e == cudaSuccess) g_tables_ready[device] = 1;
     return e;
@@ -96,12 +99,16 @@ cudaError_t read_device_status(int device, uint32_t *flags, bool clear) {
     cudaError_t e = cudaGetDevice(&prev);
     if (e != cudaSuccess) return e;
     if (prev != device && (e = cudaSetDevice(device)) != cudaSuccess) return e;
+    // The status bits of every kernel file, ORed.
     unsigned int v = 0;
-    e = cudaMemcpyFromSymbol(&v, zs_device_status_word, sizeof(v));
-    if (e == cudaSuccess && clear && v) {
-        const unsigned int zero = 0;
-        e = cudaMemcpyToSymbol(zs_device_status_word, &zero, sizeof(zero));
+#define ZS_STATUS(NAME)                                        \
+    if (e == cudaSuccess) {                                    \
+        unsigned int w = 0;                                    \
+        e = tu_device_status_##NAME(&w, clear);                \
+        v |= w;                                                \
     }
+    ZS_DEVICE_TUS(ZS_STATUS)
+#undef ZS_STATUS
     if (prev != device) cudaSetDevice(prev);
     *flags = v;
     return e;
