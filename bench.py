@@ -451,10 +451,29 @@ def workload_thumbnails(args, stream, sh):
         print("profile run done", flush=True)
         return
     ms = timed(run, max(3, args.steps // 20), args.warmup)
+    # The same 1024 thumbnails without batching: one ordinary program per image (chain ->
+    # box fit -> inscribe onto a transparent canvas -> sRGB8), fused and plain per-op FP32.
+    # Each image's executable is timed alone (1 warm-up + 2 launches, CUDA events), so its
+    # data is L2-resident when it fits: the per-image sums are lower bounds.
+    from zosimos_gb300.workloads import thumbnail
+    per = {}
+    for mode, key in ((zs.Mode.Fused, "fused"), (zs.Mode.PerOpF32, "plain_fp32")):
+        total, launches = 0.0, 0
+        for k, (w, h) in enumerate(zip(wl, hl)):
+            c, _, _ = thumbnail(w, h, 256)
+            one = zs.Linker.from_included().compile(c).lower_to(zs.Capabilities(mode=mode))
+            dst = out.ptr + k * 256 * 256 * 4
+            total += timed(lambda i, e=one, p=ptrs[k], d=dst: e.run_device([p], [d], sh), 2, 1)
+            launches += one.kernel_count()
+            del one
+        per[key] = (total, launches)
     src_px = int(sum(int(w) * int(h) for w, h in zip(ws, hs)))
     _line("thumbnails 1024 uneven RGBA8 -> colour chain -> box fit 256 -> centred 256^2", src_px,
-          src_px * 4 + 1024 * 256 * 256 * 4, ms, None,
-          {"images": 1024, "source_gpx": round(src_px / 1e9, 3), "launches_per_batch": 1})
+          src_px * 4 + 1024 * 256 * 256 * 4, ms, per["plain_fp32"][0],
+          {"images": 1024, "source_gpx": round(src_px / 1e9, 3), "launches_per_batch": 1,
+           "plain": "one per-op FP32 program per image", "plain_launches": per["plain_fp32"][1],
+           "per_image_fused_ms": round(per["fused"][0], 4), "per_image_fused_launches": per["fused"][1],
+           "speedup_vs_per_image_fused": round(per["fused"][0] / ms, 2)})
 
 
 def workload_layers(args, stream, sh):

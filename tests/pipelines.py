@@ -272,9 +272,9 @@ def oracle_chain_linear(img, f32=False):
 
 
 def fit_size(w, h, canvas):
-    if w >= h:
-        return canvas, max(1, int(round(h * canvas / w)))
-    return max(1, int(round(w * canvas / h))), canvas
+    """Long side -> canvas, short side rounded half away from zero (as the batch kernel)."""
+    from zosimos_gb300.workloads import thumbnail_fit
+    return thumbnail_fit(w, h, canvas)[:2]
 
 
 def oracle_thumbnails(images, canvas=256):
@@ -305,6 +305,16 @@ def ours_thumbnails(images, canvas=256):
     zs.device_synchronize()
     res = out.download(np.empty((len(images), canvas, canvas * 4), np.uint8))
     return [res[i] for i in range(len(images))]
+
+
+def ours_thumbnail_program(img, canvas=256, mode=zs.Mode.Fused):
+    """One thumbnail through its own program (chain -> box fit -> inscribe -> sRGB8)."""
+    from zosimos_gb300.workloads import thumbnail
+    h, w = img.shape[:2]
+    c, i, o = thumbnail(w, h, canvas)
+    pool = Pool()
+    k = pool.insert_srgb(img)
+    return run(c, pool, [(i, k)], [o], mode)[0]
 
 
 def ours_chain(img, mode=zs.Mode.Fused):

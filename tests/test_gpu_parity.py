@@ -270,6 +270,22 @@ def test_batch_thumbnails():
         assert maxdiff(o, r) <= LSB
 
 
+@pytest.mark.parametrize("mode", [zs.Mode.Fused, zs.Mode.PerOpF32])
+def test_thumbnail_program_matches_batch(mode):
+    # The one-program-per-image form of the batched thumbnails (chain, box fit, centred
+    # inscribe onto a transparent canvas) gives the batch kernel's result within 1 LSB.
+    from zosimos_gb300.synthetic import thumbnail_sizes
+    ws, hs = thumbnail_sizes(4, seed=5, lo=40, hi=700)
+    images = [srgb_gradient_noise(int(w), int(h), seed=5, image=i) for i, (w, h) in enumerate(zip(ws, hs))]
+    images.append(srgb_gradient_noise(100, 60, seed=5, image=99))     # upscale case
+    batch = P.ours_thumbnails(images, 256)
+    ref = P.oracle_thumbnails(images, 256)
+    for img, b, r in zip(images, batch, ref):
+        one = P.ours_thumbnail_program(img, 256, mode)
+        assert maxdiff(one, r) <= LSB
+        assert maxdiff(one, b) <= LSB
+
+
 def test_blend_resize_plan():
     c, _, _, _ = P.blend_resize()
     fused = zs.Linker.from_included().compile(c).lower_to()

@@ -37,6 +37,41 @@ def color_chain(w: int, h: int):
     return c, i, o
 
 
+def thumbnail_fit(w: int, h: int, canvas: int = 256):
+    """Fitted size and centred origin of one thumbnail: the long side becomes `canvas`,
+    the short side is rounded half away from zero (at least 1)."""
+    if w >= h:
+        tw, th = canvas, max(1, int(h * canvas / w + 0.5))
+    else:
+        tw, th = max(1, int(w * canvas / h + 0.5)), canvas
+    return tw, th, (canvas - tw) // 2, (canvas - th) // 2
+
+
+def thumbnail(w: int, h: int, canvas: int = 256):
+    """One image of the batched-thumbnail workload as an ordinary program (the one launch
+    per image form): the colour chain of `color_chain` in linear FP32, a box-filter fit,
+    inscribed centred on a transparent linear canvas, sRGB RGBA8 out.
+    Returns (commands, input register, output register)."""
+    from . import Filter, Rectangle
+    tw, th, x0, y0 = thumbnail_fit(w, h, canvas)
+    c = CommandBuffer()
+    src = Descriptor.srgb_rgba8(w, h)
+    i = c.input(src)
+    lin = c.color_convert(i, Descriptor.linear_rgba_f32(w, h))
+    d50 = c.chromatic_adaptation(lin, ChromaticAdaptationMethod.BradfordVonKries, Whitepoint.D50)
+    lab = c.color_convert(d50, Descriptor(w, h, Bits.Float32x4, Parts.LabA, ColorKind.Oklab,
+                                          transfer=Transfer.Linear))
+    scaled = c.color_matrix(lab, OKLAB_SCALE)
+    back = c.color_convert(scaled, Descriptor.linear_rgba_f32(w, h, whitepoint=Whitepoint.D50))
+    d65 = c.chromatic_adaptation(back, ChromaticAdaptationMethod.BradfordVonKries, Whitepoint.D65)
+    small = c.resize_filtered(d65, (tw, th), Filter.Box)
+    blank = c.solid_rgba(Descriptor.linear_rgba_f32(canvas, canvas), [0.0, 0.0, 0.0, 0.0])
+    placed = c.inscribe_placed(blank, Rectangle(x0, y0, x0 + tw, y0 + th), small)
+    out = c.color_convert(placed, Descriptor.srgb_rgba8(canvas, canvas))
+    o, _ = c.output(out)
+    return c, i, o
+
+
 def blend_resize(w: int = 512, h: int = 512, out_w: int = 384, out_h: int = 384):
     """Two RGBA8 sRGB images: decode to linear FP32, alpha-over B onto A, bilinear affine
     resize (scale out/in) onto a transparent canvas, sRGB encode to RGBA8.
