@@ -199,6 +199,17 @@ int zs_cmd_derivative(zs_cmd *cmd, uint32_t src, uint32_t method, uint32_t direc
 int zs_cmd_distribution_normal2d(zs_cmd *cmd, const zs_descriptor *desc, const float params[7], uint32_t *reg);
 int zs_normal2d_with_diagonal(float var0, float var1, float params[7]);
 int zs_normal2d_with_direction(float x, float y, float params[7]);
+/* CommandBuffer::distribution_fractal_noise (command.rs:1585-1606; shaders/fractal_noise.rs,
+ * fractal_noise.frag): fractal Brownian value noise, uncorrelated in all four channels, from
+ * the PCG4D hash of the grid cell corners with smoothstep interpolation, summed over
+ * num_octaves octaves (each rotated by 0.5 rad and scaled by 2, amplitude times damping).
+ * params = [grid_scale x, grid_scale y, initial_amplitude, amplitude_damping, num_octaves];
+ * num_octaves is an integer in [0, 32] (ZS_ERR_INVALID_ARG otherwise).
+ * zs_fractal_noise_with_octaves and zs_fractal_noise_set_damping fill `params` as
+ * FractalNoise::with_octaves and FractalNoise::set_damping do (shaders/fractal_noise.rs:20-49). */
+int zs_cmd_distribution_fractal_noise(zs_cmd *cmd, const zs_descriptor *desc, const float params[5], uint32_t *reg);
+int zs_fractal_noise_with_octaves(uint32_t num_octaves, float params[5]);
+int zs_fractal_noise_set_damping(float params[5], float damping);
 /* CommandBuffer::blend (command.rs:1509, UNIMPLEMENTED upstream, built here):
  * mode 0 Alpha/over, 1 multiply, 2 screen, 3 add; `above` placed at rect.x/rect.y. */
 int zs_cmd_blend(zs_cmd *cmd, uint32_t below, const zs_rect *rect, uint32_t above,

@@ -315,6 +315,79 @@ def normal2d(width: int, height: int, params) -> np.ndarray:
     return out
 
 
+def fractal_noise_with_octaves(num_octaves: int) -> np.ndarray:
+    """FractalNoise::with_octaves (shaders/fractal_noise.rs:20-31): grid 100 x 100, damping 1,
+    amplitude 1 / n in f64 rounded to f32.  [grid x, grid y, amplitude, damping, octaves]."""
+    return np.array([100.0, 100.0, np.float32(1.0 / float(num_octaves)), 1.0, num_octaves], np.float32)
+
+
+def fractal_noise_set_damping(params, damping: float) -> np.ndarray:
+    """FractalNoise::set_damping (shaders/fractal_noise.rs:33-49), in f32."""
+    p = np.asarray(params, np.float32).copy()
+    f = np.float32
+    d = f(damping)
+    total = f(1.0) - f(np.power(d, f(p[4]), dtype=np.float32))
+    p[2] = f(1.0) if abs(total) < f(1e-7) else f(f(1.0) - d) / total
+    p[3] = d
+    return p
+
+
+def _pcg4d(x, y):
+    """PCG4D (Jarzynski and Olano, JCGT 9(3) 2020) of uvec4(x, y, 0, 0), uint32 wraparound;
+    fractal_noise.frag:20-28."""
+    m = np.uint64(0xFFFFFFFF)
+    v = [np.asarray(t, np.uint64) & m for t in (x, y, np.zeros_like(x), np.zeros_like(x))]
+    v = [(t * np.uint64(1664525) + np.uint64(1013904223)) & m for t in v]
+
+    def mix(v):
+        v[0] = (v[0] + v[1] * v[3]) & m
+        v[1] = (v[1] + v[2] * v[0]) & m
+        v[2] = (v[2] + v[0] * v[1]) & m
+        v[3] = (v[3] + v[1] * v[2]) & m
+    mix(v)
+    v = [t ^ (t >> np.uint64(16)) for t in v]
+    mix(v)
+    return v
+
+
+def fractal_noise(width: int, height: int, params) -> np.ndarray:
+    """fractal_noise.frag: fbm(uv) at pixel centres uv = ((x + 0.5) / W, (y + 0.5) / H), in
+    f32 with every product and sum rounded separately; 4 uncorrelated channels.  The rotation
+    between octaves is 2 mat3(cos .5, sin .5, 1, -sin .5, cos .5, 1, 0, 0, 1) with f32
+    constants (only x and y feed the noise)."""
+    f = np.float32
+    p = np.asarray(params, np.float32)
+    c5, c6 = f(2.0) * f(np.cos(0.5)), f(2.0) * f(np.sin(0.5))
+    px = np.broadcast_to((np.arange(width, dtype=f) + f(0.5)) / f(width), (height, width)).astype(f)
+    py = np.broadcast_to(((np.arange(height, dtype=f) + f(0.5)) / f(height))[:, None], (height, width)).astype(f)
+    amp = f(p[2])
+    acc = np.zeros((height, width, 4), f)
+    for _ in range(int(p[4])):
+        tx, ty = (px * p[0]).astype(f), (py * p[1]).astype(f)
+        flx, fly = np.floor(tx), np.floor(ty)
+        fx, fy = (tx - flx).astype(f), (ty - fly).astype(f)
+        # float -> int32 saturates (as the GPU conversion), then reinterpreted as uint32.
+        cx = np.clip(flx.astype(np.float64), -2.0 ** 31, 2.0 ** 31 - 1).astype(np.int64) & 0xFFFFFFFF
+        cy = np.clip(fly.astype(np.float64), -2.0 ** 31, 2.0 ** 31 - 1).astype(np.int64) & 0xFFFFFFFF
+
+        def corner(dx, dy):
+            h = _pcg4d((cx + dx) & 0xFFFFFFFF, (cy + dy) & 0xFFFFFFFF)
+            return np.stack([(t.astype(f) / f(4294967296.0)).astype(f) for t in h], axis=-1)
+        A, B, C, D = corner(0, 0), corner(1, 0), corner(0, 1), corner(1, 1)
+        ux = ((fx * fx).astype(f) * (f(3.0) - (f(2.0) * fx).astype(f))).astype(f)[..., None]
+        uy = ((fy * fy).astype(f) * (f(3.0) - (f(2.0) * fy).astype(f))).astype(f)[..., None]
+        m = (A * (f(1.0) - ux) + B * ux).astype(f)
+        t1 = (((C - A) * uy).astype(f) * (f(1.0) - ux)).astype(f)
+        t2 = (((D - B) * ux).astype(f) * uy).astype(f)
+        n = ((m + t1).astype(f) + t2).astype(f)
+        acc = (acc + (amp * n).astype(f)).astype(f)
+        nx = ((c5 * px).astype(f) + (-c6 * py).astype(f)).astype(f)
+        ny = ((c6 * px).astype(f) + (c5 * py).astype(f)).astype(f)
+        px, py = nx, ny
+        amp = f(amp * p[3])
+    return acc.astype(np.float64)
+
+
 def rgb_to_xyz(primaries="Bt709", whitepoint="D65") -> np.ndarray:
     out = np.zeros(9)
     lib().zo_rgb_to_xyz(ctypes.c_int32(PRIMARIES[primaries]), ctypes.c_int32(WHITEPOINT[whitepoint]), _p(out))

@@ -331,6 +331,28 @@ def test_derivative(background, goldens, method, mode):
     assert maxdiff(ours_h, P.oracle_derivative(background, method, False)) <= LSB
 
 
+@pytest.mark.parametrize("mode", [zs.Mode.Fused, zs.Mode.PerOpF32])
+def test_distribution_fractal_noise(goldens, mode):
+    # tests/blend.rs:314-338: 400 x 400 sRGB RGBA8 fractal noise, 4 octaves.  The hash and the
+    # arithmetic are restated in f32 with the same rounding steps, so the linear values agree
+    # with the oracle to a few ulps and the 8-bit result within one code.
+    import oracle as O
+    params = zs.fractal_noise_with_octaves(4)
+    c = zs.CommandBuffer()
+    o, _ = c.output(c.distribution_fractal_noise(zs.Descriptor.srgb_rgba8(400, 400), params))
+    ours = np.frombuffer(P.run(c, zs.Pool(), [], [o], mode)[0], np.uint8).reshape(400, 1600)
+    want = O.encode(O.SRGB_RGBA8, O.fractal_noise(400, 400, params))
+    assert maxdiff(ours, want) <= LSB
+    assert blockhash256(ours.reshape(400, 400, 4)) in goldens["distribution_fractal2d"]
+    # Damped octaves and a non-square grid.
+    p2 = zs.fractal_noise_set_damping(zs.fractal_noise_with_octaves(6), 0.6)
+    p2[0], p2[1] = 37.0, 12.5
+    c = zs.CommandBuffer()
+    o, _ = c.output(c.distribution_fractal_noise(zs.Descriptor.srgb_rgba8(123, 77), p2))
+    ours = np.frombuffer(P.run(c, zs.Pool(), [], [o], mode)[0], np.uint8).reshape(77, 123 * 4)
+    assert maxdiff(ours, O.encode(O.SRGB_RGBA8, O.fractal_noise(123, 77, p2))) <= LSB
+
+
 @pytest.mark.parametrize("case", ["normal2d", "normal1d", "u8"])
 def test_distribution_normal2d(goldens, case):
     # tests/blend.rs:227-311.

@@ -195,6 +195,22 @@ def test_derivative_plan_and_unimplemented_methods():
         assert e.value.code == 2
 
 
+def test_fractal_noise_parameters_follow_the_reference_constructors():
+    import oracle as O
+    for n in (1, 4, 7):
+        assert (zs.fractal_noise_with_octaves(n) == O.fractal_noise_with_octaves(n)).all()
+        for d in (0.5, 0.8, 1.0):
+            got = zs.fractal_noise_set_damping(zs.fractal_noise_with_octaves(n), d)
+            assert (got == O.fractal_noise_set_damping(O.fractal_noise_with_octaves(n), d)).all()
+    c = CommandBuffer()
+    c.output(c.distribution_fractal_noise(Descriptor.srgb_rgba8(32, 16), zs.fractal_noise_with_octaves(4)))
+    assert Linker.from_included().compile(c).lower_to().kernel_count() == 1
+    bad = zs.fractal_noise_with_octaves(4)
+    bad[4] = 33.0
+    with pytest.raises(zs.ZosimosError):
+        CommandBuffer().distribution_fractal_noise(Descriptor.srgb_rgba8(8, 8), bad)
+
+
 def test_normal2d_parameters_follow_the_reference_constructors():
     import oracle as O
     assert (zs.normal2d_with_diagonal(0.2, 0.2) == O.normal2d_with_diagonal(0.2, 0.2)).all()

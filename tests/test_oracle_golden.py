@@ -159,3 +159,19 @@ def test_distribution_normal_goldens(goldens):
     rgba = np.stack([l8, l8, l8, np.full_like(l8, 255)], -1)
     # The two accepted hashes of the reference differ from each other by more than this.
     assert _hamming(blockhash256(rgba), goldens["distribution_u8"]) <= 3
+
+
+def test_fractal_noise_golden(goldens):
+    # tests/blend.rs:314-338: 400 x 400 sRGB RGBA8, FractalNoise::with_octaves(4).
+    img = O.fractal_noise(400, 400, O.fractal_noise_with_octaves(4))
+    assert blockhash256(O.encode(O.SRGB_RGBA8, img).reshape(400, 400, 4)) in goldens["distribution_fractal2d"]
+
+
+def test_fractal_noise_damping_sums_to_one():
+    # shaders/fractal_noise.rs:52-65: after set_damping(0.5) the 8 octave amplitudes sum to 1.
+    p = O.fractal_noise_set_damping(O.fractal_noise_with_octaves(8), 0.5)
+    amp, total = np.float32(p[2]), np.float32(0.0)
+    for _ in range(8):
+        total = np.float32(total + amp)
+        amp = np.float32(amp * p[3])
+    assert abs(1.0 - float(total)) < 1e-6

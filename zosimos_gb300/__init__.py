@@ -163,6 +163,9 @@ def _lib():
             "zs_cmd_distribution_normal2d": ([P, pD, P, pU32], I32),
             "zs_normal2d_with_diagonal": ([ctypes.c_float, ctypes.c_float, P], I32),
             "zs_normal2d_with_direction": ([ctypes.c_float, ctypes.c_float, P], I32),
+            "zs_cmd_distribution_fractal_noise": ([P, pD, P, pU32], I32),
+            "zs_fractal_noise_with_octaves": ([U32, P], I32),
+            "zs_fractal_noise_set_damping": ([P, ctypes.c_float], I32),
             "zs_cmd_output": ([P, U32, pU32, pD], I32), "zs_cmd_describe": ([P, U32, pD], I32),
             "zs_compile": ([P, ctypes.POINTER(P)], I32), "zs_program_free": ([P], None),
             "zs_lower": ([P, ctypes.POINTER(_CCaps), ctypes.POINTER(P)], I32), "zs_executable_free": ([P], None),
@@ -210,6 +213,20 @@ def normal2d_with_diagonal(var0: float, var1: float) -> np.ndarray:
     """DistributionNormal2d::with_diagonal: parameters of a centred normal density."""
     p = np.zeros(7, np.float32)
     _check(_lib().zs_normal2d_with_diagonal(var0, var1, p.ctypes.data))
+    return p
+
+
+def fractal_noise_with_octaves(num_octaves: int) -> np.ndarray:
+    """FractalNoise::with_octaves: [grid x, grid y, initial amplitude, damping, octaves]."""
+    p = np.zeros(5, np.float32)
+    _check(_lib().zs_fractal_noise_with_octaves(num_octaves, p.ctypes.data))
+    return p
+
+
+def fractal_noise_set_damping(params, damping: float) -> np.ndarray:
+    """FractalNoise::set_damping: amplitudes of all octaves sum to 1."""
+    p = np.ascontiguousarray(np.asarray(params, dtype=np.float32).reshape(5)).copy()
+    _check(_lib().zs_fractal_noise_set_damping(p.ctypes.data, damping))
     return p
 
 
@@ -510,6 +527,11 @@ class CommandBuffer:
         """params: the 7 floats of normal2d_with_diagonal / normal2d_with_direction."""
         p = np.ascontiguousarray(np.asarray(params, dtype=np.float32).reshape(7))
         return self._reg(_lib().zs_cmd_distribution_normal2d, ctypes.byref(desc._c()), p.ctypes.data)
+
+    def distribution_fractal_noise(self, desc: Descriptor, params) -> int:
+        """params: the 5 floats of fractal_noise_with_octaves / fractal_noise_set_damping."""
+        p = np.ascontiguousarray(np.asarray(params, dtype=np.float32).reshape(5))
+        return self._reg(_lib().zs_cmd_distribution_fractal_noise, ctypes.byref(desc._c()), p.ctypes.data)
 
     def derivative(self, src: int, method: int, direction: int = Direction.Width) -> int:
         return self._reg(_lib().zs_cmd_derivative, src, method, direction)

@@ -27,6 +27,9 @@ uint32_t cmd_derivative(Command &c, uint32_t src, uint32_t method, uint32_t dire
 uint32_t cmd_normal2d(Command &c, const Desc &d, const float params[7]);
 void normal2d_with_diagonal(float var0, float var1, float p[7]);
 void normal2d_with_direction(float x, float y, float p[7]);
+uint32_t cmd_fractal_noise(Command &c, const Desc &d, const float params[5]);
+void fractal_noise_with_octaves(uint32_t octaves, float p[5]);
+void fractal_noise_set_damping(float p[5], float damping);
 uint32_t cmd_output(Command &c, uint32_t src, Desc *outformat);
 int batch_thumbnails(Executable *chain, const void *const *images, const uint32_t *widths, const uint32_t *heights,
                      uint32_t n, uint32_t canvas, void *out, cudaStream_t stream);
@@ -338,6 +341,15 @@ int zs_normal2d_with_diagonal(float var0, float var1, float params[7]) {
 int zs_normal2d_with_direction(float x, float y, float params[7]) {
     return guarded([&] { NEED(params); normal2d_with_direction(x, y, params); });
 }
+int zs_cmd_distribution_fractal_noise(zs_cmd *cmd, const zs_descriptor *desc, const float params[5], uint32_t *reg) {
+    return guarded([&] { NEED(cmd); NEED(desc); NEED(params); NEED(reg); *reg = cmd_fractal_noise(cmd->c, *desc, params); });
+}
+int zs_fractal_noise_with_octaves(uint32_t num_octaves, float params[5]) {
+    return guarded([&] { NEED(params); fractal_noise_with_octaves(num_octaves, params); });
+}
+int zs_fractal_noise_set_damping(float params[5], float damping) {
+    return guarded([&] { NEED(params); fractal_noise_set_damping(params, damping); });
+}
 int zs_cmd_derivative(zs_cmd *cmd, uint32_t src, uint32_t method, uint32_t direction, uint32_t *reg) {
     return guarded([&] { NEED(cmd); NEED(reg); *reg = cmd_derivative(cmd->c, src, method, direction); });
 }
@@ -374,6 +386,7 @@ int zs_compile(const zs_cmd *cmd, zs_program **out) {
                 break;
             case OpKind::Bilinear:
             case OpKind::Normal2d:
+            case OpKind::FractalNoise:
             case OpKind::Solid: break;
             case OpKind::Derivative:
                 // DerivativeMethod::to_shader: Roberts, Scharr4, Scharr5, Scharr5Tab are

@@ -281,6 +281,40 @@ uint32_t cmd_normal2d(Command &c, const Desc &d, const float params[7]) {
     return c.push(op);
 }
 
+// CommandBuffer::distribution_fractal_noise (command.rs:1585-1606): a generator with the
+// descriptor given; params = [grid_scale x, grid_scale y, initial_amplitude,
+// amplitude_damping, num_octaves].  The octave count is capped at 32: past it the grid
+// coordinates have grown by 2^32 and carry no fractional bits in f32.
+uint32_t cmd_fractal_noise(Command &c, const Desc &d, const float params[5]) {
+    if (!is_consistent(d)) fail(ZS_ERR_TYPE, "inconsistent descriptor for fractal noise: " + describe(d));
+    const float n = params[4];
+    if (!(n >= 0.f && n <= 32.f) || n != std::floor(n)) fail(ZS_ERR_INVALID_ARG, "num_octaves must be an integer in [0, 32]");
+    Op op{OpKind::FractalNoise};
+    op.desc = d;
+    op.desc.row_stride = 0;
+    for (int k = 0; k < 5; ++k) op.fparams[k] = params[k];
+    return c.push(op);
+}
+
+// FractalNoise::with_octaves (shaders/fractal_noise.rs:20-31): damping 1, amplitude
+// 1 / n (computed in f64, rounded to f32), grid 100 x 100.
+void fractal_noise_with_octaves(uint32_t octaves, float p[5]) {
+    p[0] = 100.f;
+    p[1] = 100.f;
+    p[2] = (float)(1.0 / (double)octaves);
+    p[3] = 1.f;
+    p[4] = (float)octaves;
+}
+
+// FractalNoise::set_damping (shaders/fractal_noise.rs:33-49): the initial amplitude is chosen
+// so that the amplitudes of all octaves sum to 1, in f32.
+void fractal_noise_set_damping(float p[5], float damping) {
+    const float n = (float)(double)p[4];
+    const float total = 1.0f - std::pow(damping, n);
+    p[2] = std::fabs(total) < 1e-7f ? 1.0f : (1.0f - damping) / total;
+    p[3] = damping;
+}
+
 // DistributionNormal2d::with_diagonal (shaders/distribution_normal2d.rs:24-38), in f32.
 void normal2d_with_diagonal(float var0, float var1, float p[7]) {
     const float pi = 3.14159265358979323846f;

@@ -747,6 +747,15 @@ struct Planner {
                 for (int k = 0; k < 7; ++k) p->a.cons[k] = op.fparams[k];
                 set_pending(r, std::move(p));
             } break;
+            case OpKind::FractalNoise: {
+                auto p = new_pending(ZS_PR_FRACTAL, d.width, d.height, "distribution fractal noise");
+                for (int k = 0; k < 5; ++k) p->a.cons[k] = op.fparams[k];
+                // The rotation between octaves, 2 mat3(cos .5, sin .5, 1, -sin .5, cos .5, 1, 0, 0, 1)
+                // (fractal_noise.frag), its constants rounded to f32 before the doubling.
+                p->a.cons[5] = 2.0f * (float)std::cos(0.5);
+                p->a.cons[6] = 2.0f * (float)std::sin(0.5);
+                set_pending(r, std::move(p));
+            } break;
             case OpKind::Derivative: {
                 use(op.a);
                 need(op.a);

@@ -89,7 +89,7 @@ struct HProgram {
 enum class OpKind {
     Input, Output, Crop, ColorConvert, ChromaticAdaptation, ColorMatrix, Extract, Inject,
     Transmute, Inscribe, InscribePlaced, Palette, Bilinear, Solid, Affine, Resize,
-    ResizeFiltered, Blend, Derivative, Normal2d
+    ResizeFiltered, Blend, Derivative, Normal2d, FractalNoise
 };
 
 struct Op {

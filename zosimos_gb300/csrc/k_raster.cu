@@ -28,6 +28,48 @@ uint64_t kernel_launch_count() { return g_kernel_launches.load(); }
 void add_kernel_launches(uint64_t n) { g_kernel_launches.fetch_add(n); }
 }  // namespace zs
 
+// PCG4D hash (Jarzynski and Olano, "Hash Functions for GPU Rendering", JCGT 9(3), 2020),
+// as fractal_noise.frag applies it to uvec4(cell, 0, 0).
+__device__ __forceinline__ uint4 zs_pcg4d(uint4 v) {
+    v.x = v.x * 1664525u + 1013904223u;
+    v.y = v.y * 1664525u + 1013904223u;
+    v.z = v.z * 1664525u + 1013904223u;
+    v.w = v.w * 1664525u + 1013904223u;
+    v.x += v.y * v.w; v.y += v.z * v.x; v.z += v.x * v.y; v.w += v.y * v.z;
+    v.x ^= v.x >> 16; v.y ^= v.y >> 16; v.z ^= v.z >> 16; v.w ^= v.w >> 16;
+    v.x += v.y * v.w; v.y += v.z * v.x; v.z += v.x * v.y; v.w += v.y * v.z;
+    return v;
+}
+
+// hash(): the four hashed words as floats divided by float(0xFFFFFFFF) (= 2^32 in f32).
+__device__ __forceinline__ float4 zs_noise_hash(uint32_t cx, uint32_t cy) {
+    const uint4 h = zs_pcg4d(make_uint4(cx, cy, 0u, 0u));
+    const float m = 4294967296.0f;
+    return make_float4(__fdiv_rn(__uint2float_rn(h.x), m), __fdiv_rn(__uint2float_rn(h.y), m),
+                       __fdiv_rn(__uint2float_rn(h.z), m), __fdiv_rn(__uint2float_rn(h.w), m));
+}
+
+// noise() of fractal_noise.frag at grid point (ptx, pty): value noise of the four cell
+// corners, smoothstep weights, mix(a, b, u.x) + (c - a) u.y (1 - u.x) + (d - b) u.x u.y.
+__device__ __forceinline__ float zs_noise_mix(float a, float b, float c, float d, float ux, float uy) {
+    const float m = __fadd_rn(__fmul_rn(a, __fsub_rn(1.0f, ux)), __fmul_rn(b, ux));
+    const float t1 = __fmul_rn(__fmul_rn(__fsub_rn(c, a), uy), __fsub_rn(1.0f, ux));
+    const float t2 = __fmul_rn(__fmul_rn(__fsub_rn(d, b), ux), uy);
+    return __fadd_rn(__fadd_rn(m, t1), t2);
+}
+
+__device__ __forceinline__ float4 zs_value_noise(float ptx, float pty) {
+    const float flx = floorf(ptx), fly = floorf(pty);
+    const float fx = __fsub_rn(ptx, flx), fy = __fsub_rn(pty, fly);
+    const uint32_t cx = (uint32_t)(int)flx, cy = (uint32_t)(int)fly;
+    const float4 A = zs_noise_hash(cx, cy), B = zs_noise_hash(cx + 1u, cy), C = zs_noise_hash(cx, cy + 1u),
+                 D = zs_noise_hash(cx + 1u, cy + 1u);
+    const float ux = __fmul_rn(__fmul_rn(fx, fx), __fsub_rn(3.0f, __fmul_rn(2.0f, fx)));
+    const float uy = __fmul_rn(__fmul_rn(fy, fy), __fsub_rn(3.0f, __fmul_rn(2.0f, fy)));
+    return make_float4(zs_noise_mix(A.x, B.x, C.x, D.x, ux, uy), zs_noise_mix(A.y, B.y, C.y, D.y, ux, uy),
+                       zs_noise_mix(A.z, B.z, C.z, D.z, ux, uy), zs_noise_mix(A.w, B.w, C.w, D.w, ux, uy));
+}
+
 // The gathered image of an AFFINE launch at (x, y): a stored texel, or (virt1) its
 // pixel-aligned producer and program evaluated here.
 __device__ __forceinline__ float4 zs_src1_px(const ZsRasterArgs &a, int x, int y) {
@@ -191,6 +233,29 @@ __global__ void __launch_bounds__(256) zs_raster_kernel(const __grid_constant__ 
             const float q = px * (c[2] * px + c[4] * py) + py * (c[3] * px + c[5] * py);
             const float val = expf(-0.5f * q) / sqrtf(c[6]);
             r = make_float4(val, val, val, 1.0f);
+        } break;
+        case ZS_PR_FRACTAL: {
+            // fractal_noise.frag: fbm(uv) at the pixel centre, every product and sum rounded
+            // separately (no contraction), so the result is reproducible on the host.
+            const float *c = a.cons;
+            float px = __fdiv_rn((float)x + 0.5f, (float)a.width), py = __fdiv_rn((float)y + 0.5f, (float)a.height);
+            float amp = c[2];
+            const int octaves = (int)c[4];
+            float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int o = 0; o < octaves; ++o) {
+                const float4 n = zs_value_noise(__fmul_rn(px, c[0]), __fmul_rn(py, c[1]));
+                acc.x = __fadd_rn(acc.x, __fmul_rn(amp, n.x));
+                acc.y = __fadd_rn(acc.y, __fmul_rn(amp, n.y));
+                acc.z = __fadd_rn(acc.z, __fmul_rn(amp, n.z));
+                acc.w = __fadd_rn(acc.w, __fmul_rn(amp, n.w));
+                // next_point: (x, y) <- 2 (cos .5 x - sin .5 y, sin .5 x + cos .5 y)
+                const float nx = __fadd_rn(__fmul_rn(c[5], px), __fmul_rn(-c[6], py));
+                const float ny = __fadd_rn(__fmul_rn(c[6], px), __fmul_rn(c[5], py));
+                px = nx;
+                py = ny;
+                amp = __fmul_rn(amp, c[3]);
+            }
+            r = acc;
         } break;
         case ZS_PR_BOX3: {
             // box3.frag:12-53: clamp-to-edge nearest taps (the default sampler); each row of

@@ -85,7 +85,8 @@ enum ZsProducer : uint8_t {
     ZS_PR_LAYERS,       // planner only: a layer stack, launched by k_layers.cu
     ZS_PR_RESAMPLE_2D,  // both separable passes in one tiled launch (k_resample.cu)
     ZS_PR_BOX3,         // 3x3 stencil of src0, weights in cons[0..8]   (box3.frag)
-    ZS_PR_NORMAL2D      // normal density, params in cons[0..6]          (distribution_normal2d.frag)
+    ZS_PR_NORMAL2D,     // normal density, params in cons[0..6]          (distribution_normal2d.frag)
+    ZS_PR_FRACTAL       // fractal value noise, params in cons[0..6]     (fractal_noise.frag)
 };
 
 struct ZsSource {
