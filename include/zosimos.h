@@ -199,6 +199,16 @@ int zs_cmd_derivative(zs_cmd *cmd, uint32_t src, uint32_t method, uint32_t direc
 int zs_cmd_distribution_normal2d(zs_cmd *cmd, const zs_descriptor *desc, const float params[7], uint32_t *reg);
 int zs_normal2d_with_diagonal(float var0, float var1, float params[7]);
 int zs_normal2d_with_direction(float x, float y, float params[7]);
+/* CommandBuffer::buffer_init / buffer_zero (command.rs:1777-1803): a byte buffer register
+ * holding a copy of `bytes` (len bytes) or `len` zero bytes.  A buffer register is not an
+ * image: image ops given one fail with ZS_ERR_TYPE. */
+int zs_cmd_buffer_init(zs_cmd *cmd, const void *bytes, uint64_t len, uint32_t *reg);
+int zs_cmd_buffer_zero(zs_cmd *cmd, uint64_t len, uint32_t *reg);
+/* CommandBuffer::from_buffer (command.rs:937-968): the buffer's bytes read as an image of
+ * `desc` whose rows start every align_up(width * texel bytes, 256) bytes (the GPU row layout of
+ * Descriptor::to_aligned, buffer.rs:121-134).  ZS_ERR_TYPE when `buffer` is not a buffer
+ * register, ZS_ERR_OTHER (INVALID_CALL) when the buffer holds fewer than height aligned rows. */
+int zs_cmd_from_buffer(zs_cmd *cmd, uint32_t buffer, const zs_descriptor *desc, uint32_t *reg);
 /* CommandBuffer::distribution_fractal_noise (command.rs:1585-1606; shaders/fractal_noise.rs,
  * fractal_noise.frag): fractal Brownian value noise, uncorrelated in all four channels, from
  * the PCG4D hash of the grid cell corners with smoothstep interpolation, summed over

@@ -195,6 +195,27 @@ def test_derivative_plan_and_unimplemented_methods():
         assert e.value.code == 2
 
 
+def test_from_buffer_checks():
+    # command.rs:937-968: a buffer register is required, and it must hold `height` rows
+    # aligned to 256 bytes.
+    c = CommandBuffer()
+    b = c.buffer_init(np.zeros(8 * 256, np.uint8))
+    luma = zs.Descriptor(8, 8, zs.Bits.UInt8, zs.Parts.Luma, zs.ColorKind.Rgb, zs.Primaries.Bt709,
+                         zs.Transfer.Srgb, zs.Whitepoint.D65)
+    c.output(c.from_buffer(b, luma))
+    assert Linker.from_included().compile(c).lower_to().kernel_count() == 1
+    with pytest.raises(zs.ZosimosError) as e:
+        c.from_buffer(b, Descriptor.srgb_rgba8(65, 8))       # 512-byte rows: 4096 bytes needed
+    assert e.value.code == 4                                 # ZS_ERR_OTHER: INVALID_CALL upstream
+    with pytest.raises(zs.ZosimosError):
+        c.color_convert(b, Descriptor.srgb_rgba8(8, 8))      # a buffer is not an image
+    i = c.input(Descriptor.srgb_rgba8(8, 8))
+    with pytest.raises(zs.ZosimosError):
+        c.from_buffer(i, luma)                              # an image is not a buffer
+    z = c.buffer_zero(4096)
+    c.output(c.from_buffer(z, Descriptor.srgb_rgba8(64, 16)))
+
+
 def test_fractal_noise_parameters_follow_the_reference_constructors():
     import oracle as O
     for n in (1, 4, 7):

@@ -164,6 +164,9 @@ def _lib():
             "zs_normal2d_with_diagonal": ([ctypes.c_float, ctypes.c_float, P], I32),
             "zs_normal2d_with_direction": ([ctypes.c_float, ctypes.c_float, P], I32),
             "zs_cmd_distribution_fractal_noise": ([P, pD, P, pU32], I32),
+            "zs_cmd_buffer_init": ([P, P, U64, pU32], I32),
+            "zs_cmd_buffer_zero": ([P, U64, pU32], I32),
+            "zs_cmd_from_buffer": ([P, U32, pD, pU32], I32),
             "zs_fractal_noise_with_octaves": ([U32, P], I32),
             "zs_fractal_noise_set_damping": ([P, ctypes.c_float], I32),
             "zs_cmd_output": ([P, U32, pU32, pD], I32), "zs_cmd_describe": ([P, U32, pD], I32),
@@ -527,6 +530,19 @@ class CommandBuffer:
         """params: the 7 floats of normal2d_with_diagonal / normal2d_with_direction."""
         p = np.ascontiguousarray(np.asarray(params, dtype=np.float32).reshape(7))
         return self._reg(_lib().zs_cmd_distribution_normal2d, ctypes.byref(desc._c()), p.ctypes.data)
+
+    def buffer_init(self, data) -> int:
+        """A byte buffer register holding a copy of `data` (bytes or a uint8 array)."""
+        b = np.frombuffer(bytes(data), np.uint8) if not isinstance(data, np.ndarray) else data
+        b = np.ascontiguousarray(b, dtype=np.uint8).reshape(-1)
+        return self._reg(_lib().zs_cmd_buffer_init, b.ctypes.data, b.nbytes)
+
+    def buffer_zero(self, length: int) -> int:
+        return self._reg(_lib().zs_cmd_buffer_zero, length)
+
+    def from_buffer(self, buffer: int, desc: Descriptor) -> int:
+        """The buffer's bytes as an image of `desc`, rows 256-byte aligned."""
+        return self._reg(_lib().zs_cmd_from_buffer, buffer, ctypes.byref(desc._c()))
 
     def distribution_fractal_noise(self, desc: Descriptor, params) -> int:
         """params: the 5 floats of fractal_noise_with_octaves / fractal_noise_set_damping."""

@@ -28,6 +28,8 @@ uint32_t cmd_normal2d(Command &c, const Desc &d, const float params[7]);
 void normal2d_with_diagonal(float var0, float var1, float p[7]);
 void normal2d_with_direction(float x, float y, float p[7]);
 uint32_t cmd_fractal_noise(Command &c, const Desc &d, const float params[5]);
+uint32_t cmd_buffer_init(Command &c, const void *bytes, uint64_t n, uint64_t len);
+uint32_t cmd_from_buffer(Command &c, uint32_t buffer, const Desc &target);
 void fractal_noise_with_octaves(uint32_t octaves, float p[5]);
 void fractal_noise_set_damping(float p[5], float damping);
 uint32_t cmd_output(Command &c, uint32_t src, Desc *outformat);
@@ -344,6 +346,15 @@ int zs_normal2d_with_direction(float x, float y, float params[7]) {
 int zs_cmd_distribution_fractal_noise(zs_cmd *cmd, const zs_descriptor *desc, const float params[5], uint32_t *reg) {
     return guarded([&] { NEED(cmd); NEED(desc); NEED(params); NEED(reg); *reg = cmd_fractal_noise(cmd->c, *desc, params); });
 }
+int zs_cmd_buffer_init(zs_cmd *cmd, const void *bytes, uint64_t len, uint32_t *reg) {
+    return guarded([&] { NEED(cmd); NEED(reg); *reg = cmd_buffer_init(cmd->c, bytes, len, len); });
+}
+int zs_cmd_buffer_zero(zs_cmd *cmd, uint64_t len, uint32_t *reg) {
+    return guarded([&] { NEED(cmd); NEED(reg); *reg = cmd_buffer_init(cmd->c, nullptr, 0, len); });
+}
+int zs_cmd_from_buffer(zs_cmd *cmd, uint32_t buffer, const zs_descriptor *desc, uint32_t *reg) {
+    return guarded([&] { NEED(cmd); NEED(desc); NEED(reg); *reg = cmd_from_buffer(cmd->c, buffer, *desc); });
+}
 int zs_fractal_noise_with_octaves(uint32_t num_octaves, float params[5]) {
     return guarded([&] { NEED(params); fractal_noise_with_octaves(num_octaves, params); });
 }
@@ -387,7 +398,9 @@ int zs_compile(const zs_cmd *cmd, zs_program **out) {
             case OpKind::Bilinear:
             case OpKind::Normal2d:
             case OpKind::FractalNoise:
+            case OpKind::BufferInit:
             case OpKind::Solid: break;
+            case OpKind::FromBuffer: p.uses[op.a]++; break;
             case OpKind::Derivative:
                 // DerivativeMethod::to_shader: Roberts, Scharr4, Scharr5, Scharr5Tab are
                 // CompileError::NotYetImplemented (command.rs:3397-3402).

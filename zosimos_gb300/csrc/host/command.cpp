@@ -17,7 +17,39 @@ bool Command::is_value(uint32_t reg) const { return reg < ops.size() && ops[reg]
 
 const Desc &Command::describe(uint32_t reg) const {
     if (!is_value(reg)) fail(ZS_ERR_BAD_REGISTER, "register does not name an image value");
+    if (ops[reg].kind == OpKind::BufferInit) fail(ZS_ERR_TYPE, "register names a buffer, not an image");
     return ops[reg].desc;
+}
+
+// CommandBuffer::buffer_init / buffer_zero (command.rs:1777-1803): a byte buffer of `len`
+// bytes, the first `n` from `bytes`, the rest zero.
+uint32_t cmd_buffer_init(Command &c, const void *bytes, uint64_t n, uint64_t len) {
+    if (n > len) fail(ZS_ERR_INVALID_ARG, "buffer initialiser longer than the buffer");
+    if (n && !bytes) fail(ZS_ERR_INVALID_ARG, "null buffer initialiser");
+    Op op{OpKind::BufferInit};
+    op.len = len;
+    if (n) op.data.assign((const uint8_t *)bytes, (const uint8_t *)bytes + n);
+    return c.push(op);
+}
+
+// Rows of an image in a buffer are aligned to 256 bytes, as the GPU copy layout
+// (Descriptor::to_aligned, buffer.rs:121-134).
+uint64_t aligned_row_bytes(const Desc &d) { return ((uint64_t)d.width * texel_bytes(d.bits) + 255) & ~(uint64_t)255; }
+
+// CommandBuffer::from_buffer (command.rs:937-968): the buffer's bytes read as an image of
+// `d` with 256-byte aligned rows; the buffer must hold at least height aligned rows.
+uint32_t cmd_from_buffer(Command &c, uint32_t buffer, const Desc &target) {
+    if (!c.is_value(buffer) || c.ops[buffer].kind != OpKind::BufferInit)
+        fail(ZS_ERR_TYPE, "from_buffer needs a buffer register");
+    Desc d = target;
+    d.row_stride = 0;
+    if (!is_consistent(d)) fail(ZS_ERR_TYPE, "inconsistent descriptor for from_buffer: " + describe(d));
+    const uint64_t need = aligned_row_bytes(d) * d.height;
+    if (c.ops[buffer].len < need) fail(ZS_ERR_OTHER, "buffer too small for this image descriptor");
+    Op op{OpKind::FromBuffer};
+    op.a = buffer;
+    op.desc = d;
+    return c.push(op);
 }
 
 static Desc with_size(Desc d, uint32_t w, uint32_t h) {

@@ -14,6 +14,7 @@
 // FP16), PER_OP_F32 / PER_OP_F16 (one launch per op, linear RGBA intermediates: the
 // plain baseline the fused executor is measured against).
 #include <cmath>
+#include <algorithm>
 #include <cstring>
 #include <sstream>
 
@@ -568,7 +569,7 @@ struct Planner {
                 for (size_t k = 0; k < E.output_regs.size(); ++k)
                     if (E.output_regs[k] == r) os = E.output_slot[k];
                 if (os == vals[src].slot) break;
-                if (format_equal(vals[src].fmt, E.slots[os].fmt)) {
+                if (format_equal(vals[src].fmt, E.slots[os].fmt) && E.slots[vals[src].slot].stride == E.slots[os].stride) {
                     Step st;
                     st.kind = StepKind::Copy;
                     st.src_slot[0] = vals[src].slot;
@@ -746,6 +747,27 @@ struct Planner {
                 auto p = new_pending(ZS_PR_NORMAL2D, d.width, d.height, "distribution normal2d");
                 for (int k = 0; k < 7; ++k) p->a.cons[k] = op.fparams[k];
                 set_pending(r, std::move(p));
+            } break;
+            case OpKind::BufferInit:
+                break;   // bytes only: every from_buffer view of it becomes a constant image
+            case OpKind::FromBuffer: {
+                // CommandBuffer::from_buffer (command.rs:937-968): the buffer's bytes as an image
+                // with 256-byte aligned rows, uploaded once with the executable's tables.
+                use(op.a);
+                const Op &b = P.ops[op.a];
+                const ZsFormat f = format_of(d);
+                const int64_t stride = (int64_t)((((uint64_t)d.width * f.bpp) + 255) & ~(uint64_t)255);
+                std::vector<uint8_t> bytes((size_t)stride * d.height, 0);
+                if (!b.data.empty()) std::memcpy(bytes.data(), b.data.data(), std::min(bytes.size(), b.data.size()));
+                const int s = table_slot(bytes.data(), bytes.size());
+                Slot &sl = E.slots[s];
+                sl.width = d.width;
+                sl.height = d.height;
+                sl.fmt = f;
+                sl.stride = stride;
+                vals[r].materialized = true;
+                vals[r].slot = s;
+                vals[r].fmt = f;
             } break;
             case OpKind::FractalNoise: {
                 auto p = new_pending(ZS_PR_FRACTAL, d.width, d.height, "distribution fractal noise");

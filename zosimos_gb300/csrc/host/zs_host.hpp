@@ -89,7 +89,7 @@ struct HProgram {
 enum class OpKind {
     Input, Output, Crop, ColorConvert, ChromaticAdaptation, ColorMatrix, Extract, Inject,
     Transmute, Inscribe, InscribePlaced, Palette, Bilinear, Solid, Affine, Resize,
-    ResizeFiltered, Blend, Derivative, Normal2d, FractalNoise
+    ResizeFiltered, Blend, Derivative, Normal2d, FractalNoise, BufferInit, FromBuffer
 };
 
 struct Op {
@@ -101,6 +101,8 @@ struct Op {
     uint32_t u0 = 0, u1 = 0;     // sampling / filter / mode / channels
     int32_t i0 = -1, i1 = -1;
     HProgram prog;               // per-pixel semantics of colour ops
+    std::vector<uint8_t> data;   // BufferInit: initial bytes (zero-extended to `len`)
+    uint64_t len = 0;            // BufferInit: buffer size in bytes
 };
 
 struct Command {
