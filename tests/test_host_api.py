@@ -203,7 +203,8 @@ def test_from_buffer_checks():
     luma = zs.Descriptor(8, 8, zs.Bits.UInt8, zs.Parts.Luma, zs.ColorKind.Rgb, zs.Primaries.Bt709,
                          zs.Transfer.Srgb, zs.Whitepoint.D65)
     c.output(c.from_buffer(b, luma))
-    assert Linker.from_included().compile(c).lower_to().kernel_count() == 1
+    exe = Linker.from_included().compile(c).lower_to()
+    assert exe.kernel_count() == 0 and "copy" in exe.describe()     # a row copy, no kernel
     with pytest.raises(zs.ZosimosError) as e:
         c.from_buffer(b, Descriptor.srgb_rgba8(65, 8))       # 512-byte rows: 4096 bytes needed
     assert e.value.code == 4                                 # ZS_ERR_OTHER: INVALID_CALL upstream

@@ -569,12 +569,21 @@ struct Planner {
                 for (size_t k = 0; k < E.output_regs.size(); ++k)
                     if (E.output_regs[k] == r) os = E.output_slot[k];
                 if (os == vals[src].slot) break;
-                if (format_equal(vals[src].fmt, E.slots[os].fmt) && E.slots[vals[src].slot].stride == E.slots[os].stride) {
+                if (format_equal(vals[src].fmt, E.slots[os].fmt)) {
+                    // The same texels: a byte copy (row by row when the strides differ, as for
+                    // a from_buffer image with 256-byte aligned rows).
                     Step st;
                     st.kind = StepKind::Copy;
                     st.src_slot[0] = vals[src].slot;
                     st.dst_slot = os;
-                    st.copy_bytes = E.slots[os].bytes;
+                    const Slot &ss = E.slots[vals[src].slot], &ds = E.slots[os];
+                    st.copy_bytes = ds.bytes;
+                    if (ss.stride != ds.stride) {
+                        st.copy_bytes = (uint64_t)ds.width * ds.fmt.bpp;
+                        st.copy_rows = (uint64_t)ds.height;
+                        st.copy_src_pitch = ss.stride;
+                        st.copy_dst_pitch = ds.stride;
+                    }
                     st.label = "copy to output";
                     E.steps.push_back(st);
                 } else {

@@ -92,9 +92,15 @@ void Executable::record_range(cudaStream_t stream, const std::vector<void *> &pt
         const Step &st = steps[k];
         switch (st.kind) {
         case StepKind::Copy:
-            check_cuda(cudaMemcpyAsync(ptrs[st.dst_slot], ptrs[st.src_slot[0]], st.copy_bytes, cudaMemcpyDeviceToDevice,
-                                       stream),
-                       "device copy");
+            if (st.copy_rows > 0)
+                check_cuda(cudaMemcpy2DAsync(ptrs[st.dst_slot], (size_t)st.copy_dst_pitch, ptrs[st.src_slot[0]],
+                                             (size_t)st.copy_src_pitch, st.copy_bytes, st.copy_rows,
+                                             cudaMemcpyDeviceToDevice, stream),
+                           "device row copy");
+            else
+                check_cuda(cudaMemcpyAsync(ptrs[st.dst_slot], ptrs[st.src_slot[0]], st.copy_bytes,
+                                           cudaMemcpyDeviceToDevice, stream),
+                           "device copy");
             break;
         case StepKind::Layers: {
             ZsLayersArgs &L = *st.layers;      // pointers change per launch: patch a copy

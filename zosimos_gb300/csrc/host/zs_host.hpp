@@ -167,6 +167,9 @@ struct Step {
     int vimg_slot = -1, vimg_index_slot = -1;                   // RESAMPLE_2D tensor-core band images
     int vsrc_slot[2] = {-1, -1};                                // AFFINE virt1: the gathered producer's sources
     uint64_t copy_bytes = 0;
+    // Copy of rows between different row strides (copy_rows > 0): copy_bytes per row.
+    uint64_t copy_rows = 0;
+    int64_t copy_src_pitch = 0, copy_dst_pitch = 0;
     std::string label;
 };
 
