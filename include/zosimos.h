@@ -254,7 +254,10 @@ typedef struct zs_capabilities {
 enum {
     /* resize_filtered: use the FP32 SIMT resample kernel even where the tensor-core path
      * (f16 band matrices, FP32 accumulation) applies. */
-    ZS_CAP_SIMT_RESAMPLE = 1
+    ZS_CAP_SIMT_RESAMPLE = 1,
+    /* zs_run_host: always stage host buffers through device copies, even where the kernel
+     * could read and write pinned host memory directly (see zs_run_host). */
+    ZS_CAP_NO_ZERO_COPY = 2
 };
 
 typedef struct zs_executable zs_executable;
@@ -293,7 +296,12 @@ void zs_exec_free(zs_execution *exec);
 /* Runs the whole executable once: inputs[i] bound to the i-th input register (in
  * declaration order) from host memory, outputs[j] receive the j-th output (host
  * memory).  Equivalent to insert/bind/launch/step/retire/read.  Host buffers that
- * are pinned (zs_host_alloc) transfer at full link speed. */
+ * are pinned (zs_host_alloc) transfer at full link speed.  An executable that is one
+ * pixel-local colour chain, given pinned (device-mapped) 16-byte aligned host buffers, runs
+ * zero copy: on a Grace host the chain kernel loads its input from and stores its output to
+ * host memory over NVLink-C2C, one launch and no staging copies (ZS_CAP_NO_ZERO_COPY
+ * turns this off).  Other host buffers of such a chain go through row stripes whose upload,
+ * kernel and download overlap on three streams. */
 int zs_run_host(zs_executable *exe, const void *const *inputs, uint32_t n_inputs,
                 void *const *outputs, uint32_t n_outputs);
 /* Same, with device-resident inputs and outputs (no host copies). */

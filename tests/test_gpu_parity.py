@@ -92,6 +92,36 @@ def test_chain_run_host_striped():
     assert maxdiff(out_h[:64], P.oracle_chain(img[:64])) <= LSB
 
 
+@pytest.mark.parametrize("zero_copy", [True, False])
+def test_chain_run_host_pinned(zero_copy):
+    # Pinned host buffers: the lone chain runs zero copy (the kernel reads and writes host
+    # memory directly) or, with zero_copy off, through staged row stripes; both give the
+    # device-resident result byte for byte.
+    import ctypes
+    w, h = 2048, 2050
+    img = P.rgba_bytes(srgb_gradient_noise(w, h, seed=8))
+    c, _, _ = P.chain_commands(w, h)
+    exe = zs.Linker.from_included().compile(c).lower_to(zs.Capabilities(zero_copy=zero_copy))
+    lib = zs._lib()
+    hin, hout = lib.zs_host_alloc(img.nbytes), lib.zs_host_alloc(img.nbytes)
+    try:
+        ctypes.memmove(hin, img.ctypes.data, img.nbytes)
+        before = zs.kernel_launch_count()
+        zs._check(lib.zs_run_host(exe._h, (ctypes.c_void_p * 1)(hin), 1, (ctypes.c_void_p * 1)(hout), 1))
+        launches = zs.kernel_launch_count() - before
+        out_h = np.empty_like(img)
+        ctypes.memmove(out_h.ctypes.data, hout, img.nbytes)
+    finally:
+        lib.zs_host_free(hin)
+        lib.zs_host_free(hout)
+    assert launches == (1 if zero_copy else 8)
+    src, dst = zs.DeviceBuffer(img.nbytes), zs.DeviceBuffer(img.nbytes)
+    src.upload(img)
+    exe.run_device([src.ptr], [dst.ptr])
+    zs.device_synchronize()
+    assert (out_h == dst.download(np.empty_like(img))).all()
+
+
 def test_composed(background, foreground, goldens):
     ours = P.ours_composed(background, foreground)
     assert (ours == P.oracle_composed(background, foreground)).all()

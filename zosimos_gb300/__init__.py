@@ -385,6 +385,7 @@ class Capabilities:
     mode: int = Mode.Fused
     use_graph: bool = True
     simt_resample: bool = False
+    zero_copy: bool = True        # run_host of a lone chain on pinned host buffers: no staging copies
 
 
 # ---------------------------------------------------------------- pool
@@ -598,7 +599,8 @@ class Program:
 
     def lower_to(self, caps: Optional[Capabilities] = None) -> "Executable":
         caps = caps or Capabilities()
-        c = _CCaps(caps.device, caps.mode, int(caps.use_graph), 1 if caps.simt_resample else 0)
+        c = _CCaps(caps.device, caps.mode, int(caps.use_graph),
+                   (1 if caps.simt_resample else 0) | (0 if caps.zero_copy else 2))
         h = ctypes.c_void_p()
         _check(_lib().zs_lower(self._h, ctypes.byref(c), ctypes.byref(h)))
         return Executable(h)

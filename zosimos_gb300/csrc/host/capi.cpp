@@ -607,6 +607,40 @@ static cudaStream_t exe_stream(zs_executable *exe) {
     return exe->stream;
 }
 
+// Device address of a pinned, device-mapped host buffer (cudaMallocHost / cudaHostAlloc /
+// cudaHostRegister), or null for any other pointer or one not 16-byte aligned.
+static void *mapped_host_pointer(const void *p) {
+    cudaPointerAttributes at{};
+    if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (at.type != cudaMemoryTypeHost || !at.devicePointer || ((uintptr_t)at.devicePointer & 15u)) return nullptr;
+    return at.devicePointer;
+}
+
+// A lone fused colour chain on pinned host buffers runs zero copy: the GPU reaches pinned
+// host memory through its own address space (over NVLink-C2C on a Grace host), so the chain
+// kernel streams the input from and the output to host memory, one launch, no staging.
+static bool run_host_zero_copy(zs_executable *exe, const void *const *inputs, void *const *outputs) {
+    Executable &E = *exe->e;
+    if (E.flags & ZS_CAP_NO_ZERO_COPY) return false;
+    if (E.steps.size() != 1 || E.steps[0].kind != StepKind::Chain || E.input_slot.size() != 1 ||
+        E.output_slot.size() != 1)
+        return false;
+    const Step &st = E.steps[0];
+    if (st.src_slot[0] != E.input_slot[0] || st.dst_slot != E.output_slot[0]) return false;
+    void *din = mapped_host_pointer(inputs[0]), *dout = mapped_host_pointer(outputs[0]);
+    if (!din || !dout) return false;
+    ZsChainArgs c = st.chain;
+    c.src = (const uint8_t *)din;
+    c.dst = (uint8_t *)dout;
+    cudaStream_t s = exe_stream(exe);
+    check_cuda(launch_chain(c, st.chain_src_fast, st.chain_dst_fast, E.sm_count, s), st.label.c_str());
+    check_cuda(cudaStreamSynchronize(s), "synchronize");
+    return true;
+}
+
 // A lone fused colour chain is pixel local: its host round trip runs in row stripes on
 // three rotating streams, so that the upload of one stripe, the kernel of the previous and
 // the download of the one before overlap (both copy directions at once).
@@ -653,6 +687,7 @@ int zs_run_host(zs_executable *exe, const void *const *inputs, uint32_t n_inputs
         for (uint32_t i = 0; i < n_inputs; ++i) NEED(inputs[i]);
         for (uint32_t j = 0; j < n_outputs; ++j) NEED(outputs[j]);
         E.ensure_buffers();
+        if (run_host_zero_copy(exe, inputs, outputs)) return;
         if (run_host_striped(exe, inputs, outputs)) return;
         cudaStream_t s = exe_stream(exe);
         std::vector<void *> ptrs = E.dev_buffers;
