@@ -308,7 +308,9 @@ def run_ours(args, rank, world, dist):
         "config": {"workload": "fused colour chain (sRGB->XYZ D65->Bradford D50->Oklab->L*1.1,C*0.9->back->sRGB), "
                                "4096x4096 RGBA8 sRGB per GPU, seeded gradient+noise",
                    "l2": "4 rotating input/output buffer pairs (536 MB) > 129 MB L2",
-                   "parallelism": f"replicas x{world}", "graph": "CUDA graph replay"},
+                   "parallelism": f"replicas x{world}",
+                   "launch": "one kernel per step, launched directly with programmatic dependent launch "
+                             "(multi-kernel executables replay CUDA graphs)"},
         "plain_per_op_fp32": {"value": round(aggregate_mpix(world, NPX, ms_plain * 1e-3), 1), "unit": "Mpix/s",
                               "ms_per_step": round(ms_plain, 4), "kernels": plain.kernel_count()},
         "per_op_fp16": {"value": round(aggregate_mpix(world, NPX, ms_plain16 * 1e-3), 1), "unit": "Mpix/s",

@@ -724,7 +724,10 @@ int zs_run_device(zs_executable *exe, const void *const *inputs, uint32_t n_inpu
             NEED(outputs[j]);
             ptrs[E.output_slot[j]] = outputs[j];
         }
-        if (!E.use_graph) {
+        // A single kernel gains nothing from a graph; launched directly, a colour chain keeps
+        // its programmatic dependent launch across consecutive calls (its table staging
+        // overlaps the previous kernel's tail), which separate graph launches would not.
+        if (!E.use_graph || E.steps.size() == 1) {
             E.record(s, ptrs);
             return;
         }

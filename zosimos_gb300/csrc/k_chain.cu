@@ -86,14 +86,9 @@ __global__ void __launch_bounds__(ZS_CHAIN_THREADS, 2) zs_chain_srgb8_kernel(con
     const int64_t nvec = a.npx >> 2;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
     int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    // The first two vectors are requested before the tables are staged, so that their
-    // DRAM latency overlaps the table fill.
-    const bool piped = v + stride < nvec;
-    uint4 w0 = make_uint4(0, 0, 0, 0), w1 = w0;
-    if (piped) {
-        w0 = __ldcs(in + v);
-        w1 = __ldcs(in + v + stride);
-    }
+    // Programmatic dependent launch: the next launch in the stream may start as soon as this
+    // one runs; its CTAs stage their tables while this grid drains, then wait below.
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     // Tables: one 16-byte store writes four lane copies of an entry.
     for (int i = threadIdx.x; i < 256 * 8; i += blockDim.x) {
         const float d = zs_srgb_decode_lut[i >> 3];
@@ -103,6 +98,16 @@ __global__ void __launch_bounds__(ZS_CHAIN_THREADS, 2) zs_chain_srgb8_kernel(con
     for (int i = threadIdx.x; i < ZS_ENCS_ENTRIES; i += blockDim.x) {
         const uint32_t e = zs_srgb_encode_tab_shifted[i];
         reinterpret_cast<uint4 *>(sm.enc)[i] = make_uint4(e, e, e, e);
+    }
+    // Image data only after the previous grid in the stream has completed and its writes are
+    // visible (a no-op without programmatic dependent launch); the first two vectors are
+    // requested before the barrier that publishes the tables.
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    const bool piped = v + stride < nvec;
+    uint4 w0 = make_uint4(0, 0, 0, 0), w1 = w0;
+    if (piped) {
+        w0 = __ldcs(in + v);
+        w1 = __ldcs(in + v + stride);
     }
     __syncthreads();
     const int lane = threadIdx.x & 31;
@@ -170,7 +175,21 @@ static cudaError_t launch_chain_t(const ZsChainArgs &args, int sm_count, cudaStr
     const int64_t cap = (int64_t)(sm_count > 0 ? sm_count : 148) * per_sm;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
-    kernel<<<(unsigned)blocks, ZS_CHAIN_THREADS, smem, stream>>>(args);
+    // Launched with programmatic stream serialization: the table staging of this launch
+    // overlaps the tail of the previous kernel in the stream (the kernel waits for it with
+    // griddepcontrol.wait before touching image data).
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)blocks);
+    cfg.blockDim = dim3(ZS_CHAIN_THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    cudaError_t e = cudaLaunchKernelEx(&cfg, kernel, args);
+    if (e != cudaSuccess) return e;
     g_kernel_launches.fetch_add(1);
     return cudaGetLastError();
 }
