@@ -247,7 +247,7 @@ enum {
 typedef struct zs_capabilities {
     int32_t device;           /* CUDA device ordinal */
     uint32_t mode;            /* ZS_MODE_* */
-    uint32_t use_graph;       /* capture the kernel sequence as a CUDA graph and replay it */
+    uint32_t use_graph;       /* capture a multi-step kernel sequence as a CUDA graph and replay it */
     uint32_t flags;           /* ZS_CAP_* bits */
 } zs_capabilities;
 
