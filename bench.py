@@ -500,6 +500,58 @@ def workload_thumbnails(args, stream, sh):
            "speedup_vs_per_image_fused": round(per["fused"][0] / ms, 2)})
 
 
+def workload_loop(args, stream, sh):
+    """The reference's one published figure (lib/zosimos/tests/loop.rs:60-98): a 157x151 RGBA8
+    sRGB image inscribed onto a 512x512 one by a reused executable, each iteration writing both
+    pool images from host memory (uploaded at launch), binding them, stepping to the end,
+    retiring the output into the pool and reading it back to host memory.  Quoted there:
+    "around 240 fps" (2021, unstated hardware).  Seeded synthetic images of the same sizes."""
+    import time
+
+    import zosimos_gb300 as zs
+    from zosimos_gb300 import Rectangle
+    from zosimos_gb300.synthetic import srgb_gradient_noise
+    from zosimos_gb300.workloads import rgba_bytes
+    bg = rgba_bytes(srgb_gradient_noise(512, 512, seed=1, image=0))
+    fg = rgba_bytes(srgb_gradient_noise(157, 151, seed=1, image=1))
+    pool = zs.Pool()
+    kb, kf = pool.insert(zs.Descriptor.srgb_rgba8(512, 512), bg), pool.insert(zs.Descriptor.srgb_rgba8(157, 151), fg)
+    c = zs.CommandBuffer()
+    b, f = c.input(pool.descriptor(kb)), c.input(pool.descriptor(kf))
+    o, _ = c.output(c.inscribe(b, Rectangle(0, 0, 157, 151), f))
+    exe = zs.Linker.from_included().compile(c).lower_to()
+
+    def once():
+        pool.write(kb, bg)
+        pool.write(kf, fg)
+        env = exe.from_pool(pool)
+        env.bind(b, kb)
+        env.bind(f, kf)
+        x = exe.launch(env)
+        while x.is_running():
+            x.step()
+        k = x.retire_output(o)
+        out = pool.read(k)
+        pool.remove(k)
+        return out
+
+    for _ in range(max(3, args.warmup)):
+        once()
+    n = 200
+    t0 = time.perf_counter()
+    for _ in range(n):
+        once()
+    dt = (time.perf_counter() - t0) / n
+    print(json.dumps({"workload": "loop.rs: inscribe 157x151 onto 512x512 RGBA8 sRGB, reused executable, "
+                                  "host write + upload + readback per iteration",
+                      "metric": "fps", "value": round(1.0 / dt, 1), "unit": "iterations/s",
+                      "ms_per_iteration": round(dt * 1e3, 4), "iterations": n,
+                      "output_mpix_s": round(512 * 512 / dt / 1e6, 1), "kernels": exe.kernel_count(),
+                      "reference_published": {"value": 240, "unit": "fps", "hardware": "unstated (2021, wgpu/Vulkan)",
+                                              "source": "lib/zosimos/tests/loop.rs:85-86"},
+                      "ratio_vs_published": round(1.0 / dt / 240.0, 1)}), flush=True)
+
+
 def workload_layers(args, stream, sh):
     import numpy as np
 
@@ -539,7 +591,7 @@ def run_workloads(args):
     import torch
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
     stream = torch.cuda.Stream()
-    names = ["blend_resize", "resample", "thumbnails", "layers"] if args.workload == "all" else [args.workload]
+    names = ["blend_resize", "resample", "thumbnails", "layers", "loop"] if args.workload == "all" else [args.workload]
     for name in names:
         globals()["workload_" + name](args, stream, stream.cuda_stream)
 
@@ -554,7 +606,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--profile", action="store_true", help="short fixed launch sequence for ncu captures")
     ap.add_argument("--workload", default="chain",
-                    choices=["chain", "blend_resize", "resample", "thumbnails", "layers", "all"],
+                    choices=["chain", "blend_resize", "resample", "thumbnails", "layers", "loop", "all"],
                     help="chain (default) is the headline line; the others print secondary lines")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
