@@ -87,6 +87,11 @@ __device__ __forceinline__ float4 zs_src1_px(const ZsRasterArgs &a, int x, int y
 }
 
 __global__ void __launch_bounds__(256) zs_raster_kernel(const __grid_constant__ ZsRasterArgs a) {
+    // Programmatic dependent launch: let the next launch in the stream be scheduled now, and
+    // touch no global memory before the previous grid has completed and its writes are visible
+    // (griddepcontrol.wait is a no-op for an ordinary launch).
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+    asm volatile("griddepcontrol.wait;" ::: "memory");
     // Affine gathers walk 32 x 8 pixel tiles (8 x 4 per warp) so that a warp's samples
     // fall into a compact source footprint; everything else walks rows.
     const bool tiled = a.producer == ZS_PR_AFFINE;
@@ -391,7 +396,21 @@ cudaError_t launch_raster(const ZsRasterArgs &args, int sm_count, cudaStream_t s
     int64_t blocks = (n + 255) / 256;
     const int64_t cap = (int64_t)(sm_count > 0 ? sm_count : 148) * 8;
     if (blocks > cap) blocks = cap;
-    zs_raster_kernel<<<(unsigned)blocks, 256, 0, stream>>>(args);
+    // Programmatic stream serialization: this launch's CTAs may be scheduled while the previous
+    // kernel drains (they wait for it before any memory access), hiding the launch gap between
+    // the short kernels of latency-bound programs.
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)blocks);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = stream;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    attr[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const cudaError_t e = cudaLaunchKernelEx(&cfg, zs_raster_kernel, args);
+    if (e != cudaSuccess) return e;
     g_kernel_launches.fetch_add(1);
     return cudaGetLastError();
 }
