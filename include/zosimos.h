@@ -5,7 +5,7 @@
  * the zosimos project, cited per function).  The wgpu backend of the reference
  * is replaced by hand-written CUDA kernels for sm_103a; the API shape (Pool,
  * CommandBuffer, Linker/Program, Executable, Environment, Execution, Retire)
- * is kept so that a thin FFI crate can bind it.
+ * is kept so that a thin FFI crate (a Rust -sys crate) can bind it.
  *
  * Conventions
  *  - Every function returns an int status (ZS_OK = 0) unless stated otherwise;
@@ -334,11 +334,14 @@ int zs_batch_thumbnails(zs_executable *chain, const void *const *images, const u
  * zs_cmd_resize_filtered for tightly packed RGBA16F linear images, with src/dst
  * supplied by the caller and every temporary (filter tables, FP16 intermediate) kept
  * in one fixed 32 MiB device array per GPU.  Calls that need more than that array
- * (tables + dst_width * src_height * 8 bytes) return ZS_ERR_INVALID_ARG.  All calls on
- * a device share the array: calls that overlap on the GPU race, so order them on one
- * stream.  The first call on a device resolves the array's address for the current
- * device; make it before any stream capture.  filter: 0 Box, 1 Lanczos-3, 2 Triangle;
- * stream may be null (the legacy default stream). */
+ * (tables + dst_width * src_height * 8 bytes) return ZS_ERR_INVALID_ARG, and so do src or
+ * dst pointers that are not 8-byte aligned and sides above 2^24.  All calls on a device
+ * share the array: calls that overlap on the GPU race, so order them on one stream.  The
+ * first call on a device loads the array's module (the driver reserves the 32 MiB then,
+ * so that call can fail for lack of memory) and resolves the array's address for the
+ * current device: make one warm-up call at start-up, before any stream capture, and do
+ * not use this entry point across a device reset.  filter: 0 Box, 1 Lanczos-3,
+ * 2 Triangle; stream may be null (the legacy default stream). */
 int zs_resample_rgba16f_noalloc(const void *src, uint32_t src_width, uint32_t src_height, void *dst,
                                 uint32_t dst_width, uint32_t dst_height, uint32_t filter, void *stream);
 

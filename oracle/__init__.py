@@ -222,6 +222,31 @@ def affine(below, above, inverse, bilinear, f32=False):
     return below
 
 
+def affine_rows(band, y0, above, inverse, bilinear, f32=False):
+    """Rows [y0, y0 + band height) of affine(): `band` holds those rows of the full-size
+    `below` and is painted in place with the pixel centres of the full image."""
+    inv = np.ascontiguousarray(np.asarray(inverse, dtype=np.float32).reshape(9))
+    above = np.ascontiguousarray(above, dtype=_dtype(f32))
+    nh, bw = band.shape[:2]
+    ah, aw = above.shape[:2]
+    getattr(lib(), _prefix(f32) + "affine_rows")(_p(band), ctypes.c_int32(bw), ctypes.c_int32(y0),
+                                                 ctypes.c_int32(y0 + nh), _p(above), ctypes.c_int32(aw),
+                                                 ctypes.c_int32(ah), _p(inv), ctypes.c_int32(int(bilinear)))
+    return band
+
+
+def resample_rows(src, width, height, y0, y1, filt="Lanczos3", f32=False):
+    """Output rows [y0, y1) of resample(src, width, height, filt), same arithmetic."""
+    src = np.ascontiguousarray(src, dtype=_dtype(f32))
+    sh, sw = src.shape[:2]
+    out = np.empty((y1 - y0, width, 4), dtype=_dtype(f32))
+    getattr(lib(), _prefix(f32) + "resample_rows")(_p(src), ctypes.c_int32(sw), ctypes.c_int32(sh), _p(out),
+                                                   ctypes.c_int32(width), ctypes.c_int32(height),
+                                                   ctypes.c_int32(y0), ctypes.c_int32(y1),
+                                                   ctypes.c_int32(FILTER[filt] if isinstance(filt, str) else filt))
+    return out
+
+
 def resample(src, width, height, filt="Lanczos3", f32=False):
     src = np.ascontiguousarray(src, dtype=_dtype(f32))
     sh, sw = src.shape[:2]

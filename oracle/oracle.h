@@ -60,6 +60,10 @@ int zo_texel_bytes(int32_t bits);
                    int32_t ah, const float inv[9], int32_t bilinear);                      \
     void P##resample(const R *src, int32_t sw, int32_t sh, R *dst, int32_t dw,             \
                      int32_t dh, int32_t filter);                                          \
+    void P##resample_rows(const R *src, int32_t sw, int32_t sh, R *band, int32_t dw,       \
+                          int32_t dh, int32_t y0, int32_t y1, int32_t filter);             \
+    void P##affine_rows(R *band, int32_t bw, int32_t y0, int32_t y1, const R *above,       \
+                        int32_t aw, int32_t ah, const float inv[9], int32_t bilinear);     \
     void P##transfer(R *img, int64_t n, int32_t transfer, int32_t forward);                 \
     void P##box3(const R *src, int32_t w, int32_t h, R *dst, const double m[9]);
 

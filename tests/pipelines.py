@@ -268,6 +268,21 @@ def oracle_chain_linear(img, f32=False):
     return x
 
 
+def rgb_cube_image() -> np.ndarray:
+    """4096 x 4096 RGBA8 holding every RGB triple exactly once: pixel i has colour
+    (i * 0x9E3779B1) mod 2^24 (an odd multiplier permutes the 2^24 values), alpha a hash
+    of i (all 256 codes occur)."""
+    i = np.arange(1 << 24, dtype=np.uint64)
+    c = (i * np.uint64(0x9E3779B1)) & np.uint64(0xFFFFFF)
+    out = np.empty((4096, 4096, 4), dtype=np.uint8)
+    flat = out.reshape(-1, 4)
+    flat[:, 0] = (c >> np.uint64(16)).astype(np.uint8)
+    flat[:, 1] = ((c >> np.uint64(8)) & np.uint64(255)).astype(np.uint8)
+    flat[:, 2] = (c & np.uint64(255)).astype(np.uint8)
+    flat[:, 3] = ((i ^ (i >> np.uint64(9)) ^ (i >> np.uint64(17))) & np.uint64(255)).astype(np.uint8)
+    return out
+
+
 # ---------------------------------------------------------------- batched uneven thumbnails (config 4)
 
 
@@ -408,6 +423,15 @@ def ours_rotation(img16, degrees, mode=zs.Mode.Fused):
     return f16_from_bytes(run(c, pool, [(i, k)], [o], mode)[0], w, h)
 
 
+def oracle_rotation_rows(img64, degrees, y0, y1):
+    """Rows [y0, y1) of oracle_rotation (img64: the source as float64)."""
+    h, w = img64.shape[:2]
+    _, _, _, rot = rotation_cmds(w, h, degrees)
+    band = np.zeros((y1 - y0, w, 4))
+    O.affine_rows(band, y0, img64, inv3_f32(rot.transformation), True)
+    return band
+
+
 def oracle_rotation(img16, degrees):
     h, w = img16.shape[:2]
     _, _, _, rot = rotation_cmds(w, h, degrees)
@@ -436,6 +460,18 @@ def oracle_layer_stack(layers16, transforms):
     for i, (img, (deg, s)) in enumerate(zip(layers16, transforms)):
         placed = np.zeros((h, w, 4))
         O.affine(placed, img.astype(np.float64), inv3_f32(layer_affine(w, h, deg, s).transformation), True)
+        O.blend(acc, placed, (0, 0), BLEND_CYCLE[i % 4], straight=False)
+    return acc
+
+
+def oracle_layer_stack_rows(layers16, transforms, y0, y1):
+    """Rows [y0, y1) of oracle_layer_stack: each layer painted into the band with the pixel
+    centres of the full image, then blended onto the band's accumulator."""
+    h, w = layers16[0].shape[:2]
+    acc = np.zeros((y1 - y0, w, 4))
+    for i, (img, (deg, s)) in enumerate(zip(layers16, transforms)):
+        placed = np.zeros((y1 - y0, w, 4))
+        O.affine_rows(placed, y0, img.astype(np.float64), inv3_f32(layer_affine(w, h, deg, s).transformation), True)
         O.blend(acc, placed, (0, 0), BLEND_CYCLE[i % 4], straight=False)
     return acc
 

@@ -441,3 +441,79 @@ def test_distribution_normal2d(goldens, case):
         assert min(bin(int(h, 16) ^ int(a, 16)).count("1") for a in goldens["distribution_u8"]) <= 3
     else:
         assert blockhash256(luma_alpha16_to_rgba8(ours)) in goldens["distribution_" + case]
+
+
+@pytest.mark.parametrize("rect", [(100, 50, 356, 306), (0, 0, 512, 512), (17, 301, 18, 512), (200, 10, 461, 139)])
+@pytest.mark.parametrize("mode", [zs.Mode.Fused, zs.Mode.PerOpF32])
+def test_crop(background, rect, mode):
+    """CommandBuffer::crop (command.rs:971): the result keeps the source descriptor and the
+    selection is painted over it by the quad copy (copy.frag + box.vert): byte exact."""
+    pool = zs.Pool()
+    k = pool.insert_srgb(background)
+    c = zs.CommandBuffer()
+    i = c.input(pool.descriptor(k))
+    o, _ = c.output(c.crop(i, zs.Rectangle(*rect)))
+    ours = P.run(c, pool, [(i, k)], [o], mode)[0]
+    want = np.zeros((512, 512 * 4), np.uint8)
+    P.O.gather_quad(P.rgba_bytes(background), 512, 512, want, 512, 512, 4, (0, 0, 512, 512), selection=rect)
+    assert (ours == want).all()
+
+
+@pytest.mark.parametrize("size", [(384, 384), (157, 151), (1000, 700), (1, 1), (512, 3)])
+@pytest.mark.parametrize("mode", [zs.Mode.Fused, zs.Mode.PerOpF32])
+def test_resize_reference_nearest(background, size, mode):
+    """CommandBuffer::resize (command.rs:1675-1702): a bilinear coordinate grid stored as
+    truncated 8-bit texels feeding a nearest palette lookup -- an integer gather, byte exact
+    against the oracle's index tables."""
+    pool = zs.Pool()
+    k = pool.insert_srgb(background)
+    c = zs.CommandBuffer()
+    i = c.input(pool.descriptor(k))
+    o, _ = c.output(c.resize(i, size))
+    ours = P.run(c, pool, [(i, k)], [o], mode)[0]
+    ix = P.O.resize_ref_index(512, size[0])
+    iy = P.O.resize_ref_index(512, size[1])
+    assert (ours == P.rgba_bytes(background[iy][:, ix])).all()
+
+
+def test_pool_upload_device_resident_input():
+    """Pool::upload (pool.rs:292): a device-resident pool image is bound without a host
+    copy (zs_pool_device_ptr exposes it) and gives the same result as a host image."""
+    img = srgb_gradient_noise(333, 211, seed=21)
+    c, i, o = P.chain_commands(333, 211)
+    pool = zs.Pool()
+    k = pool.insert_srgb(img)
+    pool.upload(k)
+    ptr = pool.device_ptr(k)
+    assert ptr
+    # the device copy holds the image bytes
+    dev = np.empty((211, 333 * 4), np.uint8)
+    zs._check(zs._lib().zs_memcpy_d2h(dev.ctypes.data, ptr, dev.nbytes))
+    assert (dev == P.rgba_bytes(img)).all()
+    ours = P.run(c, pool, [(i, k)], [o])[0]
+    assert maxdiff(ours, P.oracle_chain(img)) <= LSB
+
+
+def test_two_chain_executables_on_the_per_device_path():
+    """Two executables whose chains use different kernel specialisations (with and without
+    cube roots), lowered for the same device and launched alternately: each launcher sets
+    its kernel's shared-memory attribute for the device current at the launch."""
+    img = srgb_gradient_noise(300, 200, seed=22)
+    c1, i1, o1 = P.chain_commands(300, 200)
+    c2 = zs.CommandBuffer()
+    j = c2.input(zs.Descriptor.srgb_rgba8(300, 200))
+    o2, _ = c2.output(c2.chromatic_adaptation(j, zs.ChromaticAdaptationMethod.BradfordVonKries,
+                                              zs.Whitepoint.D50))
+    e1 = zs.Linker.from_included().compile(c1).lower_to(zs.Capabilities(device=0))
+    e2 = zs.Linker.from_included().compile(c2).lower_to(zs.Capabilities(device=0))
+    assert "fused chain kernel" in e1.describe() and "fused chain kernel" in e2.describe()
+    out1, out2 = np.empty((200, 1200), np.uint8), np.empty((200, 1200), np.uint8)
+    for _ in range(2):
+        e1.run_host([P.rgba_bytes(img)], [out1])
+        e2.run_host([P.rgba_bytes(img)], [out2])
+    assert maxdiff(out1, P.oracle_chain(img)) <= LSB
+    lin = P.O.decode(P.O.SRGB_RGBA8, P.rgba_bytes(img), 300, 200)
+    m = (np.linalg.inv(P.O.rgb_to_xyz("Bt709", "D50")) @ P.O.adaptation("BradfordVonKries", "D65", "D50")
+         @ P.O.rgb_to_xyz())
+    P.O.mat3(lin, m)
+    assert maxdiff(out2, P.O.encode(P.O.SRGB_RGBA8, lin)) <= LSB

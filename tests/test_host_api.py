@@ -178,6 +178,14 @@ def test_noalloc_rejects_oversized_without_device():
                    ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p]
     fn.restype = ctypes.c_int32
     assert fn(ctypes.c_void_p(16), 8192, 8192, ctypes.c_void_p(16), 4096, 4096, 1, None) == 10
+    # Misaligned texel pointers and sides above 2^24 are argument errors, rejected before
+    # anything reaches a device.
+    assert fn(ctypes.c_void_p(20), 64, 64, ctypes.c_void_p(16), 32, 32, 1, None) == 10
+    assert b"aligned" in zs._lib().zs_last_error()
+    assert fn(ctypes.c_void_p(16), 64, 64, ctypes.c_void_p(17), 32, 32, 1, None) == 10
+    assert fn(ctypes.c_void_p(16), (1 << 24) + 1, 4, ctypes.c_void_p(16), 32, 4, 1, None) == 10
+    # A ratio whose filter tables alone exceed the array is rejected, not computed from garbage.
+    assert fn(ctypes.c_void_p(16), 1 << 24, 4, ctypes.c_void_p(16), 1 << 20, 4, 1, None) == 10
 
 
 def test_derivative_plan_and_unimplemented_methods():

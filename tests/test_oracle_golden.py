@@ -175,3 +175,17 @@ def test_fractal_noise_damping_sums_to_one():
         total = np.float32(total + amp)
         amp = np.float32(amp * p[3])
     assert abs(1.0 - float(total)) < 1e-6
+
+
+def test_oracle_int444i_round_trips():
+    """UInt444_ (stage.frag's Int444i): R, G, B at bits 4, 8, 12, as mux writes them
+    (stage.frag:608).  The demux reads G from bit 8 so that mux and demux invert each other;
+    stage.frag:547-548 reads bit 9, a path the reference never reaches (serialize_bits has no
+    code for the padded layouts, stage.rs:98-118)."""
+    f = O.Format(O.BITS["UInt444_"], O.PARTS["Rgb"], O.TRANSFER["Linear"], False)
+    texels = np.array([[0x0010, 0x0100, 0x1000, 0xFFF0]], dtype=np.uint16).view(np.uint8)
+    rgba = O.decode(f, texels, 4, 1).reshape(4, 4)
+    assert np.allclose(rgba[:, :3], [[1 / 15, 0, 0], [0, 1 / 15, 0], [0, 0, 1 / 15], [1, 1, 1]])
+    every = np.arange(0, 1 << 16, 16, dtype=np.uint16).reshape(1, -1)
+    back = O.encode(f, O.decode(f, every.view(np.uint8), every.shape[1], 1))
+    assert (back.view(np.uint16) == every).all()

@@ -1,5 +1,6 @@
 """The allocation-free resample entry point (zs_resample_rgba16f_noalloc), called
-through the C ABI and checked against the regular resize_filtered executable.
+through the C ABI and checked against the regular resize_filtered executable and
+against the FP64 oracle.
 
 It exists for callers that may not allocate device memory while they run; it keeps
 its filter tables and intermediate in one fixed device array.  This file is collected
@@ -38,25 +39,58 @@ def _regular(img16, out, filt):
     return P.f16_from_bytes(dst.download(np.empty((out[1], out[0] * 8), np.uint8)), *out)
 
 
-def _noalloc_call(img16, out, filt):
-    h, w = img16.shape[:2]
-    src = zs.DeviceBuffer(w * h * 8)
-    dst = zs.DeviceBuffer(out[0] * out[1] * 8)
-    src.upload(P.f16_bytes(img16))
-    rc = _noalloc()(src.ptr, w, h, dst.ptr, out[0], out[1], filt, None)
-    assert rc == 0, zs._lib().zs_last_error()
-    zs.device_synchronize()
-    return P.f16_from_bytes(dst.download(np.empty((out[1], out[0] * 8), np.uint8)), *out)
+class _Buffers:
+    """Source and destination device buffers, allocated before the calls under test."""
+
+    def __init__(self, img16, out):
+        h, w = img16.shape[:2]
+        self.w, self.h, self.out = w, h, out
+        self.src = zs.DeviceBuffer(w * h * 8)
+        self.dst = zs.DeviceBuffer(out[0] * out[1] * 8)
+        self.src.upload(P.f16_bytes(img16))
+
+    def call(self, filt, stream=None):
+        rc = _noalloc()(self.src.ptr, self.w, self.h, self.dst.ptr, self.out[0], self.out[1], filt, stream)
+        assert rc == 0, zs._lib().zs_last_error()
+
+    def result(self):
+        zs.device_synchronize()
+        return P.f16_from_bytes(self.dst.download(np.empty((self.out[1], self.out[0] * 8), np.uint8)), *self.out)
 
 
-def test_noalloc_matches_regular_entry_point_twice():
-    cases = [((1024, 768), (277, 208), zs.Filter.Lanczos3),
-             ((640, 480), (320, 240), zs.Filter.Box)]
-    for (w, h), out, filt in cases:       # two calls in a row share the scratch array
+CASES = [((1024, 768), (277, 208), zs.Filter.Lanczos3),
+         ((640, 480), (320, 240), zs.Filter.Box),
+         ((333, 250), (100, 80), zs.Filter.Triangle),
+         ((100, 80), (333, 250), zs.Filter.Lanczos3)]      # upscale: the windows do not widen
+
+
+def test_noalloc_matches_regular_entry_point_and_oracle_twice():
+    for (w, h), out, filt in CASES:
         img = linear_gradient_gauss(w, h, seed=11)
-        ours = _noalloc_call(img, out, filt)
+        bufs = _Buffers(img, out)
         ref = _regular(img, out, filt)
-        assert np.abs(ours - ref).max() <= F16_TOL
+        exact = P.oracle_resample(P.f16_from_bytes(P.f16_bytes(img), w, h), out, filt)
+        for _ in range(2):              # two calls in a row share the scratch array
+            bufs.call(filt)
+            ours = bufs.result()
+            assert np.abs(ours - ref).max() <= F16_TOL
+            assert np.abs(ours - exact).max() <= F16_TOL
+
+
+def test_noalloc_allocates_nothing_and_runs_on_a_stream():
+    import torch
+    img = linear_gradient_gauss(512, 384, seed=12)
+    bufs = _Buffers(img, (200, 150))
+    bufs.call(zs.Filter.Lanczos3)       # warm-up: loads the module, reserves the fixed array
+    zs.device_synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    stream = torch.cuda.Stream()
+    bufs.call(zs.Filter.Lanczos3, ctypes.c_void_p(stream.cuda_stream))
+    stream.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    exact = P.oracle_resample(P.f16_from_bytes(P.f16_bytes(img), 512, 384), (200, 150), zs.Filter.Lanczos3)
+    assert np.abs(bufs.result() - exact).max() <= F16_TOL
 
 
 def test_noalloc_rejects_oversized_requests():

@@ -738,6 +738,29 @@ class DeviceBuffer:
         self.free()
 
 
+class PinnedBuffer:
+    """Page-locked, device-mapped host memory (zs_host_alloc) viewed as a numpy array;
+    Executable.run_host streams such buffers directly where the plan allows it."""
+
+    def __init__(self, shape, dtype=np.uint8):
+        dt = np.dtype(dtype)
+        self.nbytes = int(np.prod(shape)) * dt.itemsize
+        self.ptr = _lib().zs_host_alloc(self.nbytes)
+        if not self.ptr:
+            raise ZosimosError(11, f"pinned host allocation of {self.nbytes} bytes failed")
+        buf = (ctypes.c_uint8 * self.nbytes).from_address(self.ptr)
+        self.array = np.frombuffer(buf, dtype=dt).reshape(shape)
+
+    def free(self) -> None:
+        if self.ptr:
+            self.array = None
+            _lib().zs_host_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        self.free()
+
+
 def device_synchronize() -> None:
     _check(_lib().zs_device_synchronize())
 

@@ -42,6 +42,27 @@ def _deps():
     return out
 
 
+SYNTH_SRC = os.path.join(HERE, "synth", "zs_synth.c")
+SYNTH_LIB = os.path.join(BUILD, "libzs_synth.so")
+
+
+def build_synth() -> str:
+    """The host-side generator of seeded synthetic inputs (bench and tests only)."""
+    if os.path.exists(SYNTH_LIB) and os.path.getmtime(SYNTH_LIB) >= os.path.getmtime(SYNTH_SRC):
+        return SYNTH_LIB
+    os.makedirs(BUILD, exist_ok=True)
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        raise RuntimeError("no C compiler for the synthetic-input generator")
+    tmp = SYNTH_LIB + ".tmp"
+    r = subprocess.run([cc, "-O2", "-fopenmp", "-ffp-contract=off", "-fPIC", "-shared", "-o", tmp, SYNTH_SRC, "-lm"],
+                       capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("synthetic generator build failed\n" + r.stdout + r.stderr)
+    os.replace(tmp, SYNTH_LIB)
+    return SYNTH_LIB
+
+
 def _stale() -> bool:
     if not os.path.exists(LIB):
         return True
@@ -50,6 +71,7 @@ def _stale() -> bool:
 
 
 def build(force: bool = False, verbose: bool = False) -> str:
+    build_synth()
     if not force and not _stale():
         return LIB
     os.makedirs(BUILD, exist_ok=True)

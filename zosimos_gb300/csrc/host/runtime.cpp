@@ -87,7 +87,25 @@ void Executable::record(cudaStream_t stream, const std::vector<void *> &ptrs) {
     record_range(stream, ptrs, 0, steps.size());
 }
 
+// Launches go to the executable's device whatever device the caller has current; the
+// caller's current device is restored afterwards.
+struct DeviceScope {
+    int prev = -1;
+    explicit DeviceScope(int device) {
+        if (cudaGetDevice(&prev) != cudaSuccess) {
+            cudaGetLastError();
+            prev = -1;
+        }
+        if (prev != device) check_cuda(cudaSetDevice(device), "cudaSetDevice");
+    }
+    ~DeviceScope() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
 void Executable::record_range(cudaStream_t stream, const std::vector<void *> &ptrs, size_t begin, size_t end) {
+    DeviceScope scope(device);
     for (size_t k = begin; k < end && k < steps.size(); ++k) {
         const Step &st = steps[k];
         switch (st.kind) {

@@ -162,13 +162,21 @@ template <bool CBRT, bool CUBE, bool CLAMP, bool NONNEG>
 static cudaError_t launch_chain_t(const ZsChainArgs &args, int sm_count, cudaStream_t stream) {
     auto kernel = zs_chain_srgb8_kernel<CBRT, CUBE, CLAMP, NONNEG>;
     const size_t smem = sizeof(ZsChainSmem);
-    static int per_sm = 0;
+    // The shared-memory opt-in is a per-device attribute of the kernel: set it (and size the
+    // grid) once per device, on the device that is current for this launch.
+    static std::atomic<int> per_sm_of[ZS_MAX_DEVICES];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= ZS_MAX_DEVICES) return cudaErrorInvalidDevice;
+    int per_sm = per_sm_of[dev].load();
     if (per_sm == 0) {
-        cudaError_t e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, ZS_CHAIN_THREADS, smem);
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
+        per_sm_of[dev].store(per_sm);
     }
     const int64_t nvec = (args.npx + 3) / 4;
     int64_t blocks = (nvec + ZS_CHAIN_THREADS - 1) / ZS_CHAIN_THREADS;
@@ -188,7 +196,7 @@ static cudaError_t launch_chain_t(const ZsChainArgs &args, int sm_count, cudaStr
     attr[0].val.programmaticStreamSerializationAllowed = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    cudaError_t e = cudaLaunchKernelEx(&cfg, kernel, args);
+    e = cudaLaunchKernelEx(&cfg, kernel, args);
     if (e != cudaSuccess) return e;
     g_kernel_launches.fetch_add(1);
     return cudaGetLastError();

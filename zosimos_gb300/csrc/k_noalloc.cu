@@ -16,8 +16,14 @@
 // FP64, stored as FP32 -- the same rule the host planner uses.
 //
 // Limits and sharing:
-//  * the scratch array holds ZS_NOALLOC_SCRATCH_BYTES (32 MiB) on every GPU that loads
-//    this library, for the life of the process;
+//  * the scratch array holds ZS_NOALLOC_SCRATCH_BYTES (32 MiB) per GPU.  With CUDA's lazy
+//    module loading (the default) the driver reserves it when this file's module is first
+//    used on a device -- at the first call of this entry point there -- and keeps it until
+//    the process exits, so the first call may itself fail with an out-of-memory error.
+//    Callers with a fixed device budget make one small warm-up call at start-up, outside
+//    any stream capture, and count the 32 MiB in their budget;
+//  * src and dst must be 8-byte aligned (the kernels move whole RGBA16F texels), and
+//    widths and heights at most ZS_NOALLOC_MAX_SIDE;
 //  * a call is rejected (ZS_ERR_INVALID_ARG, with the reason in zs_last_error) when its
 //    tables plus the dst_width x src_height x 8-byte intermediate do not fit;
 //  * every call on a device uses the same array and leaves its contents behind; nothing
@@ -25,8 +31,9 @@
 //  * calls whose work overlaps on the GPU (e.g. issued on different streams without an
 //    ordering between them) race on the array: order them on one stream or serialise them.
 //  * the first call on a device looks up the array's device address
-//    (cudaGetSymbolAddress, with that device current); make that first call before any
-//    stream capture begins.
+//    (cudaGetSymbolAddress, with that device current) and keeps it for the life of the
+//    process; make that first call before any stream capture begins, and do not use this
+//    entry point across a reset of the device (cudaDeviceReset), which unloads the module.
 #include <math.h>
 
 #include <cstring>
@@ -39,6 +46,7 @@
 
 #define ZS_NOALLOC_SCRATCH_BYTES (32u << 20)
 #define ZS_NOALLOC_MAX_DEVICES 64
+#define ZS_NOALLOC_MAX_SIDE (1u << 24)
 
 static __device__ __align__(256) unsigned char zs_noalloc_scratch[ZS_NOALLOC_SCRATCH_BYTES];
 
@@ -129,10 +137,12 @@ void *g_noalloc_ptr[ZS_NOALLOC_MAX_DEVICES] = {nullptr};
 
 size_t align256(size_t v) { return (v + 255) & ~(size_t)255; }
 
-int taps_for(uint32_t src, uint32_t dst, uint32_t filter) {
+// Taps per output pixel of one axis (the host planner's rule); sides are bounded by
+// ZS_NOALLOC_MAX_SIDE, so the count fits easily in 64 bits.
+int64_t taps_for(uint32_t src, uint32_t dst, uint32_t filter) {
     const double s = (double)src / (double)dst, f = s > 1.0 ? s : 1.0;
     const double R = filter == 1 ? 3.0 : (filter == 2 ? 1.0 : 0.5);
-    return (int)ceil(2.0 * R * f) + 2;
+    return (int64_t)ceil(2.0 * R * f) + 2;
 }
 
 }  // namespace
@@ -145,7 +155,23 @@ extern "C" int zs_resample_rgba16f_noalloc(const void *src, uint32_t src_width, 
         set_last_error("zs_resample_rgba16f_noalloc: null buffer, empty size or unknown filter");
         return ZS_ERR_INVALID_ARG;
     }
-    const int tx = taps_for(src_width, dst_width, filter), ty = taps_for(src_height, dst_height, filter);
+    if (src_width > ZS_NOALLOC_MAX_SIDE || src_height > ZS_NOALLOC_MAX_SIDE || dst_width > ZS_NOALLOC_MAX_SIDE ||
+        dst_height > ZS_NOALLOC_MAX_SIDE) {
+        set_last_error("zs_resample_rgba16f_noalloc: a width or height exceeds " +
+                       std::to_string((unsigned)ZS_NOALLOC_MAX_SIDE));
+        return ZS_ERR_INVALID_ARG;
+    }
+    if (((uintptr_t)src | (uintptr_t)dst) & 7u) {
+        set_last_error("zs_resample_rgba16f_noalloc: src and dst must be 8-byte aligned (whole RGBA16F texels)");
+        return ZS_ERR_INVALID_ARG;
+    }
+    const int64_t tx = taps_for(src_width, dst_width, filter), ty = taps_for(src_height, dst_height, filter);
+    if (4ull * (uint64_t)dst_width * (uint64_t)tx > ZS_NOALLOC_SCRATCH_BYTES ||
+        4ull * (uint64_t)dst_height * (uint64_t)ty > ZS_NOALLOC_SCRATCH_BYTES) {
+        set_last_error("zs_resample_rgba16f_noalloc: the filter tables alone need more scratch than the fixed " +
+                       std::to_string((size_t)ZS_NOALLOC_SCRATCH_BYTES) + " bytes");
+        return ZS_ERR_INVALID_ARG;
+    }
     // Scratch layout: [first_x count_x weights_x][first_y count_y weights_y][intermediate]
     const size_t fx = 0, cx = align256(fx + 4ull * dst_width), wx = align256(cx + 4ull * dst_width);
     const size_t fy = align256(wx + 4ull * dst_width * tx), cy = align256(fy + 4ull * dst_height);
@@ -183,9 +209,9 @@ extern "C" int zs_resample_rgba16f_noalloc(const void *src, uint32_t src_width, 
     int32_t *first_y = (int32_t *)(base + fy), *count_y = (int32_t *)(base + cy);
     float *w_x = (float *)(base + wx), *w_y = (float *)(base + wy);
     zs_noalloc_weights_kernel<<<(dst_width + 127) / 128, 128, 0, s>>>((int)src_width, (int)dst_width, (int)filter,
-                                                                       tx, first_x, count_x, w_x);
+                                                                       (int)tx, first_x, count_x, w_x);
     zs_noalloc_weights_kernel<<<(dst_height + 127) / 128, 128, 0, s>>>((int)src_height, (int)dst_height, (int)filter,
-                                                                        ty, first_y, count_y, w_y);
+                                                                        (int)ty, first_y, count_y, w_y);
     e = cudaGetLastError();
     if (e != cudaSuccess) {
         set_last_error(std::string("zs_resample_rgba16f_noalloc: ") + cudaGetErrorString(e));
@@ -216,7 +242,7 @@ extern "C" int zs_resample_rgba16f_noalloc(const void *src, uint32_t src_width, 
     a.index_x = first_x;
     a.index_y = count_x;
     a.weights = w_x;
-    a.taps = tx;
+    a.taps = (int32_t)tx;
     a.dst = base + mid;
     a.dst_stride = 8ll * dst_width;
     a.width = (int)dst_width;
@@ -232,7 +258,7 @@ extern "C" int zs_resample_rgba16f_noalloc(const void *src, uint32_t src_width, 
         a.index_x = first_y;
         a.index_y = count_y;
         a.weights = w_y;
-        a.taps = ty;
+        a.taps = (int32_t)ty;
         a.dst = (uint8_t *)dst;
         a.dst_stride = 8ll * dst_width;
         a.height = (int)dst_height;

@@ -14,6 +14,8 @@
 #define ZS_MAX_PARAMS 320
 #define ZS_MAX_FMTS 8
 #define ZS_MAX_SRCS 3
+// Device ordinals with per-device launcher state (kernel attributes, tables).
+#define ZS_MAX_DEVICES 64
 
 // Storage format of one register (what lib/zosimos/src/program.rs:781-946 derives from a
 // Descriptor).  `fast` selects a specialised decode/encode path.

@@ -6,7 +6,29 @@ any machine.
 """
 from __future__ import annotations
 
+import ctypes
+import os
+
 import numpy as np
+
+_SYNTH = os.path.join(os.path.dirname(os.path.abspath(__file__)), "_build", "libzs_synth.so")
+_synth_lib = None
+
+
+def _c():
+    """The OpenMP C generator (synth/zs_synth.c, built by build.py) when it is built, else
+    None (the numpy forms below then compute the same values, more slowly)."""
+    global _synth_lib
+    if _synth_lib is None:
+        if not os.path.exists(_SYNTH):
+            return None
+        lib = ctypes.CDLL(_SYNTH)
+        i32, p = ctypes.c_int32, ctypes.c_void_p
+        lib.zs_synth_srgb_gradient_noise.argtypes = [i32, i32, i32, i32, i32, i32, p]
+        lib.zs_synth_linear_gradient_gauss.argtypes = [i32, i32, i32, i32, ctypes.c_double, p]
+        lib.zs_synth_premultiplied_layer.argtypes = [i32, i32, i32, i32, i32, p]
+        _synth_lib = lib
+    return _synth_lib
 
 _M1 = np.uint64(0xBF58476D1CE4E5B9)
 _M2 = np.uint64(0x94D049BB133111EB)
@@ -30,6 +52,11 @@ def srgb_gradient_noise(width: int, height: int, seed: int = 1, image: int = 0, 
                         random_alpha: bool = True) -> np.ndarray:
     """RGBA8 sRGB: R = x ramp, G = y ramp, B = diagonal ramp, plus uniform integer noise
     in [-noise, noise] (clamped), alpha uniform in [0, 255] (or opaque)."""
+    lib = _c()
+    if lib is not None:
+        out = np.empty((height, width, 4), dtype=np.uint8)
+        lib.zs_synth_srgb_gradient_noise(width, height, seed, image, noise, int(random_alpha), out.ctypes.data)
+        return out
     y, x = np.mgrid[0:height, 0:width]
     r = np.rint(255.0 * x / max(width - 1, 1))
     g = np.rint(255.0 * y / max(height - 1, 1))
@@ -51,6 +78,11 @@ def linear_gradient_gauss(width: int, height: int, seed: int = 3, image: int = 0
                           dtype=np.float16) -> np.ndarray:
     """Linear RGBA: gradient ramps plus Gaussian noise (Box-Muller on splitmix64),
     clamped to [0, 1], alpha 1."""
+    lib = _c()
+    if lib is not None and dtype == np.float16:
+        out = np.empty((height, width, 4), dtype=np.float16)
+        lib.zs_synth_linear_gradient_gauss(width, height, seed, image, sigma, out.ctypes.data)
+        return out
     y, x = np.mgrid[0:height, 0:width].astype(np.float64)
     base = [x / max(width - 1, 1), y / max(height - 1, 1), (x + y) / max(width + height - 2, 1)]
     n = width * height
@@ -75,6 +107,11 @@ def premultiplied_layer(width: int, height: int, seed: int = 5, image: int = 0, 
                         dtype=np.float16) -> np.ndarray:
     """Premultiplied linear RGBA: gradient + Gaussian-noise colour, alpha = clamped sum of
     2D Gaussian blobs (sigma in [128, 768] px at 4096 px, scaled with the image)."""
+    lib = _c()
+    if lib is not None and dtype == np.float16:
+        out = np.empty((height, width, 4), dtype=np.float16)
+        lib.zs_synth_premultiplied_layer(width, height, seed, image, blobs, out.ctypes.data)
+        return out
     rgb = linear_gradient_gauss(width, height, seed=seed, image=image, dtype=np.float64)
     u = _uniform(seed, image ^ 0x8000, 4 * blobs, 7)
     y, x = np.mgrid[0:height, 0:width].astype(np.float64)
