@@ -81,12 +81,16 @@ def test_noalloc_allocates_nothing_and_runs_on_a_stream():
     import torch
     img = linear_gradient_gauss(512, 384, seed=12)
     bufs = _Buffers(img, (200, 150))
+    stream = torch.cuda.Stream()        # the caller's stream exists before the calls under test
+    handle = ctypes.c_void_p(stream.cuda_stream)
     bufs.call(zs.Filter.Lanczos3)       # warm-up: loads the module, reserves the fixed array
+    bufs.call(zs.Filter.Lanczos3, handle)
     zs.device_synchronize()
     free0, _ = torch.cuda.mem_get_info()
-    stream = torch.cuda.Stream()
-    bufs.call(zs.Filter.Lanczos3, ctypes.c_void_p(stream.cuda_stream))
-    stream.synchronize()
+    for _ in range(3):
+        bufs.call(zs.Filter.Lanczos3, handle)
+        bufs.call(zs.Filter.Box)
+    zs.device_synchronize()
     free1, _ = torch.cuda.mem_get_info()
     assert free1 == free0
     exact = P.oracle_resample(P.f16_from_bytes(P.f16_bytes(img), 512, 384), (200, 150), zs.Filter.Lanczos3)
