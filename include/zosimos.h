@@ -304,7 +304,10 @@ void zs_exec_free(zs_execution *exec);
  * kernel and download overlap on three streams. */
 int zs_run_host(zs_executable *exe, const void *const *inputs, uint32_t n_inputs,
                 void *const *outputs, uint32_t n_outputs);
-/* Same, with device-resident inputs and outputs (no host copies). */
+/* Same, with device-resident inputs and outputs (no host copies).  Each buffer must start
+ * on its texel's natural alignment (the largest power of two dividing the texel size, at
+ * most 16 bytes), else ZS_ERR_INVALID_ARG; a colour chain on 16-byte aligned buffers runs
+ * on the chain kernel, on others on the generic raster kernel. */
 int zs_run_device(zs_executable *exe, const void *const *inputs, uint32_t n_inputs,
                   void *const *outputs, uint32_t n_outputs, void *stream);
 /* Pinned host memory helpers. */

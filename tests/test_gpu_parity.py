@@ -517,3 +517,24 @@ def test_two_chain_executables_on_the_per_device_path():
          @ P.O.rgb_to_xyz())
     P.O.mat3(lin, m)
     assert maxdiff(out2, P.O.encode(P.O.SRGB_RGBA8, lin)) <= LSB
+
+
+def test_chain_on_buffers_not_16_byte_aligned():
+    """Texel-aligned buffers that the chain kernel cannot stream in 16-byte vectors run the
+    same fused program on the generic raster kernel; buffers not even texel aligned are an
+    argument error, raised before anything is launched."""
+    img = srgb_gradient_noise(123, 77, seed=23)
+    c, _, _ = P.chain_commands(123, 77)
+    exe = zs.Linker.from_included().compile(c).lower_to()
+    n = img.nbytes
+    src, dst = zs.DeviceBuffer(n + 64), zs.DeviceBuffer(n + 64)
+    host = np.zeros(n + 64, np.uint8)
+    host[4:4 + n] = P.rgba_bytes(img).reshape(-1)
+    src.upload(host)
+    exe.run_device([src.ptr + 4], [dst.ptr + 4])
+    zs.device_synchronize()
+    out = dst.download(np.empty(n + 64, np.uint8))[4:4 + n].reshape(77, 123 * 4)
+    assert maxdiff(out, P.oracle_chain(img)) <= LSB
+    with pytest.raises(zs.ZosimosError) as err:
+        exe.run_device([src.ptr + 1], [dst.ptr])
+    assert err.value.code == 10

@@ -42,6 +42,8 @@ def test_colour_chain_fuses_to_one_kernel():
     c, _, _ = color_chain(4096, 4096)
     fused = lower(c)
     assert fused.kernel_count() == 1 and "fused chain kernel" in fused.describe()
+    # the Oklab L/C scaling between cube root and cube is detected as d I + (1,1,1)^T v
+    assert "rank-1 L/C scaling" in fused.describe()
     assert lower(c, zs.Mode.PerOpF32).kernel_count() == 7
     assert lower(c, zs.Mode.PerOpF16).kernel_count() == 7
 

@@ -716,12 +716,21 @@ int zs_run_device(zs_executable *exe, const void *const *inputs, uint32_t n_inpu
         E.ensure_buffers();
         cudaStream_t s = stream ? (cudaStream_t)stream : exe_stream(exe);
         std::vector<void *> ptrs = E.dev_buffers;
+        // Kernels read and write whole texels: a buffer must start on its texel's natural
+        // alignment (the largest power of two dividing the texel size, at most 16 bytes).
+        auto aligned = [&](const void *p, int slot) {
+            const uint32_t bpp = E.slots[slot].fmt.bpp;
+            const uintptr_t a = bpp >= 16 ? 16 : (bpp & 7) == 0 ? 8 : (bpp & 3) == 0 ? 4 : (bpp & 1) == 0 ? 2 : 1;
+            return ((uintptr_t)p & (a - 1)) == 0;
+        };
         for (uint32_t i = 0; i < n_inputs; ++i) {
             NEED(inputs[i]);
+            if (!aligned(inputs[i], E.input_slot[i])) fail(ZS_ERR_INVALID_ARG, "input buffer is not texel aligned");
             ptrs[E.input_slot[i]] = const_cast<void *>(inputs[i]);
         }
         for (uint32_t j = 0; j < n_outputs; ++j) {
             NEED(outputs[j]);
+            if (!aligned(outputs[j], E.output_slot[j])) fail(ZS_ERR_INVALID_ARG, "output buffer is not texel aligned");
             ptrs[E.output_slot[j]] = outputs[j];
         }
         // A single kernel gains nothing from a graph; launched directly, a colour chain keeps

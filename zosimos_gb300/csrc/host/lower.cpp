@@ -271,29 +271,43 @@ struct Planner {
             }
             st.raster.raw_copy = same ? 1 : 0;
         }
-        try_chain(st);
+        try_chain(st, p.prog);
         E.steps.push_back(st);
     }
 
+    // M == d I + (1,1,1)^T v (every row of M - d I equal), the middle matrix of an Oklab L/C
+    // scaling: M2^-1 diag(sL, sC, sC) M2 = sC I + (sL - sC) M2^-1 e1 (row 0 of M2), and
+    // M2^-1 e1 = (1, 1, 1).  Checked in FP64 against the matrix's own scale.
+    static bool rank1_middle(const Mat3 &m, double &d, double v[3]) {
+        double scale = 0.0;
+        for (double x : m.m) scale = std::max(scale, std::fabs(x));
+        if (scale == 0.0) return false;
+        d = m.m[0] - m.m[3];
+        for (int j = 0; j < 3; ++j) {
+            double col[3];
+            for (int i = 0; i < 3; ++i) col[i] = m.m[3 * i + j] - (i == j ? d : 0.0);
+            if (std::fabs(col[0] - col[1]) > 1e-12 * scale || std::fabs(col[0] - col[2]) > 1e-12 * scale) return false;
+            v[j] = (col[0] + col[1] + col[2]) / 3.0;
+        }
+        return true;
+    }
+
     // The canonical colour chain: [M] [cbrt [M]] [cube [M]] [clamp [M]], RGBA8 sRGB in/out.
-    void try_chain(Step &st) {
+    // `hp` is the FP64 form of the launch's pixel program (the matrices before rounding).
+    void try_chain(Step &st, const HProgram &hp) {
         if (E.mode != ZS_MODE_FUSED) return;
         const ZsRasterArgs &a = st.raster;
         if (a.producer != ZS_PR_LOAD || a.nsrc != 1) return;
         if (a.src[0].fmt.fast != ZS_FAST_RGBA8_SRGB || a.dst_fmt.fast != ZS_FAST_RGBA8_SRGB) return;
-        const ZsPixelProgram &pp = a.prog;
         ZsChainArgs c;
         std::memset(&c, 0, sizeof(c));
-        for (int k = 0; k < 4; ++k) {
-            c.m[k][0] = c.m[k][4] = c.m[k][8] = 1.0f;
-        }
+        Mat3 mats[4] = {Mat3::identity(), Mat3::identity(), Mat3::identity(), Mat3::identity()};
         int stage = 0;   // 0: before cbrt (M_a), 1: M_b, 2: M_c, 3: M_d
-        for (int i = 0; i < pp.n; ++i) {
-            const ZsPInstr &o = pp.ins[i];
+        for (const HInstr &o : hp.ins) {
             if (o.op == ZS_P_MAT3) {
                 // two matrices in one stage cannot happen after optimise(); guard anyway
                 if (c.flags & (ZS_CHAIN_MA << stage)) return;
-                for (int k = 0; k < 9; ++k) c.m[stage][k] = pp.prm[o.p + k];
+                mats[stage] = o.mat;
                 c.flags |= ZS_CHAIN_MA << stage;
             } else if (o.op == ZS_P_CBRT && stage < 1) {
                 stage = 1;
@@ -309,19 +323,27 @@ struct Planner {
             }
         }
         if (a.src[0].width != a.width || a.src[0].height != a.height) return;
+        for (int s = 0; s < 4; ++s)
+            for (int k = 0; k < 9; ++k) c.m[s][k] = (float)mats[s].m[k];
         c.npx = (int64_t)a.width * a.height;
         // Decoded sRGB8 values are in [0, 1]; a non-negative M_a keeps the cube-root
         // arguments non-negative, so the kernel may skip the sign handling.
         bool nonneg = true;
         for (int k = 0; k < 9; ++k) nonneg = nonneg && c.m[0][k] >= 0.0f;
         if (nonneg) c.flags |= ZS_CHAIN_CBRT_NONNEG;
+        double d, v[3];
+        if ((c.flags & ZS_CHAIN_CBRT) && (c.flags & ZS_CHAIN_CUBE) && rank1_middle(mats[1], d, v)) {
+            c.flags |= ZS_CHAIN_MB_RANK1;
+            for (int j = 0; j < 3; ++j) c.mb_v[j][0] = c.mb_v[j][1] = (float)v[j];
+            c.mb_d[0] = c.mb_d[1] = (float)d;
+        }
         for (int s = 0; s < 4; ++s)
             for (int k = 0; k < 9; ++k) c.m2[s][k][0] = c.m2[s][k][1] = c.m[s][k];
         st.kind = StepKind::Chain;
         st.chain = c;
         st.chain_src_fast = ZS_FAST_RGBA8_SRGB;
         st.chain_dst_fast = ZS_FAST_RGBA8_SRGB;
-        st.label += " [fused chain kernel]";
+        st.label += (c.flags & ZS_CHAIN_MB_RANK1) ? " [fused chain kernel, rank-1 L/C scaling]" : " [fused chain kernel]";
     }
 
     void materialize(uint32_t reg) {

@@ -87,6 +87,25 @@ void Executable::record(cudaStream_t stream, const std::vector<void *> &ptrs) {
     record_range(stream, ptrs, 0, steps.size());
 }
 
+// The raster arguments of a step with this launch's buffer pointers filled in.
+static ZsRasterArgs raster_args(const Step &st, const std::vector<void *> &ptrs) {
+    ZsRasterArgs a = st.raster;
+    for (int i = 0; i < ZS_MAX_SRCS; ++i)
+        a.src[i].ptr = st.src_slot[i] >= 0 ? (const uint8_t *)ptrs[st.src_slot[i]] : nullptr;
+    a.dst = (uint8_t *)ptrs[st.dst_slot];
+    a.index_x = st.idx_x_slot >= 0 ? (const int32_t *)ptrs[st.idx_x_slot] : nullptr;
+    a.index_y = st.idx_y_slot >= 0 ? (const int32_t *)ptrs[st.idx_y_slot] : nullptr;
+    a.weights = st.weight_slot >= 0 ? (const float *)ptrs[st.weight_slot] : nullptr;
+    a.vfirst = st.vfirst_slot >= 0 ? (const int32_t *)ptrs[st.vfirst_slot] : nullptr;
+    a.vcount = st.vcount_slot >= 0 ? (const int32_t *)ptrs[st.vcount_slot] : nullptr;
+    a.vweights = st.vweight_slot >= 0 ? (const float *)ptrs[st.vweight_slot] : nullptr;
+    a.vimg = st.vimg_slot >= 0 ? (const uint8_t *)ptrs[st.vimg_slot] : nullptr;
+    a.vimg_index = st.vimg_index_slot >= 0 ? (const int32_t *)ptrs[st.vimg_index_slot] : nullptr;
+    for (int i = 0; i < 2; ++i)
+        a.vsrc[i].ptr = st.vsrc_slot[i] >= 0 ? (const uint8_t *)ptrs[st.vsrc_slot[i]] : nullptr;
+    return a;
+}
+
 // Launches go to the executable's device whatever device the caller has current; the
 // caller's current device is restored afterwards.
 struct DeviceScope {
@@ -132,25 +151,19 @@ void Executable::record_range(cudaStream_t stream, const std::vector<void *> &pt
             ZsChainArgs c = st.chain;
             c.src = (const uint8_t *)ptrs[st.src_slot[0]];
             c.dst = (uint8_t *)ptrs[st.dst_slot];
-            check_cuda(launch_chain(c, st.chain_src_fast, st.chain_dst_fast, sm_count, stream), st.label.c_str());
+            const cudaError_t e = launch_chain(c, st.chain_src_fast, st.chain_dst_fast, sm_count, stream);
+            if (e != cudaErrorNotSupported) {
+                check_cuda(e, st.label.c_str());
+                break;
+            }
+            // Buffers the chain kernel cannot stream (not 16-byte aligned): the same fused
+            // program on the generic raster kernel.
+            cudaGetLastError();
+            check_cuda(launch_raster(raster_args(st, ptrs), sm_count, stream), st.label.c_str());
         } break;
-        case StepKind::Raster: {
-            ZsRasterArgs a = st.raster;
-            for (int i = 0; i < ZS_MAX_SRCS; ++i)
-                a.src[i].ptr = st.src_slot[i] >= 0 ? (const uint8_t *)ptrs[st.src_slot[i]] : nullptr;
-            a.dst = (uint8_t *)ptrs[st.dst_slot];
-            a.index_x = st.idx_x_slot >= 0 ? (const int32_t *)ptrs[st.idx_x_slot] : nullptr;
-            a.index_y = st.idx_y_slot >= 0 ? (const int32_t *)ptrs[st.idx_y_slot] : nullptr;
-            a.weights = st.weight_slot >= 0 ? (const float *)ptrs[st.weight_slot] : nullptr;
-            a.vfirst = st.vfirst_slot >= 0 ? (const int32_t *)ptrs[st.vfirst_slot] : nullptr;
-            a.vcount = st.vcount_slot >= 0 ? (const int32_t *)ptrs[st.vcount_slot] : nullptr;
-            a.vweights = st.vweight_slot >= 0 ? (const float *)ptrs[st.vweight_slot] : nullptr;
-            a.vimg = st.vimg_slot >= 0 ? (const uint8_t *)ptrs[st.vimg_slot] : nullptr;
-            a.vimg_index = st.vimg_index_slot >= 0 ? (const int32_t *)ptrs[st.vimg_index_slot] : nullptr;
-            for (int i = 0; i < 2; ++i)
-                a.vsrc[i].ptr = st.vsrc_slot[i] >= 0 ? (const uint8_t *)ptrs[st.vsrc_slot[i]] : nullptr;
-            check_cuda(launch_raster(a, sm_count, stream), st.label.c_str());
-        } break;
+        case StepKind::Raster:
+            check_cuda(launch_raster(raster_args(st, ptrs), sm_count, stream), st.label.c_str());
+            break;
         }
     }
 }

@@ -9,21 +9,24 @@
 // every pass (lib/zosimos/src/program.rs:1486-1533), this is one HBM pass:
 // 4 bytes read and 4 bytes written per pixel.
 //
-// The chain is issue-bound on GB300 rather than HBM-bound (about 60 instructions per
+// The chain is issue-bound on GB300 rather than HBM-bound (about 58 instructions per
 // 8 bytes moved), so the data path is built to minimise instructions per pixel:
 //  * 16-byte coalesced streaming loads/stores; two vectors (8 pixels) computed while the
-//    next two are in flight (software pipeline), 512-thread blocks, two per SM;
+//    next two are in flight (software pipeline); one 1024-thread block per SM, so the
+//    replicated tables fit beside each other;
 //  * sRGB decode from a lane-replicated shared table (lane l reads column l: no bank
 //    conflicts whatever the data);
 //  * pixels processed in pairs with packed FP32x2 FMA (one instruction, two pixels),
 //    the matrix coefficients read as 64-bit constant operands;
 //  * cube roots as ex2(lg2(x)/3) on the MUFU pipe (the sign fix-up is dropped when the
 //    host proves M_a keeps [0,1]^3 non-negative);
+//  * an Oklab L/C scaling between the cube root and the cube (M_b = d I + (1,1,1)^T v,
+//    detected on the host in FP64) costs 6 FMAs instead of 9;
 //  * clamps folded into the last FMA of each matrix row (fma.sat on the FMA pipe), the
 //    encode shift added to a pixel pair by one packed add;
-//  * the first loads issued before the shared tables are staged;
-//  * exact round-to-nearest sRGB encode from a bucketed threshold table replicated 4x
-//    across lanes (entry + float bits carries the code into byte 3), packed with PRMT;
+//  * exact round-to-nearest sRGB encode from a bucketed threshold table replicated 8x
+//    across lanes (entry + float bits carries the code into byte 3): one shift, one
+//    shift-add, one shared load and one add per channel, packed with PRMT;
 //  * alpha bytes passed through (unorm8 alpha decode + encode is the identity).
 #include <atomic>
 
@@ -31,19 +34,18 @@
 #include "zs_device.cuh"
 #include "zs_kernels.h"
 
-#define ZS_CHAIN_THREADS 512
+#define ZS_CHAIN_THREADS 1024
 
 // Decode rows are 256 bytes apart so that the byte offset of (code, lane) is
 // (code << 8) | (lane << 2): one PRMT builds it from the packed texel.
 struct ZsChainSmem {
     float lut[256 * 64];                         // [code][lane], lanes 32..63 unused
-    uint32_t enc[ZS_ENCS_ENTRIES * ZS_ENC_REP];   // [bucket][lane & 3], shifted domain
+    uint32_t enc[ZS_ENCS_ENTRIES * ZS_ENC_REP];   // [bucket][lane & 7], shifted domain
 };
 
-template <bool CBRT, bool CUBE, bool CLAMP, bool NONNEG>
+template <bool CBRT, bool CUBE, bool CLAMP, bool NONNEG, bool RANK1>
 __device__ __forceinline__ void zs_chain_pair(uint32_t &wp, uint32_t &wq, const unsigned char *lut,
-                                              uint32_t lane4, const uint32_t *enc_lane,
-                                              const ZsChainArgs &a) {
+                                              uint32_t lane4, uint32_t ebase, const ZsChainArgs &a) {
     float2 r = make_float2(zs_dec<0>(lut, wp, lane4), zs_dec<0>(lut, wq, lane4));
     float2 g = make_float2(zs_dec<1>(lut, wp, lane4), zs_dec<1>(lut, wq, lane4));
     float2 b = make_float2(zs_dec<2>(lut, wp, lane4), zs_dec<2>(lut, wq, lane4));
@@ -59,7 +61,17 @@ __device__ __forceinline__ void zs_chain_pair(uint32_t &wp, uint32_t &wq, const 
             b.x = zs_cbrt1<false>(b.x); b.y = zs_cbrt1<false>(b.y);
         }
     }
-    zs_m3x2<false>(a.m2[1], r, g, b);
+    if (RANK1) {
+        // c' = d c + (v . c) (1, 1, 1)
+        const float2 *v = reinterpret_cast<const float2 *>(a.mb_v);
+        const float2 d = *reinterpret_cast<const float2 *>(a.mb_d);
+        const float2 t = __ffma2_rn(v[0], r, __ffma2_rn(v[1], g, __fmul2_rn(v[2], b)));
+        r = __ffma2_rn(d, r, t);
+        g = __ffma2_rn(d, g, t);
+        b = __ffma2_rn(d, b, t);
+    } else {
+        zs_m3x2<false>(a.m2[1], r, g, b);
+    }
     if (CUBE) {
         r = __fmul2_rn(__fmul2_rn(r, r), r);
         g = __fmul2_rn(__fmul2_rn(g, g), g);
@@ -71,14 +83,14 @@ __device__ __forceinline__ void zs_chain_pair(uint32_t &wp, uint32_t &wq, const 
     r = __fadd2_rn(r, sh);
     g = __fadd2_rn(g, sh);
     b = __fadd2_rn(b, sh);
-    const uint32_t rp = zs_enc_q(enc_lane, r.x), gp = zs_enc_q(enc_lane, g.x), bp = zs_enc_q(enc_lane, b.x);
-    const uint32_t rq = zs_enc_q(enc_lane, r.y), gq = zs_enc_q(enc_lane, g.y), bq = zs_enc_q(enc_lane, b.y);
+    const uint32_t rp = zs_enc_q(ebase, r.x), gp = zs_enc_q(ebase, g.x), bp = zs_enc_q(ebase, b.x);
+    const uint32_t rq = zs_enc_q(ebase, r.y), gq = zs_enc_q(ebase, g.y), bq = zs_enc_q(ebase, b.y);
     wp = __byte_perm(__byte_perm(rp, gp, 0x0073), __byte_perm(bp, wp, 0x0073), 0x5410);
     wq = __byte_perm(__byte_perm(rq, gq, 0x0073), __byte_perm(bq, wq, 0x0073), 0x5410);
 }
 
-template <bool CBRT, bool CUBE, bool CLAMP, bool NONNEG>
-__global__ void __launch_bounds__(ZS_CHAIN_THREADS, 2) zs_chain_srgb8_kernel(const __grid_constant__ ZsChainArgs a) {
+template <bool CBRT, bool CUBE, bool CLAMP, bool NONNEG, bool RANK1>
+__global__ void __launch_bounds__(ZS_CHAIN_THREADS, 1) zs_chain_srgb8_kernel(const __grid_constant__ ZsChainArgs a) {
     extern __shared__ __align__(16) unsigned char zs_smem_raw[];
     ZsChainSmem &sm = *reinterpret_cast<ZsChainSmem *>(zs_smem_raw);
     const uint4 *in = reinterpret_cast<const uint4 *>(a.src);
@@ -94,9 +106,9 @@ __global__ void __launch_bounds__(ZS_CHAIN_THREADS, 2) zs_chain_srgb8_kernel(con
         const float d = zs_srgb_decode_lut[i >> 3];
         reinterpret_cast<float4 *>(sm.lut)[(i >> 3) * 16 + (i & 7)] = make_float4(d, d, d, d);
     }
-    static_assert(ZS_ENC_REP == 4, "one uint4 per encode bucket");
-    for (int i = threadIdx.x; i < ZS_ENCS_ENTRIES; i += blockDim.x) {
-        const uint32_t e = zs_srgb_encode_tab_shifted[i];
+    static_assert(ZS_ENC_REP == 8, "two uint4 per encode bucket");
+    for (int i = threadIdx.x; i < 2 * ZS_ENCS_ENTRIES; i += blockDim.x) {
+        const uint32_t e = zs_srgb_encode_tab_shifted[i >> 1];
         reinterpret_cast<uint4 *>(sm.enc)[i] = make_uint4(e, e, e, e);
     }
     // Image data only after the previous grid in the stream has completed and its writes are
@@ -113,7 +125,7 @@ __global__ void __launch_bounds__(ZS_CHAIN_THREADS, 2) zs_chain_srgb8_kernel(con
     const int lane = threadIdx.x & 31;
     const unsigned char *lut = reinterpret_cast<const unsigned char *>(sm.lut);
     const uint32_t lane4 = (uint32_t)lane << 2;
-    const uint32_t *enc_lane = sm.enc + (lane & (ZS_ENC_REP - 1));
+    const uint32_t ebase = zs_enc_base(sm.enc, lane);
 
     if (piped) {
         // Software pipeline: the next two vectors are in flight while the current two are
@@ -126,11 +138,11 @@ __global__ void __launch_bounds__(ZS_CHAIN_THREADS, 2) zs_chain_srgb8_kernel(con
                 n0 = __ldcs(in + nx);
                 n1 = __ldcs(in + nx + stride);
             }
-            zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG>(w0.x, w0.y, lut, lane4, enc_lane, a);
-            zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG>(w0.z, w0.w, lut, lane4, enc_lane, a);
+            zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG, RANK1>(w0.x, w0.y, lut, lane4, ebase, a);
+            zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG, RANK1>(w0.z, w0.w, lut, lane4, ebase, a);
             __stcs(out + v, w0);
-            zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG>(w1.x, w1.y, lut, lane4, enc_lane, a);
-            zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG>(w1.z, w1.w, lut, lane4, enc_lane, a);
+            zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG, RANK1>(w1.x, w1.y, lut, lane4, ebase, a);
+            zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG, RANK1>(w1.z, w1.w, lut, lane4, ebase, a);
             __stcs(out + v + stride, w1);
             v = nx;
             if (!more) break;
@@ -140,8 +152,8 @@ __global__ void __launch_bounds__(ZS_CHAIN_THREADS, 2) zs_chain_srgb8_kernel(con
     }
     if (v < nvec) {
         uint4 w = __ldcs(in + v);
-        zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG>(w.x, w.y, lut, lane4, enc_lane, a);
-        zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG>(w.z, w.w, lut, lane4, enc_lane, a);
+        zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG, RANK1>(w.x, w.y, lut, lane4, ebase, a);
+        zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG, RANK1>(w.z, w.w, lut, lane4, ebase, a);
         __stcs(out + v, w);
     }
     // Tail pixels (npx not a multiple of 4): block 0, threads 0..3.
@@ -151,16 +163,16 @@ __global__ void __launch_bounds__(ZS_CHAIN_THREADS, 2) zs_chain_srgb8_kernel(con
         const uint32_t *in32 = reinterpret_cast<const uint32_t *>(a.src);
         uint32_t *out32 = reinterpret_cast<uint32_t *>(a.dst);
         uint32_t p = in32[t], q = p;
-        zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG>(p, q, lut, lane4, enc_lane, a);
+        zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG, RANK1>(p, q, lut, lane4, ebase, a);
         out32[t] = p;
     }
 }
 
 namespace zs {
 
-template <bool CBRT, bool CUBE, bool CLAMP, bool NONNEG>
+template <bool CBRT, bool CUBE, bool CLAMP, bool NONNEG, bool RANK1 = false>
 static cudaError_t launch_chain_t(const ZsChainArgs &args, int sm_count, cudaStream_t stream) {
-    auto kernel = zs_chain_srgb8_kernel<CBRT, CUBE, CLAMP, NONNEG>;
+    auto kernel = zs_chain_srgb8_kernel<CBRT, CUBE, CLAMP, NONNEG, RANK1>;
     const size_t smem = sizeof(ZsChainSmem);
     // The shared-memory opt-in is a per-device attribute of the kernel: set it (and size the
     // grid) once per device, on the device that is current for this launch.
@@ -205,6 +217,11 @@ static cudaError_t launch_chain_t(const ZsChainArgs &args, int sm_count, cudaStr
 template <bool NONNEG>
 static cudaError_t launch_chain_n(const ZsChainArgs &args, int sm_count, cudaStream_t stream) {
     const bool cb = args.flags & ZS_CHAIN_CBRT, cu = args.flags & ZS_CHAIN_CUBE, cl = args.flags & ZS_CHAIN_CLAMP;
+    // The Oklab form (cube root, L/C scaling, cube) with the rank-1 middle matrix.
+    if (cb && cu && (args.flags & ZS_CHAIN_MB_RANK1)) {
+        if (cl) return launch_chain_t<true, true, true, NONNEG, true>(args, sm_count, stream);
+        return launch_chain_t<true, true, false, NONNEG, true>(args, sm_count, stream);
+    }
     if (cb && cu && cl) return launch_chain_t<true, true, true, NONNEG>(args, sm_count, stream);
     if (cb && cu && !cl) return launch_chain_t<true, true, false, NONNEG>(args, sm_count, stream);
     if (cb && !cu && cl) return launch_chain_t<true, false, true, NONNEG>(args, sm_count, stream);
@@ -219,6 +236,8 @@ cudaError_t launch_chain(const ZsChainArgs &args, uint8_t src_fast, uint8_t dst_
                          cudaStream_t stream) {
     if (src_fast != ZS_FAST_RGBA8_SRGB || dst_fast != ZS_FAST_RGBA8_SRGB) return cudaErrorNotSupported;
     if (args.npx <= 0) return cudaSuccess;
+    // 16-byte vector loads and stores: other pointers take the generic raster kernel.
+    if (((uintptr_t)args.src | (uintptr_t)args.dst) & 15u) return cudaErrorNotSupported;
     if ((args.flags & ZS_CHAIN_CBRT_NONNEG) || !(args.flags & ZS_CHAIN_CBRT))
         return launch_chain_n<true>(args, sm_count, stream);
     return launch_chain_n<false>(args, sm_count, stream);

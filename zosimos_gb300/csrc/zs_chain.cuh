@@ -6,8 +6,9 @@
 
 #include "zs_shared.h"
 
-// Lane copies of each sRGB encode bucket in shared memory (lane & 3 reads copy lane & 3).
-#define ZS_ENC_REP 4
+// Lane copies of each sRGB encode bucket in shared memory (lane & 7 reads copy lane & 7):
+// at most 4 lanes share a copy, so a warp's 32 random bucket lookups rarely conflict.
+#define ZS_ENC_REP 8
 
 __device__ __forceinline__ float zs_ex2(float x) {
     float y;
@@ -60,10 +61,26 @@ __device__ __forceinline__ void zs_m3x2(const float (*m)[2], float2 &r, float2 &
 
 // xs = x + 2^-12 for x in [0, 1] -> table entry + bits of xs; the sRGB8 code is byte 3
 // of the result.  The shift (added to a pixel pair by one packed add) keeps the argument
-// inside the table without an integer clamp.
-__device__ __forceinline__ uint32_t zs_enc_q(const uint32_t *enc_lane, float xs) {
+// inside the table without an integer clamp.  `ebase` is the 32-bit shared address of this
+// lane's copy of bucket 0 minus ZS_ENCS_BASE buckets, so the lookup is one shift, one
+// shift-add, one shared load and one add.
+__device__ __forceinline__ uint32_t zs_enc_q(uint32_t ebase, float xs) {
+    static_assert(ZS_ENC_REP == 8, "32-byte buckets");
     const uint32_t b = __float_as_uint(xs);
-    return enc_lane[((b >> 16) - ZS_ENCS_BASE) * ZS_ENC_REP] + b;
+    uint32_t e;
+    asm("{\n\t.reg .u32 t, a;\n\t"
+        "shr.u32 t, %1, 16;\n\t"
+        "shl.b32 t, t, 5;\n\t"
+        "add.u32 a, t, %2;\n\t"
+        "ld.shared.u32 %0, [a];\n\t}"
+        : "=r"(e)
+        : "r"(b), "r"(ebase));
+    return e + b;
+}
+
+// Shared address base for zs_enc_q: copy (lane & 7) of the replicated table at `enc`.
+__device__ __forceinline__ uint32_t zs_enc_base(const uint32_t *enc, int lane) {
+    return (uint32_t)__cvta_generic_to_shared(enc + (lane & (ZS_ENC_REP - 1))) - ZS_ENCS_BASE * ZS_ENC_REP * 4u;
 }
 
 // Decoded value of byte K of texel w for this lane: (code << 8) | (lane << 2) is the

@@ -219,6 +219,10 @@ struct ZsChainArgs {
     int32_t flags;        // ZS_CHAIN_* bits
     int32_t pad;
     float m2[4][9][2];    // the same matrices with every coefficient duplicated (f32x2 operands)
+    // ZS_CHAIN_MB_RANK1: M_b = d I + (1,1,1)^T v (an Oklab L/C scaling), applied as
+    // s = v . c, c' = d c + s (6 FMAs instead of 9); duplicated for f32x2 operands.
+    float mb_v[3][2];
+    float mb_d[2];
 };
 
 enum {
@@ -229,7 +233,8 @@ enum {
     ZS_CHAIN_MB = 16,
     ZS_CHAIN_MC = 32,
     ZS_CHAIN_MD = 64,
-    ZS_CHAIN_CBRT_NONNEG = 128   // M_a maps [0,1]^3 to non-negative values: no sign handling
+    ZS_CHAIN_CBRT_NONNEG = 128,  // M_a maps [0,1]^3 to non-negative values: no sign handling
+    ZS_CHAIN_MB_RANK1 = 256      // M_b is d I + (1,1,1)^T v (mb_v, mb_d)
 };
 
 // Entry count of the exact sRGB8 encode table: buckets of the float bit pattern
