@@ -277,7 +277,9 @@ struct Planner {
 
     // M == d I + (1,1,1)^T v (every row of M - d I equal), the middle matrix of an Oklab L/C
     // scaling: M2^-1 diag(sL, sC, sC) M2 = sC I + (sL - sC) M2^-1 e1 (row 0 of M2), and
-    // M2^-1 e1 = (1, 1, 1).  Checked in FP64 against the matrix's own scale.
+    // M2^-1 e1 = (1, 1, 1).  Checked in FP64: the rows may differ by less than 2^-24 of the
+    // matrix's scale, below the rounding of the coefficients to f32 (Oklab's published M2
+    // has 10 digits, so its inverse's first column is (1, 1 + 1e-8, 1 + 5e-8)).
     static bool rank1_middle(const Mat3 &m, double &d, double v[3]) {
         double scale = 0.0;
         for (double x : m.m) scale = std::max(scale, std::fabs(x));
@@ -286,7 +288,8 @@ struct Planner {
         for (int j = 0; j < 3; ++j) {
             double col[3];
             for (int i = 0; i < 3; ++i) col[i] = m.m[3 * i + j] - (i == j ? d : 0.0);
-            if (std::fabs(col[0] - col[1]) > 1e-12 * scale || std::fabs(col[0] - col[2]) > 1e-12 * scale) return false;
+            const double tol = scale * 0x1p-24;
+            if (std::fabs(col[0] - col[1]) > tol || std::fabs(col[0] - col[2]) > tol) return false;
             v[j] = (col[0] + col[1] + col[2]) / 3.0;
         }
         return true;
