@@ -339,7 +339,9 @@ int zs_batch_thumbnails(zs_executable *chain, const void *const *images, const u
  * in one fixed 32 MiB device array per GPU.  Calls that need more than that array
  * (tables + dst_width * src_height * 8 bytes) return ZS_ERR_INVALID_ARG, and so do src or
  * dst pointers that are not 8-byte aligned and sides above 2^24.  All calls on a device
- * share the array: calls that overlap on the GPU race, so order them on one stream.  The
+ * share the array: calls that overlap on the GPU race (their results are undefined), so
+ * order them on one stream; a non-blocking stream is not ordered against the legacy default
+ * stream.  The
  * first call on a device loads the array's module (the driver reserves the 32 MiB then,
  * so that call can fail for lack of memory) and resolves the array's address for the
  * current device: make one warm-up call at start-up, before any stream capture, and do

@@ -78,19 +78,21 @@ def test_noalloc_matches_regular_entry_point_and_oracle_twice():
 
 
 def test_noalloc_allocates_nothing_and_runs_on_a_stream():
+    """After a warm-up call, calls allocate no device memory.  Every call here is ordered on
+    one created stream: calls share the scratch array, so calls that overlap on the GPU
+    (e.g. the legacy default stream against a non-blocking stream such as torch's) race."""
     import torch
     img = linear_gradient_gauss(512, 384, seed=12)
     bufs = _Buffers(img, (200, 150))
     stream = torch.cuda.Stream()        # the caller's stream exists before the calls under test
     handle = ctypes.c_void_p(stream.cuda_stream)
-    bufs.call(zs.Filter.Lanczos3)       # warm-up: loads the module, reserves the fixed array
-    bufs.call(zs.Filter.Lanczos3, handle)
-    zs.device_synchronize()
+    bufs.call(zs.Filter.Lanczos3, handle)   # warm-up: loads the module, reserves the fixed array
+    stream.synchronize()
     free0, _ = torch.cuda.mem_get_info()
     for _ in range(3):
+        bufs.call(zs.Filter.Box, handle)
         bufs.call(zs.Filter.Lanczos3, handle)
-        bufs.call(zs.Filter.Box)
-    zs.device_synchronize()
+    stream.synchronize()
     free1, _ = torch.cuda.mem_get_info()
     assert free1 == free0
     exact = P.oracle_resample(P.f16_from_bytes(P.f16_bytes(img), 512, 384), (200, 150), zs.Filter.Lanczos3)

@@ -29,7 +29,10 @@
 //  * every call on a device uses the same array and leaves its contents behind; nothing
 //    in it has to start at zero, because each call writes every byte it later reads;
 //  * calls whose work overlaps on the GPU (e.g. issued on different streams without an
-//    ordering between them) race on the array: order them on one stream or serialise them.
+//    ordering between them, such as the legacy default stream and a non-blocking stream)
+//    race on the array and their results are undefined: order them on one stream or
+//    serialise them.  The resample kernels clamp every tap window to their source, so a
+//    race corrupts pixels but reads no memory outside the buffers.
 //  * the first call on a device looks up the array's device address
 //    (cudaGetSymbolAddress, with that device current) and keeps it for the life of the
 //    process; make that first call before any stream capture begins, and do not use this

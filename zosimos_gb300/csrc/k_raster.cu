@@ -286,7 +286,11 @@ __global__ void __launch_bounds__(256) zs_raster_kernel(const __grid_constant__ 
                             rows[0][2] + rows[1][2] + rows[2][2], 1.0f);
         } break;
         case ZS_PR_RESAMPLE_H: {
-            int first = a.index_x[x], cnt = a.index_y[x];
+            // The tap window is clamped to the source row and the table width, so that no
+            // table content (e.g. one rewritten by an overlapping call of the allocation-free
+            // entry point) can index outside the source.
+            const int first = min(max(a.index_x[x], 0), s0.width - 1);
+            const int cnt = min(min(a.index_y[x], a.taps), s0.width - first);
             const float *w = a.weights + (int64_t)x * a.taps;
             float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
             for (int t = 0; t < cnt; ++t) {
@@ -298,7 +302,8 @@ __global__ void __launch_bounds__(256) zs_raster_kernel(const __grid_constant__ 
             r = acc;
         } break;
         case ZS_PR_RESAMPLE_V: {
-            int first = a.index_x[y], cnt = a.index_y[y];
+            const int first = min(max(a.index_x[y], 0), s0.height - 1);
+            const int cnt = min(min(a.index_y[y], a.taps), s0.height - first);
             const float *w = a.weights + (int64_t)y * a.taps;
             float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
             for (int t = 0; t < cnt; ++t) {
