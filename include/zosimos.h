@@ -227,6 +227,19 @@ int zs_cmd_blend(zs_cmd *cmd, uint32_t below, const zs_rect *rect, uint32_t abov
 /* Extension: a 3x3 linear map applied to the colour channels in the image's own
  * colour space (e.g. scaling Oklab L and C); alpha is kept. */
 int zs_cmd_color_matrix(zs_cmd *cmd, uint32_t src, const float matrix[9], uint32_t *reg);
+/* CommandBuffer::with_knob (command.rs:1740-1742, WithKnob :1865-1961): the next operation's
+ * parameter block becomes a knob that a launch may replace without recompiling.  Operations
+ * that take one: bilinear (6 x 4 f32), solid_rgba (4 f32), distribution_normal2d (8 f32:
+ * mu0, mu1, C+ row major, pseudo-determinant, pad), distribution_fractal_noise (2 f32 grid
+ * scale, f32 amplitude, f32 damping, u32 octaves, 4 bytes pad) and buffer_init (the buffer's
+ * bytes); any other operation fails with ZS_ERR_UNIMPLEMENTED. */
+int zs_cmd_with_knob(zs_cmd *cmd);
+/* CommandBuffer::with_buffer (command.rs:1751-1765, WithBuffer :1963-2060): the next
+ * operation (bilinear, solid_rgba, distribution_normal2d, distribution_fractal_noise) reads
+ * its parameter block from the start of `buffer` (a buffer_init / buffer_zero register), and
+ * follows the buffer's knob when it has one.  ZS_ERR_TYPE when `buffer` is not a buffer,
+ * ZS_ERR_OTHER (INVALID_CALL) when it is shorter than the parameter block. */
+int zs_cmd_with_buffer(zs_cmd *cmd, uint32_t buffer);
 /* CommandBuffer::output (command.rs:1707). */
 int zs_cmd_output(zs_cmd *cmd, uint32_t src, uint32_t *reg, zs_descriptor *outformat);
 /* Describe a register (command.rs describe_reg). */
@@ -264,8 +277,19 @@ typedef struct zs_executable zs_executable;
 /* Program::lower_to (program.rs:1304). */
 int zs_lower(const zs_program *program, const zs_capabilities *caps, zs_executable **out);
 void zs_executable_free(zs_executable *exe);
+/* Executable::query_knob (run.rs:1012-1014) for RegisterKnob { link_idx, register }: the knob
+ * id and the byte length of its parameter block.  ZS_ERR_BAD_REGISTER when the register has
+ * no knob (link_idx must be 0: the program itself). */
+int zs_executable_query_knob(const zs_executable *exe, uint32_t link_idx, uint32_t reg, uint32_t *knob,
+                             uint64_t *len);
+/* Replaces the parameter block of a knob for every later launch of the executable (the
+ * one-call paths zs_run_host / zs_run_device / batches included); len must equal the knob's.
+ * No counterpart in the reference, whose knob data is per launch (zs_env_knob). */
+int zs_executable_set_knob(zs_executable *exe, uint32_t knob, const void *data, uint64_t len);
 /* Number of kernel launches one launch of this executable issues. */
 int zs_executable_kernel_count(const zs_executable *exe, uint32_t *count);
+/* Numbers of input and output registers (either pointer may be null). */
+int zs_executable_io_count(const zs_executable *exe, uint32_t *inputs, uint32_t *outputs);
 /* Human readable plan (the analogue of Executable::dot, run.rs:491). */
 const char *zs_executable_describe(const zs_executable *exe);
 
@@ -277,6 +301,9 @@ int zs_env_new(zs_executable *exe, zs_pool *pool, zs_environment **out);
 void zs_env_free(zs_environment *env);
 /* Environment::bind (run.rs:1171). */
 int zs_env_bind(zs_environment *env, uint32_t reg, uint64_t key);
+/* Environment::knob (run.rs:1292-1306): the parameter block of `knob` for this launch only (len
+ * must equal the knob's, else ZS_ERR_INVALID_ARG); launches without one use the static block. */
+int zs_env_knob(zs_environment *env, uint32_t knob, const void *data, uint64_t len);
 /* Environment::bind_output (run.rs:1207): write the output into an existing image. */
 int zs_env_bind_output(zs_environment *env, uint32_t reg, uint64_t key);
 /* Executable::launch (run.rs:1016): consumes `env` (even on failure). */
@@ -329,6 +356,23 @@ int zs_device_synchronize(void);
 int zs_batch_thumbnails(zs_executable *chain, const void *const *images, const uint32_t *widths,
                         const uint32_t *heights, uint32_t n, uint32_t canvas, void *out,
                         void *stream);
+
+/* ---- batches of runs of one executable (the reference's batch-reuse case: one Executable
+ *      launched for many images, tests/loop.rs:80-95, Environment::recover_buffers
+ *      run.rs:1312-1347) ---- */
+/* Runs `exe` once per set of device buffers: inputs holds n x (number of inputs) pointers,
+ * run i's inputs in declaration order at inputs[i * n_inputs ...], outputs likewise.  The n
+ * runs are recorded into one CUDA graph -- independent runs on up to 8 parallel branches; an
+ * executable that stores intermediates runs them one after another -- which is cached per
+ * pointer table and replayed when the same table comes again.  Buffers follow the alignment
+ * rule of zs_run_device.  stream may be null (the executable's own stream). */
+int zs_batch_run_device(zs_executable *exe, const void *const *inputs, void *const *outputs, uint32_t n,
+                        void *stream);
+/* The same over pool images: keys holds n x (number of inputs) pool keys, each checked against
+ * the input's descriptor (StartError::MismatchedDescriptor) and made device resident
+ * (Pool::upload); every run's outputs are retired into new pool images (Retire::output),
+ * whose keys are written to out_keys (n x number of outputs).  Synchronous. */
+int zs_batch_run(zs_executable *exe, zs_pool *pool, const uint64_t *keys, uint32_t n, uint64_t *out_keys);
 
 /* ---- resample without any device allocation ------------------------------------ */
 /* No counterpart in the reference.  For callers that may not allocate device memory

@@ -300,6 +300,30 @@ def test_batch_thumbnails():
         assert maxdiff(o, r) <= LSB
 
 
+def test_batch_thumbnails_graph_replay():
+    """The batch launch is captured as a CUDA graph once and replayed for later batches with
+    the same output buffer, count and canvas (the per-batch image table is uploaded before
+    each replay); a different canvas captures anew.  Every batch matches the oracle."""
+    from zosimos_gb300.synthetic import thumbnail_sizes
+    c, _, _ = P.chain_commands(1, 1)
+    exe = zs.Linker.from_included().compile(c).lower_to()
+    out = zs.DeviceBuffer(6 * 128 * 128 * 4)
+    for seed, canvas in ((6, 128), (7, 128), (8, 96), (9, 128)):
+        ws, hs = thumbnail_sizes(6, seed=seed, lo=33, hi=900)
+        images = [srgb_gradient_noise(int(w), int(h), seed=seed, image=i) for i, (w, h) in enumerate(zip(ws, hs))]
+        bufs = []
+        for img in images:
+            b = zs.DeviceBuffer(img.nbytes)
+            b.upload(P.rgba_bytes(img))
+            bufs.append(b)
+        exe.batch_thumbnails([b.ptr for b in bufs], [im.shape[1] for im in images], [im.shape[0] for im in images],
+                             canvas, out.ptr)
+        zs.device_synchronize()
+        got = out.download(np.empty(out.nbytes, np.uint8))[:6 * canvas * canvas * 4].reshape(6, canvas, canvas * 4)
+        for k, r in enumerate(P.oracle_thumbnails(images, canvas)):
+            assert maxdiff(got[k], r) <= LSB, (seed, k)
+
+
 @pytest.mark.parametrize("mode", [zs.Mode.Fused, zs.Mode.PerOpF32])
 def test_thumbnail_program_matches_batch(mode):
     # The one-program-per-image form of the batched thumbnails (chain, box fit, centred
@@ -538,3 +562,60 @@ def test_chain_on_buffers_not_16_byte_aligned():
     with pytest.raises(zs.ZosimosError) as err:
         exe.run_device([src.ptr + 1], [dst.ptr])
     assert err.value.code == 10
+
+
+def _chain_outputs(exe, images):
+    bufs, outs = [], []
+    for img in images:
+        b, o = zs.DeviceBuffer(img.nbytes), zs.DeviceBuffer(img.nbytes)
+        b.upload(P.rgba_bytes(img))
+        bufs.append(b)
+        outs.append(o)
+    return bufs, outs
+
+
+def test_batch_run_device_matches_single_runs():
+    """zs_batch_run_device: n runs of one executable as one replayed graph (independent runs on
+    parallel branches) give exactly the bytes of n separate runs; the same pointer table again
+    replays the cached graph, a new table captures anew."""
+    c, _, _ = P.chain_commands(97, 61)
+    exe = zs.Linker.from_included().compile(c).lower_to()
+    images = [srgb_gradient_noise(97, 61, seed=30, image=k) for k in range(11)]
+    bufs, outs = _chain_outputs(exe, images)
+    for _ in range(2):
+        exe.batch_run_device([[b.ptr] for b in bufs], [[o.ptr] for o in outs])
+        zs.device_synchronize()
+        for img, o in zip(images, outs):
+            got = o.download(np.empty((61, 97 * 4), np.uint8))
+            assert maxdiff(got, P.oracle_chain(img)) <= LSB
+    single = zs.DeviceBuffer(images[3].nbytes)
+    exe.run_device([bufs[3].ptr], [single.ptr])
+    zs.device_synchronize()
+    assert (single.download(np.empty((61, 97 * 4), np.uint8)) == outs[3].download(np.empty((61, 97 * 4), np.uint8))).all()
+    # a different pointer table: a shorter batch over other buffers
+    exe.batch_run_device([[b.ptr] for b in bufs[5:]], [[o.ptr] for o in outs[:6]])
+    zs.device_synchronize()
+    for k in range(6):
+        got = outs[k].download(np.empty((61, 97 * 4), np.uint8))
+        assert maxdiff(got, P.oracle_chain(images[5 + k])) <= LSB
+
+
+@pytest.mark.parametrize("mode", [zs.Mode.Fused, zs.Mode.PerOpF32])
+def test_batch_run_pool_keys_two_inputs(mode):
+    """zs_batch_run over pool keys: a two-input executable (blend + bilinear resize; its per-op
+    form stores intermediates, so its runs are recorded one after another) for four pairs of
+    images; every run's output is a new pool image matching the oracle."""
+    c, a, b, o = P.blend_resize(256, 192, 150, 100)
+    exe = zs.Linker.from_included().compile(c).lower_to(zs.Capabilities(mode=mode))
+    pool = zs.Pool()
+    pairs, keys = [], []
+    for k in range(4):
+        ia = srgb_gradient_noise(256, 192, seed=31, image=2 * k)
+        ib = srgb_gradient_noise(256, 192, seed=31, image=2 * k + 1)
+        pairs.append((ia, ib))
+        keys.append([pool.insert_srgb(ia), pool.insert_srgb(ib)])
+    outs = exe.batch_run(pool, keys)
+    assert len(outs) == 4 and all(len(r) == 1 for r in outs)
+    for (ia, ib), (ko,) in zip(pairs, outs):
+        got = pool.read(ko)
+        assert maxdiff(got, P.oracle_blend_resize(ia, ib, (150, 100))) <= LSB

@@ -250,3 +250,51 @@ def test_normal2d_parameters_follow_the_reference_constructors():
     c = CommandBuffer()
     c.output(c.distribution_normal2d(Descriptor.srgb_rgba8(32, 16), zs.normal2d_with_diagonal(0.2, 0.2)))
     assert Linker.from_included().compile(c).lower_to().kernel_count() == 1
+
+
+def test_batch_entry_points_check_arguments_without_device():
+    import ctypes
+    lib = zs._lib()
+    c, _, _ = color_chain(16, 16)
+    exe = lower(c)
+    assert exe.output_count() == 1
+    # an empty batch is a no-op; null handles and tables are argument errors
+    assert lib.zs_batch_run_device(exe._h, None, None, 0, None) == 0
+    assert lib.zs_batch_run_device(None, None, None, 1, None) == 10
+    assert lib.zs_batch_run_device(exe._h, None, None, 1, None) == 10
+    pool = zs.Pool()
+    assert lib.zs_batch_run(exe._h, pool._h, None, 1, None) == 10
+    assert lib.zs_batch_run(exe._h, pool._h, None, 0, None) == 0
+
+
+def test_knobs_and_buffer_parameters_host_side():
+    c = CommandBuffer()
+    d = Descriptor.srgb_rgba8(16, 16)
+    plain = c.bilinear(d, [0] * 4, [1] * 4, [0] * 4, [1] * 4, [0] * 4, [0] * 4)
+    knobbed = c.with_knob().bilinear(d, [0] * 4, [1] * 4, [0] * 4, [1] * 4, [0] * 4, [0] * 4)
+    # with_knob on an operation without a parameter block fails and is not left pending
+    with pytest.raises(ZosimosError) as e:
+        c.with_knob().color_convert(plain, Descriptor.linear_rgba_f32(16, 16))
+    assert e.value.code == 2
+    later = c.bilinear(d, [0] * 4, [1] * 4, [0] * 4, [1] * 4, [0] * 4, [0] * 4)
+    short = c.buffer_init(np.zeros(32, np.uint8))
+    with pytest.raises(ZosimosError) as e:
+        c.with_buffer(short).bilinear(d, [0] * 4, [1] * 4, [0] * 4, [1] * 4, [0] * 4, [0] * 4)
+    assert e.value.code == 4            # CommandError::INVALID_CALL: buffer too short
+    with pytest.raises(ZosimosError) as e:
+        c.with_buffer(plain)
+    assert e.value.is_type_err
+    outs = [c.output(r)[0] for r in (plain, knobbed, later)]
+    exe = Linker.from_included().compile(c).lower_to()
+    knob, n = exe.query_knob(knobbed)
+    assert n == 96 and "[knob]" in exe.describe()
+    for reg in (plain, later):
+        with pytest.raises(ZosimosError) as e:
+            exe.query_knob(reg)
+        assert e.value.code == 3
+    env = exe.from_pool(zs.Pool())
+    with pytest.raises(ZosimosError) as e:
+        env.knob(knob, np.zeros(95, np.uint8))
+    assert e.value.code == 10
+    env.knob(knob, np.zeros(24, np.float32))
+    assert len(outs) == 3

@@ -187,6 +187,11 @@ def _lib():
             "zs_descriptor_is_consistent": ([pD], I32), "zs_descriptor_byte_len": ([pD], U64),
             "zs_texel_bytes": ([U32], U32),
             "zs_batch_thumbnails": ([P, P, P, P, U32, U32, P, P], I32),
+            "zs_batch_run_device": ([P, P, P, U32, P], I32), "zs_batch_run": ([P, P, P, U32, P], I32),
+            "zs_executable_io_count": ([P, P, P], I32),
+            "zs_cmd_with_knob": ([P], I32), "zs_cmd_with_buffer": ([P, U32], I32),
+            "zs_executable_query_knob": ([P, U32, U32, pU32, pU64], I32),
+            "zs_executable_set_knob": ([P, U32, P, U64], I32), "zs_env_knob": ([P, U32, P, U64], I32),
         }
         for name, (args, res) in sig.items():
             fn = getattr(lib, name)
@@ -560,6 +565,16 @@ class CommandBuffer:
         m = np.ascontiguousarray(np.asarray(matrix, dtype=np.float32).reshape(9))
         return self._reg(_lib().zs_cmd_color_matrix, src, m.ctypes.data)
 
+    def with_knob(self) -> "CommandBuffer":
+        """CommandBuffer::with_knob: the next operation's parameters become a run-time knob."""
+        _check(_lib().zs_cmd_with_knob(self._h))
+        return self
+
+    def with_buffer(self, buffer: int) -> "CommandBuffer":
+        """CommandBuffer::with_buffer: the next operation reads its parameters from `buffer`."""
+        _check(_lib().zs_cmd_with_buffer(self._h, buffer))
+        return self
+
     def output(self, src: int):
         reg = ctypes.c_uint32()
         d = _CDesc()
@@ -653,6 +668,43 @@ class Executable:
         hs = (ctypes.c_uint32 * n)(*heights)
         _check(_lib().zs_batch_thumbnails(self._h, ptrs, ws, hs, n, canvas, out, stream or None))
 
+    def batch_run_device(self, inputs: Sequence[Sequence[int]], outputs: Sequence[Sequence[int]],
+                         stream: int = 0) -> None:
+        """zs_batch_run_device: one run per row of device pointers, recorded into one CUDA
+        graph (cached per pointer table, replayed when the same table comes again)."""
+        n = len(inputs)
+        flat_in = [p for row in inputs for p in row]
+        flat_out = [p for row in outputs for p in row]
+        ins = (ctypes.c_void_p * max(len(flat_in), 1))(*flat_in)
+        outs = (ctypes.c_void_p * max(len(flat_out), 1))(*flat_out)
+        _check(_lib().zs_batch_run_device(self._h, ins, outs, n, stream or None))
+
+    def batch_run(self, pool: "Pool", keys: Sequence[Sequence[int]]):
+        """zs_batch_run: one run per row of pool keys; returns the output keys per run."""
+        n = len(keys)
+        flat = [k for row in keys for k in row]
+        arr = (ctypes.c_uint64 * max(len(flat), 1))(*flat)
+        nout = self.output_count()
+        out = (ctypes.c_uint64 * max(n * nout, 1))()
+        _check(_lib().zs_batch_run(self._h, pool._h, arr, n, out))
+        return [list(out[i * nout:(i + 1) * nout]) for i in range(n)]
+
+    def query_knob(self, register: int, link_idx: int = 0):
+        """Executable::query_knob: (knob id, byte length of its parameter block)."""
+        k, n = ctypes.c_uint32(), ctypes.c_uint64()
+        _check(_lib().zs_executable_query_knob(self._h, link_idx, register, ctypes.byref(k), ctypes.byref(n)))
+        return k.value, n.value
+
+    def set_knob(self, knob: int, data) -> None:
+        """The knob's parameter block for every later launch (one-call paths included)."""
+        b = bytes(np.ascontiguousarray(data).view(np.uint8).reshape(-1)) if isinstance(data, np.ndarray) else bytes(data)
+        _check(_lib().zs_executable_set_knob(self._h, knob, b, len(b)))
+
+    def output_count(self) -> int:
+        n = ctypes.c_uint32()
+        _check(_lib().zs_executable_io_count(self._h, None, ctypes.byref(n)))
+        return n.value
+
     def run_device(self, inputs: Sequence[int], outputs: Sequence[int], stream: int = 0) -> None:
         """One launch on device pointers (no host copies); graph-replayed when enabled."""
         ins = (ctypes.c_void_p * len(inputs))(*inputs)
@@ -678,6 +730,11 @@ class Environment:
 
     def bind_output(self, reg: int, key: int) -> None:
         _check(_lib().zs_env_bind_output(self._h, reg, key))
+
+    def knob(self, knob: int, data) -> None:
+        """Environment::knob: this launch's parameter block for `knob`."""
+        b = bytes(np.ascontiguousarray(data).view(np.uint8).reshape(-1)) if isinstance(data, np.ndarray) else bytes(data)
+        _check(_lib().zs_env_knob(self._h, knob, b, len(b)))
 
 
 class Execution:
@@ -763,6 +820,20 @@ class PinnedBuffer:
 
 def device_synchronize() -> None:
     _check(_lib().zs_device_synchronize())
+
+
+def run_executable(exe: Executable, pool: Pool, binds, knobs, outputs):
+    """tests/util.rs run_executable_with_output: bind, set this launch's knobs, step to the end,
+    retire the outputs into the pool."""
+    env = exe.from_pool(pool)
+    for reg, key in binds:
+        env.bind(reg, key)
+    for knob, data in knobs:
+        env.knob(knob, data)
+    execution = exe.launch(env)
+    while execution.is_running():
+        execution.step()
+    return [execution.retire_output(r) for r in outputs]
 
 
 def run_pipeline(commands: CommandBuffer, pool: Pool, binds, outputs, caps: Optional[Capabilities] = None):

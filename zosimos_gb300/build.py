@@ -92,10 +92,24 @@ def build(force: bool = False, verbose: bool = False) -> str:
             raise RuntimeError("compile failed: " + " ".join(cmd) + "\n" + r.stdout + r.stderr)
         return r.stdout + r.stderr
 
+    # An object is rebuilt when it is missing or older than its source or any header.
+    headers = [p for p in _deps() if not p.endswith((".cu", ".cpp"))]
+    newest_header = max(os.path.getmtime(p) for p in headers)
+
+    def stale(cmd):
+        src, obj = cmd[-3], cmd[-1]
+        if force or verbose or not os.path.exists(obj):
+            return True
+        t = os.path.getmtime(obj)
+        return os.path.getmtime(src) > t or newest_header > t
+
+    todo = [c for c in jobs if stale(c)]
     # The slowest object (k_raster.cu) goes first so that it overlaps the rest.
-    jobs.sort(key=lambda c: not c[-3].endswith("k_raster.cu"))
-    with cf.ThreadPoolExecutor(max_workers=min(len(jobs), max(4, os.cpu_count() or 4))) as ex:
-        logs = list(ex.map(run, jobs))
+    todo.sort(key=lambda c: not c[-3].endswith("k_raster.cu"))
+    logs = []
+    if todo:
+        with cf.ThreadPoolExecutor(max_workers=min(len(todo), max(4, os.cpu_count() or 4))) as ex:
+            logs = list(ex.map(run, todo))
     if verbose:
         for log in logs:
             sys.stdout.write(log)

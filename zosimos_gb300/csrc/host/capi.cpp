@@ -42,16 +42,29 @@ using namespace zs;
 struct zs_pool { Pool p; };
 struct zs_cmd { Command c; };
 struct zs_program { Program p; };
+#define ZS_BATCH_BRANCHES 8
 struct zs_executable {
     std::unique_ptr<Executable> e;
     cudaStream_t stream = nullptr;
     cudaStream_t stripes[3] = {nullptr, nullptr, nullptr};   // striped host round trips
+    // zs_batch_run_device: capture streams of the independent runs, fork / join events, and
+    // the instantiated graphs per pointer table (bounded, oldest evicted first)
+    cudaStream_t branches[ZS_BATCH_BRANCHES] = {};
+    cudaEvent_t fork = nullptr, joins[ZS_BATCH_BRANCHES] = {};
+    std::map<std::vector<void *>, cudaGraphExec_t> batch_graphs;
+    std::vector<std::vector<void *>> batch_order;
     ~zs_executable();
 };
 struct zs_environment { Environment env; };
 struct zs_execution { Execution x; std::vector<int> kinds; std::vector<int> args; };
 
 zs_executable::~zs_executable() {
+    for (auto &kv : batch_graphs) cudaGraphExecDestroy(kv.second);
+    for (cudaStream_t t : branches)
+        if (t) cudaStreamDestroy(t);
+    for (cudaEvent_t ev : joins)
+        if (ev) cudaEventDestroy(ev);
+    if (fork) cudaEventDestroy(fork);
     if (stream) cudaStreamDestroy(stream);
     for (cudaStream_t t : stripes)
         if (t) cudaStreamDestroy(t);
@@ -88,6 +101,15 @@ static int guarded(F &&f) {
     do {                                                           \
         if (!(ptr)) fail(ZS_ERR_INVALID_ARG, #ptr " is null");     \
     } while (0)
+
+// Command-building calls: a failed call also drops a pending with_knob / with_buffer, so that
+// it cannot attach to a later, unrelated operation.
+template <class F>
+static int cmd_guarded(zs_cmd *cmd, F &&f) {
+    const int rc = guarded(std::forward<F>(f));
+    if (rc != ZS_OK && cmd) cmd->c.clear_pending();
+    return rc;
+}
 
 extern "C" {
 
@@ -285,22 +307,22 @@ void zs_cmd_free(zs_cmd *cmd) { delete cmd; }
     })
 
 int zs_cmd_input(zs_cmd *cmd, const zs_descriptor *desc, uint32_t *reg) {
-    return guarded([&] { NEED(cmd); NEED(desc); NEED(reg); *reg = cmd_input(cmd->c, *desc); });
+    return cmd_guarded(cmd, [&] { NEED(cmd); NEED(desc); NEED(reg); *reg = cmd_input(cmd->c, *desc); });
 }
 int zs_cmd_crop(zs_cmd *cmd, uint32_t src, const zs_rect *rect, uint32_t *reg) {
-    return guarded([&] { NEED(cmd); NEED(rect); NEED(reg); *reg = cmd_crop(cmd->c, src, *rect); });
+    return cmd_guarded(cmd, [&] { NEED(cmd); NEED(rect); NEED(reg); *reg = cmd_crop(cmd->c, src, *rect); });
 }
 int zs_cmd_color_convert(zs_cmd *cmd, uint32_t src, const zs_descriptor *target, uint32_t *reg) {
-    return guarded([&] { NEED(cmd); NEED(target); NEED(reg); *reg = cmd_color_convert(cmd->c, src, *target); });
+    return cmd_guarded(cmd, [&] { NEED(cmd); NEED(target); NEED(reg); *reg = cmd_color_convert(cmd->c, src, *target); });
 }
 int zs_cmd_chromatic_adaptation(zs_cmd *cmd, uint32_t src, uint32_t method, uint32_t target_wp, uint32_t *reg) {
     CMD_BODY(cmd_chromatic_adaptation(cmd->c, src, method, target_wp));
 }
 int zs_cmd_inscribe(zs_cmd *cmd, uint32_t below, const zs_rect *rect, uint32_t above, uint32_t *reg) {
-    return guarded([&] { NEED(cmd); NEED(rect); NEED(reg); *reg = cmd_inscribe(cmd->c, below, *rect, above, false); });
+    return cmd_guarded(cmd, [&] { NEED(cmd); NEED(rect); NEED(reg); *reg = cmd_inscribe(cmd->c, below, *rect, above, false); });
 }
 int zs_cmd_inscribe_placed(zs_cmd *cmd, uint32_t below, const zs_rect *rect, uint32_t above, uint32_t *reg) {
-    return guarded([&] { NEED(cmd); NEED(rect); NEED(reg); *reg = cmd_inscribe(cmd->c, below, *rect, above, true); });
+    return cmd_guarded(cmd, [&] { NEED(cmd); NEED(rect); NEED(reg); *reg = cmd_inscribe(cmd->c, below, *rect, above, true); });
 }
 int zs_cmd_extract(zs_cmd *cmd, uint32_t src, uint32_t channel, uint32_t *reg) {
     CMD_BODY(cmd_extract(cmd->c, src, channel));
@@ -309,20 +331,20 @@ int zs_cmd_inject(zs_cmd *cmd, uint32_t below, uint32_t channel, uint32_t above,
     CMD_BODY(cmd_inject(cmd->c, below, channel, above));
 }
 int zs_cmd_transmute(zs_cmd *cmd, uint32_t src, const zs_descriptor *target, uint32_t *reg) {
-    return guarded([&] { NEED(cmd); NEED(target); NEED(reg); *reg = cmd_transmute(cmd->c, src, *target); });
+    return cmd_guarded(cmd, [&] { NEED(cmd); NEED(target); NEED(reg); *reg = cmd_transmute(cmd->c, src, *target); });
 }
 int zs_cmd_palette(zs_cmd *cmd, uint32_t palette, int32_t wch, int32_t hch, uint32_t indices, uint32_t *reg) {
     CMD_BODY(cmd_palette(cmd->c, palette, wch, hch, indices));
 }
 int zs_cmd_bilinear(zs_cmd *cmd, const zs_descriptor *desc, const float params[24], uint32_t *reg) {
-    return guarded([&] { NEED(cmd); NEED(desc); NEED(params); NEED(reg); *reg = cmd_bilinear(cmd->c, *desc, params); });
+    return cmd_guarded(cmd, [&] { NEED(cmd); NEED(desc); NEED(params); NEED(reg); *reg = cmd_bilinear(cmd->c, *desc, params); });
 }
 int zs_cmd_solid_rgba(zs_cmd *cmd, const zs_descriptor *desc, const float color[4], uint32_t *reg) {
-    return guarded([&] { NEED(cmd); NEED(desc); NEED(color); NEED(reg); *reg = cmd_solid(cmd->c, *desc, color); });
+    return cmd_guarded(cmd, [&] { NEED(cmd); NEED(desc); NEED(color); NEED(reg); *reg = cmd_solid(cmd->c, *desc, color); });
 }
 int zs_cmd_affine(zs_cmd *cmd, uint32_t below, const float matrix[9], uint32_t sampling, uint32_t above,
                   uint32_t *reg) {
-    return guarded([&] {
+    return cmd_guarded(cmd, [&] {
         NEED(cmd); NEED(matrix); NEED(reg);
         *reg = cmd_affine(cmd->c, below, matrix, sampling, above);
     });
@@ -335,7 +357,7 @@ int zs_cmd_resize_filtered(zs_cmd *cmd, uint32_t src, uint32_t width, uint32_t h
     CMD_BODY(cmd_resize(cmd->c, src, width, height, true, filter));
 }
 int zs_cmd_distribution_normal2d(zs_cmd *cmd, const zs_descriptor *desc, const float params[7], uint32_t *reg) {
-    return guarded([&] { NEED(cmd); NEED(desc); NEED(params); NEED(reg); *reg = cmd_normal2d(cmd->c, *desc, params); });
+    return cmd_guarded(cmd, [&] { NEED(cmd); NEED(desc); NEED(params); NEED(reg); *reg = cmd_normal2d(cmd->c, *desc, params); });
 }
 int zs_normal2d_with_diagonal(float var0, float var1, float params[7]) {
     return guarded([&] { NEED(params); normal2d_with_diagonal(var0, var1, params); });
@@ -344,16 +366,16 @@ int zs_normal2d_with_direction(float x, float y, float params[7]) {
     return guarded([&] { NEED(params); normal2d_with_direction(x, y, params); });
 }
 int zs_cmd_distribution_fractal_noise(zs_cmd *cmd, const zs_descriptor *desc, const float params[5], uint32_t *reg) {
-    return guarded([&] { NEED(cmd); NEED(desc); NEED(params); NEED(reg); *reg = cmd_fractal_noise(cmd->c, *desc, params); });
+    return cmd_guarded(cmd, [&] { NEED(cmd); NEED(desc); NEED(params); NEED(reg); *reg = cmd_fractal_noise(cmd->c, *desc, params); });
 }
 int zs_cmd_buffer_init(zs_cmd *cmd, const void *bytes, uint64_t len, uint32_t *reg) {
-    return guarded([&] { NEED(cmd); NEED(reg); *reg = cmd_buffer_init(cmd->c, bytes, len, len); });
+    return cmd_guarded(cmd, [&] { NEED(cmd); NEED(reg); *reg = cmd_buffer_init(cmd->c, bytes, len, len); });
 }
 int zs_cmd_buffer_zero(zs_cmd *cmd, uint64_t len, uint32_t *reg) {
-    return guarded([&] { NEED(cmd); NEED(reg); *reg = cmd_buffer_init(cmd->c, nullptr, 0, len); });
+    return cmd_guarded(cmd, [&] { NEED(cmd); NEED(reg); *reg = cmd_buffer_init(cmd->c, nullptr, 0, len); });
 }
 int zs_cmd_from_buffer(zs_cmd *cmd, uint32_t buffer, const zs_descriptor *desc, uint32_t *reg) {
-    return guarded([&] { NEED(cmd); NEED(desc); NEED(reg); *reg = cmd_from_buffer(cmd->c, buffer, *desc); });
+    return cmd_guarded(cmd, [&] { NEED(cmd); NEED(desc); NEED(reg); *reg = cmd_from_buffer(cmd->c, buffer, *desc); });
 }
 int zs_fractal_noise_with_octaves(uint32_t num_octaves, float params[5]) {
     return guarded([&] { NEED(params); fractal_noise_with_octaves(num_octaves, params); });
@@ -362,17 +384,33 @@ int zs_fractal_noise_set_damping(float params[5], float damping) {
     return guarded([&] { NEED(params); fractal_noise_set_damping(params, damping); });
 }
 int zs_cmd_derivative(zs_cmd *cmd, uint32_t src, uint32_t method, uint32_t direction, uint32_t *reg) {
-    return guarded([&] { NEED(cmd); NEED(reg); *reg = cmd_derivative(cmd->c, src, method, direction); });
+    return cmd_guarded(cmd, [&] { NEED(cmd); NEED(reg); *reg = cmd_derivative(cmd->c, src, method, direction); });
 }
 int zs_cmd_blend(zs_cmd *cmd, uint32_t below, const zs_rect *rect, uint32_t above, uint32_t mode, uint32_t *reg) {
-    return guarded([&] { NEED(cmd); NEED(rect); NEED(reg); *reg = cmd_blend(cmd->c, below, *rect, above, mode); });
+    return cmd_guarded(cmd, [&] { NEED(cmd); NEED(rect); NEED(reg); *reg = cmd_blend(cmd->c, below, *rect, above, mode); });
 }
 int zs_cmd_color_matrix(zs_cmd *cmd, uint32_t src, const float matrix[9], uint32_t *reg) {
-    return guarded([&] { NEED(cmd); NEED(matrix); NEED(reg); *reg = cmd_color_matrix(cmd->c, src, matrix); });
+    return cmd_guarded(cmd, [&] { NEED(cmd); NEED(matrix); NEED(reg); *reg = cmd_color_matrix(cmd->c, src, matrix); });
 }
 int zs_cmd_output(zs_cmd *cmd, uint32_t src, uint32_t *reg, zs_descriptor *outformat) {
-    return guarded([&] { NEED(cmd); NEED(reg); *reg = cmd_output(cmd->c, src, outformat); });
+    return cmd_guarded(cmd, [&] { NEED(cmd); NEED(reg); *reg = cmd_output(cmd->c, src, outformat); });
 }
+int zs_cmd_with_knob(zs_cmd *cmd) {
+    return guarded([&] {
+        NEED(cmd);
+        cmd->c.pending_knob = true;
+    });
+}
+
+int zs_cmd_with_buffer(zs_cmd *cmd, uint32_t buffer) {
+    return guarded([&] {
+        NEED(cmd);
+        if (buffer >= cmd->c.ops.size()) fail(ZS_ERR_BAD_REGISTER, "no such register");
+        if (cmd->c.ops[buffer].kind != OpKind::BufferInit) fail(ZS_ERR_TYPE, "register is not a buffer");
+        cmd->c.pending_buffer = (int32_t)buffer;
+    });
+}
+
 int zs_cmd_describe(const zs_cmd *cmd, uint32_t reg, zs_descriptor *out) {
     return guarded([&] { NEED(cmd); NEED(out); *out = cmd->c.describe(reg); });
 }
@@ -448,6 +486,60 @@ int zs_executable_kernel_count(const zs_executable *exe, uint32_t *count) {
     });
 }
 
+int zs_executable_io_count(const zs_executable *exe, uint32_t *inputs, uint32_t *outputs) {
+    return guarded([&] {
+        NEED(exe);
+        if (inputs) *inputs = (uint32_t)exe->e->input_regs.size();
+        if (outputs) *outputs = (uint32_t)exe->e->output_regs.size();
+    });
+}
+
+int zs_executable_query_knob(const zs_executable *exe, uint32_t link_idx, uint32_t reg, uint32_t *knob,
+                             uint64_t *len) {
+    return guarded([&] {
+        NEED(exe); NEED(knob);
+        if (link_idx != 0) fail(ZS_ERR_BAD_REGISTER, "only link index 0 (the program itself) has knobs");
+        const Executable &E = *exe->e;
+        for (size_t i = 0; i < E.knobs.size(); ++i)
+            if (E.knobs[i].reg == reg) {
+                *knob = (uint32_t)i;
+                if (len) *len = E.knobs[i].len;
+                return;
+            }
+        fail(ZS_ERR_BAD_REGISTER, "register has no knob");
+    });
+}
+
+int zs_executable_set_knob(zs_executable *exe, uint32_t knob, const void *data, uint64_t len) {
+    return guarded([&] {
+        NEED(exe); NEED(data);
+        Executable &E = *exe->e;
+        if (knob >= E.knobs.size()) fail(ZS_ERR_INVALID_ARG, "no such knob");
+        const KnobInfo &K = E.knobs[knob];
+        if (len != K.len) fail(ZS_ERR_INVALID_ARG, "knob data length differs from the knob's parameter block");
+        const uint8_t *bytes = (const uint8_t *)data;
+        for (const KnobSite &site : K.sites) {
+            if (site.step >= 0) {
+                const std::vector<float> c = knob_cons(site.kind, bytes, len);
+                for (size_t i = 0; i < c.size(); ++i) E.steps[site.step].raster.cons[i] = c[i];
+            } else {
+                Slot &sl = E.slots[site.slot];
+                std::memcpy(sl.table.data(), bytes, std::min<uint64_t>(len, sl.table.size()));
+                if (!E.dev_buffers.empty() && E.dev_buffers[site.slot])
+                    check_cuda(cudaMemcpy(E.dev_buffers[site.slot], sl.table.data(), sl.bytes, cudaMemcpyHostToDevice),
+                               "knob upload");
+            }
+        }
+        // Graphs captured the old parameters.
+        for (auto &kv : E.graphs) cudaGraphExecDestroy(kv.second);
+        E.graphs.clear();
+        E.graph_order.clear();
+        for (auto &kv : exe->batch_graphs) cudaGraphExecDestroy(kv.second);
+        exe->batch_graphs.clear();
+        exe->batch_order.clear();
+    });
+}
+
 const char *zs_executable_describe(const zs_executable *exe) { return exe ? exe->e->plan_text.c_str() : ""; }
 
 // ---------------------------------------------------------------- environment / execution
@@ -480,6 +572,18 @@ int zs_env_bind(zs_environment *env, uint32_t reg, uint64_t key) {
             fail(ZS_ERR_MISMATCHED_DESCRIPTOR, "bound image " + describe(img.desc) + " does not match input " +
                                                    describe(E.input_desc[i]));
         env->env.binds[reg] = key;
+    });
+}
+
+int zs_env_knob(zs_environment *env, uint32_t knob, const void *data, uint64_t len) {
+    return guarded([&] {
+        NEED(env); NEED(data);
+        const Executable &E = *env->env.exe;
+        if (knob >= E.knobs.size()) fail(ZS_ERR_INVALID_ARG, "no such knob");
+        if (len != E.knobs[knob].len) fail(ZS_ERR_INVALID_ARG, "knob data length differs from the knob's parameter block");
+        for (const KnobSite &site : E.knobs[knob].sites)
+            if (site.step >= 0) (void)knob_cons(site.kind, (const uint8_t *)data, len);   // validate
+        env->env.knob_data[knob].assign((const uint8_t *)data, (const uint8_t *)data + len);
     });
 }
 
@@ -524,6 +628,29 @@ int zs_launch(zs_executable *exe, zs_environment *env, zs_execution **out) {
                 x->args.push_back((int)i);
             }
         }
+        // Environment::knob (run.rs:1292-1306): this launch's parameter blocks replace the
+        // static ones -- producer constants patched at launch, table slots copied into
+        // buffers owned by the execution (Low::BufferInit, run.rs:1588-1606).
+        for (const auto &kv : env->env.knob_data) {
+            const KnobInfo &K = E.knobs[kv.first];
+            for (const KnobSite &site : K.sites) {
+                if (site.step >= 0) {
+                    ConsPatch p;
+                    p.step = (size_t)site.step;
+                    p.cons = knob_cons(site.kind, kv.second.data(), kv.second.size());
+                    X.patches.push_back(p);
+                } else {
+                    const Slot &sl = E.slots[site.slot];
+                    std::vector<uint8_t> bytes(sl.table);
+                    std::memcpy(bytes.data(), kv.second.data(), std::min(bytes.size(), kv.second.size()));
+                    void *buf = nullptr;
+                    check_cuda(cudaMalloc(&buf, sl.bytes), "cudaMalloc");
+                    X.owned.push_back(buf);
+                    check_cuda(cudaMemcpy(buf, bytes.data(), sl.bytes, cudaMemcpyHostToDevice), "knob upload");
+                    X.ptrs[site.slot] = buf;
+                }
+            }
+        }
         for (size_t s = 0; s < E.steps.size(); ++s) {
             x->kinds.push_back(1);
             x->args.push_back((int)s);
@@ -549,7 +676,7 @@ int zs_exec_step(zs_execution *exec) {
                                          row_bytes(img.desc), img.desc.height, cudaMemcpyHostToDevice, X.stream),
                        "input upload");
         } else {
-            E.record_range(X.stream, X.ptrs, (size_t)arg, (size_t)arg + 1);
+            E.record_range(X.stream, X.ptrs, (size_t)arg, (size_t)arg + 1, &X.patches);
         }
         X.cursor++;
     });
@@ -811,6 +938,157 @@ int zs_batch_thumbnails(zs_executable *chain, const void *const *images, const u
         cudaStream_t s = stream ? (cudaStream_t)stream : exe_stream(chain);
         int rc = batch_thumbnails(chain->e.get(), images, widths, heights, n, canvas, out, s);
         if (rc != ZS_OK) fail(rc, last_error());
+    });
+}
+
+// ---------------------------------------------------------------- batches of runs
+
+// The texel alignment a kernel needs of a buffer of this slot (see zs_run_device).
+static bool slot_aligned(const Executable &E, int slot, const void *p) {
+    const uint32_t bpp = E.slots[slot].fmt.bpp;
+    const uintptr_t a = bpp >= 16 ? 16 : (bpp & 7) == 0 ? 8 : (bpp & 3) == 0 ? 4 : (bpp & 1) == 0 ? 2 : 1;
+    return ((uintptr_t)p & (a - 1)) == 0;
+}
+
+// n runs of one executable recorded into one CUDA graph: run i on capture stream
+// i % branches, all forked from and joined back into `s`, so runs on different branches may
+// execute at the same time.  An executable that stores intermediates in its own buffers
+// records its runs on one branch, one after another.
+static cudaGraphExec_t capture_batch(zs_executable *exe, const std::vector<void *> &table, uint32_t n,
+                                     cudaStream_t s) {
+    Executable &E = *exe->e;
+    const size_t ni = E.input_regs.size(), no = E.output_regs.size();
+    for (cudaStream_t &t : exe->branches)
+        if (!t) check_cuda(cudaStreamCreateWithFlags(&t, cudaStreamNonBlocking), "stream");
+    for (cudaEvent_t &ev : exe->joins)
+        if (!ev) check_cuda(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming), "event");
+    if (!exe->fork) check_cuda(cudaEventCreateWithFlags(&exe->fork, cudaEventDisableTiming), "event");
+    bool shared = false;
+    for (const Slot &sl : E.slots) shared = shared || sl.kind == SlotKind::Intermediate;
+    const uint32_t nb = shared ? 1u : std::min<uint32_t>(n, ZS_BATCH_BRANCHES);
+    check_cuda(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+    cudaGraph_t g = nullptr;
+    try {
+        check_cuda(cudaEventRecord(exe->fork, s), "fork");
+        for (uint32_t b = 0; b < nb; ++b) check_cuda(cudaStreamWaitEvent(exe->branches[b], exe->fork, 0), "fork wait");
+        for (uint32_t i = 0; i < n; ++i) {
+            std::vector<void *> ptrs = E.dev_buffers;
+            for (size_t k = 0; k < ni; ++k) ptrs[E.input_slot[k]] = table[i * (ni + no) + k];
+            for (size_t k = 0; k < no; ++k) ptrs[E.output_slot[k]] = table[i * (ni + no) + ni + k];
+            E.record(exe->branches[i % nb], ptrs);
+        }
+        for (uint32_t b = 0; b < nb; ++b) {
+            check_cuda(cudaEventRecord(exe->joins[b], exe->branches[b]), "join");
+            check_cuda(cudaStreamWaitEvent(s, exe->joins[b], 0), "join wait");
+        }
+    } catch (...) {
+        cudaStreamEndCapture(s, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+    }
+    check_cuda(cudaStreamEndCapture(s, &g), "end capture");
+    cudaGraphExec_t ge = nullptr;
+    const cudaError_t e = cudaGraphInstantiate(&ge, g, 0);
+    cudaGraphDestroy(g);
+    check_cuda(e, "graph instantiate");
+    return ge;
+}
+
+static void batch_run_device(zs_executable *exe, const void *const *inputs, void *const *outputs, uint32_t n,
+                             cudaStream_t s) {
+    Executable &E = *exe->e;
+    const size_t ni = E.input_regs.size(), no = E.output_regs.size();
+    E.ensure_buffers();
+    std::vector<void *> table((ni + no) * n);
+    for (uint32_t i = 0; i < n; ++i) {
+        for (size_t k = 0; k < ni; ++k) {
+            const void *p = inputs[i * ni + k];
+            NEED(p);
+            if (!slot_aligned(E, E.input_slot[k], p)) fail(ZS_ERR_INVALID_ARG, "input buffer is not texel aligned");
+            table[i * (ni + no) + k] = const_cast<void *>(p);
+        }
+        for (size_t k = 0; k < no; ++k) {
+            void *p = outputs[i * no + k];
+            NEED(p);
+            if (!slot_aligned(E, E.output_slot[k], p)) fail(ZS_ERR_INVALID_ARG, "output buffer is not texel aligned");
+            table[i * (ni + no) + ni + k] = p;
+        }
+    }
+    auto it = exe->batch_graphs.find(table);
+    if (it == exe->batch_graphs.end()) {
+        if (exe->batch_graphs.size() >= 8) {
+            auto victim = exe->batch_graphs.find(exe->batch_order.front());
+            if (victim != exe->batch_graphs.end()) {
+                cudaGraphExecDestroy(victim->second);
+                exe->batch_graphs.erase(victim);
+            }
+            exe->batch_order.erase(exe->batch_order.begin());
+        }
+        it = exe->batch_graphs.emplace(table, capture_batch(exe, table, n, s)).first;
+        exe->batch_order.push_back(table);
+    }
+    check_cuda(cudaGraphLaunch(it->second, s), "graph launch");
+    for (uint32_t i = 0; i < n; ++i) note_graph_launch(E);
+}
+
+int zs_batch_run_device(zs_executable *exe, const void *const *inputs, void *const *outputs, uint32_t n,
+                        void *stream) {
+    return guarded([&] {
+        NEED(exe);
+        if (n == 0) return;
+        NEED(inputs); NEED(outputs);
+        cudaStream_t s = stream ? (cudaStream_t)stream : exe_stream(exe);
+        batch_run_device(exe, inputs, outputs, n, s);
+    });
+}
+
+int zs_batch_run(zs_executable *exe, zs_pool *pool, const uint64_t *keys, uint32_t n, uint64_t *out_keys) {
+    return guarded([&] {
+        NEED(exe); NEED(pool);
+        if (n == 0) return;
+        NEED(keys); NEED(out_keys);
+        Executable &E = *exe->e;
+        const size_t ni = E.input_regs.size(), no = E.output_regs.size();
+        E.ensure_buffers();
+        // Inputs: bound pool images, made device resident (Pool::upload).
+        std::vector<const void *> ins(n * ni);
+        for (uint32_t i = 0; i < n; ++i)
+            for (size_t k = 0; k < ni; ++k) {
+                PoolImage &img = pool->p.get(keys[i * ni + k]);
+                if (!desc_matches(img.desc, E.input_desc[k]))
+                    fail(ZS_ERR_MISMATCHED_DESCRIPTOR, "bound image " + describe(img.desc) + " does not match input " +
+                                                           describe(E.input_desc[k]));
+                pool_upload(img);
+                ins[i * ni + k] = img.dev;
+            }
+        // Outputs: new pool images with device storage, retired into the pool (Retire::output).
+        std::vector<uint64_t> made;
+        std::vector<void *> outs(n * no);
+        try {
+            for (uint32_t i = 0; i < n; ++i)
+                for (size_t k = 0; k < no; ++k) {
+                    const Desc &d = E.output_desc[k];
+                    const uint64_t key = pool_add(pool->p, d);
+                    made.push_back(key);
+                    PoolImage &img = pool->p.get(key);
+                    img.dev_len = row_bytes(d) * d.height;
+                    check_cuda(cudaMalloc(&img.dev, img.dev_len), "cudaMalloc");
+                    img.host_valid = false;
+                    outs[i * no + k] = img.dev;
+                }
+            cudaStream_t s = exe_stream(exe);
+            batch_run_device(exe, ins.data(), outs.data(), n, s);
+            check_cuda(cudaStreamSynchronize(s), "synchronize");
+        } catch (...) {
+            for (uint64_t key : made) pool->p.images.erase(key);
+            throw;
+        }
+        for (size_t j = 0; j < made.size(); ++j) {
+            PoolImage &img = pool->p.get(made[j]);
+            img.dev_valid = true;
+            pool_sync_host(img);
+            out_keys[j] = made[j];
+        }
     });
 }
 

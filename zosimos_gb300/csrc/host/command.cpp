@@ -8,7 +8,49 @@
 
 namespace zs {
 
+uint64_t knob_param_bytes(OpKind kind) {
+    switch (kind) {
+    case OpKind::Bilinear: return 6 * 16;     // shaders/bilinear.rs into_std430
+    case OpKind::Solid: return 16;            // shaders/solid_rgb.rs [f32; 4]
+    case OpKind::Normal2d: return 32;         // shaders/distribution_normal2d.rs [f32; 8]
+    case OpKind::FractalNoise: return 24;     // shaders/fractal_noise.rs, aligned to 8
+    default: return 0;
+    }
+}
+
+std::vector<float> knob_cons(OpKind kind, const uint8_t *data, uint64_t len) {
+    const uint64_t need = knob_param_bytes(kind);
+    if (!need || len < need) fail(ZS_ERR_INVALID_ARG, "parameter block too short for this operation");
+    std::vector<float> f(need / 4);
+    std::memcpy(f.data(), data, need);
+    if (kind == OpKind::Normal2d) f.resize(7);
+    if (kind == OpKind::FractalNoise) {
+        uint32_t octaves;
+        std::memcpy(&octaves, data + 16, 4);
+        if (octaves > 32) fail(ZS_ERR_INVALID_ARG, "fractal noise octaves above 32");
+        f.resize(5);
+        f[4] = (float)octaves;
+    }
+    return f;
+}
+
 uint32_t Command::push(Op op) {
+    // CommandBuffer::with_knob / with_buffer apply to exactly this op (command.rs:1740-1765).
+    const bool knob = pending_knob;
+    const int32_t buffer = pending_buffer;
+    clear_pending();
+    if (knob) {
+        if (!knob_param_bytes(op.kind) && op.kind != OpKind::BufferInit)
+            fail(ZS_ERR_UNIMPLEMENTED, "this operation takes no knob (bilinear, solid_rgba, distribution_normal2d, "
+                                       "distribution_fractal_noise and buffer_init do)");
+        op.knob = true;
+    }
+    if (buffer >= 0) {
+        const uint64_t need = knob_param_bytes(op.kind);
+        if (!need) fail(ZS_ERR_UNIMPLEMENTED, "this operation takes no parameters from a buffer");
+        if (ops[buffer].len < need) fail(ZS_ERR_OTHER, "buffer shorter than the operation's parameters");
+        op.param_buffer = buffer;
+    }
     ops.push_back(std::move(op));
     return (uint32_t)ops.size() - 1;
 }

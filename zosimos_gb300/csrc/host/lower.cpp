@@ -35,6 +35,10 @@ struct Pending {
     std::string label;
     // ZS_PR_LAYERS: base (src_slot[0] when has_below, else a.cons[0..3]) and the layers.
     std::vector<LayerRef> layers;
+    // A knob whose parameter block feeds this launch's producer constants (or -1), and the
+    // construct whose layout those constants follow.
+    int knob = -1;
+    OpKind knob_kind = OpKind::BufferInit;
 };
 
 struct Val {
@@ -54,6 +58,33 @@ struct Planner {
     Planner(const Program &p, Executable &e) : P(p), E(e) {}
 
     const Desc &desc(uint32_t r) const { return P.ops[r].desc; }
+
+    // The knob declared on register `reg` (parameter block of `len` bytes), created on first use.
+    int knob_of(uint32_t reg, uint64_t len) {
+        for (size_t i = 0; i < E.knobs.size(); ++i)
+            if (E.knobs[i].reg == reg) return (int)i;
+        KnobInfo k;
+        k.reg = reg;
+        k.len = len;
+        E.knobs.push_back(k);
+        return (int)E.knobs.size() - 1;
+    }
+
+    // Producer constants of a parameterised construct: its own parameters, or those read from a
+    // buffer (CommandBuffer::with_buffer); registers the knob the constants answer to.
+    void construct_params(uint32_t r, const Op &op, Pending &p, float *cons, int n) {
+        if (op.param_buffer >= 0) {
+            const Op &b = P.ops[op.param_buffer];
+            std::vector<uint8_t> bytes(b.data);
+            bytes.resize(std::max<uint64_t>(b.len, knob_param_bytes(op.kind)), 0);
+            const std::vector<float> f = knob_cons(op.kind, bytes.data(), bytes.size());
+            for (int k = 0; k < n && k < (int)f.size(); ++k) cons[k] = f[k];
+            if (b.knob) p.knob = knob_of((uint32_t)op.param_buffer, b.len);
+        } else {
+            for (int k = 0; k < n; ++k) cons[k] = op.fparams[k];
+            if (op.knob) p.knob = knob_of(r, knob_param_bytes(op.kind));
+        }
+    }
 
     int new_slot(SlotKind k, int w, int h, const ZsFormat &f, uint32_t reg = 0) {
         Slot s;
@@ -198,6 +229,13 @@ struct Planner {
         Step st;
         st.kind = StepKind::Raster;
         st.label = p.label;
+        if (p.knob >= 0) {
+            KnobSite site;
+            site.step = (int)E.steps.size();
+            site.kind = p.knob_kind;
+            E.knobs[p.knob].sites.push_back(site);
+            st.label += " [knob]";
+        }
         st.raster = p.a;
         st.raster.dst_stride = d.stride;
         st.raster.dst_fmt = d.fmt;
@@ -451,7 +489,7 @@ struct Planner {
     bool solid_value(uint32_t reg, float out[4]) {
         Val &v = vals[reg];
         if (E.mode != ZS_MODE_FUSED || v.materialized || !v.pend || v.pend->a.producer != ZS_PR_SOLID ||
-            out_slot_of[reg] >= 0)
+            out_slot_of[reg] >= 0 || v.pend->knob >= 0)
             return false;
         HProgram p = v.pend->prog;
         p.optimise();
@@ -733,12 +771,14 @@ struct Planner {
             } break;
             case OpKind::Bilinear: {
                 auto p = new_pending(ZS_PR_BILINEAR, d.width, d.height, "bilinear");
-                for (int k = 0; k < 24; ++k) p->a.cons[k] = op.fparams[k];
+                p->knob_kind = OpKind::Bilinear;
+                construct_params(r, op, *p, p->a.cons, 24);
                 set_pending(r, std::move(p));
             } break;
             case OpKind::Solid: {
                 auto p = new_pending(ZS_PR_SOLID, d.width, d.height, "solid");
-                for (int k = 0; k < 4; ++k) p->a.cons[k] = op.fparams[k];
+                p->knob_kind = OpKind::Solid;
+                construct_params(r, op, *p, p->a.cons, 4);
                 set_pending(r, std::move(p));
             } break;
             case OpKind::Resize: {
@@ -779,7 +819,8 @@ struct Planner {
             } break;
             case OpKind::Normal2d: {
                 auto p = new_pending(ZS_PR_NORMAL2D, d.width, d.height, "distribution normal2d");
-                for (int k = 0; k < 7; ++k) p->a.cons[k] = op.fparams[k];
+                p->knob_kind = OpKind::Normal2d;
+                construct_params(r, op, *p, p->a.cons, 7);
                 set_pending(r, std::move(p));
             } break;
             case OpKind::BufferInit:
@@ -794,6 +835,12 @@ struct Planner {
                 std::vector<uint8_t> bytes((size_t)stride * d.height, 0);
                 if (!b.data.empty()) std::memcpy(bytes.data(), b.data.data(), std::min(bytes.size(), b.data.size()));
                 const int s = table_slot(bytes.data(), bytes.size());
+                if (b.knob) {
+                    KnobSite site;
+                    site.slot = s;
+                    site.kind = OpKind::BufferInit;
+                    E.knobs[knob_of(op.a, b.len)].sites.push_back(site);
+                }
                 Slot &sl = E.slots[s];
                 sl.width = d.width;
                 sl.height = d.height;
@@ -805,7 +852,8 @@ struct Planner {
             } break;
             case OpKind::FractalNoise: {
                 auto p = new_pending(ZS_PR_FRACTAL, d.width, d.height, "distribution fractal noise");
-                for (int k = 0; k < 5; ++k) p->a.cons[k] = op.fparams[k];
+                p->knob_kind = OpKind::FractalNoise;
+                construct_params(r, op, *p, p->a.cons, 5);
                 // The rotation between octaves, 2 mat3(cos .5, sin .5, 1, -sin .5, cos .5, 1, 0, 0, 1)
                 // (fractal_noise.frag), its constants rounded to f32 before the doubling.
                 p->a.cons[5] = 2.0f * (float)std::cos(0.5);

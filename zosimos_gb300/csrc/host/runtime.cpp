@@ -59,7 +59,13 @@ PoolImage &Pool::get(uint64_t key) {
 
 Executable::~Executable() {
     for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
+    if (batch_graph) cudaGraphExecDestroy(batch_graph);
+    if (batch_done) {
+        cudaEventSynchronize(batch_done);
+        cudaEventDestroy(batch_done);
+    }
     if (batch_scratch) cudaFree(batch_scratch);
+    if (batch_staging) cudaFreeHost(batch_staging);
     if (graph_stream) cudaStreamDestroy(graph_stream);
     for (void *p : dev_buffers)
         if (p) cudaFree(p);
@@ -123,7 +129,8 @@ struct DeviceScope {
     }
 };
 
-void Executable::record_range(cudaStream_t stream, const std::vector<void *> &ptrs, size_t begin, size_t end) {
+void Executable::record_range(cudaStream_t stream, const std::vector<void *> &ptrs, size_t begin, size_t end,
+                              const std::vector<ConsPatch> *patches) {
     DeviceScope scope(device);
     for (size_t k = begin; k < end && k < steps.size(); ++k) {
         const Step &st = steps[k];
@@ -161,9 +168,14 @@ void Executable::record_range(cudaStream_t stream, const std::vector<void *> &pt
             cudaGetLastError();
             check_cuda(launch_raster(raster_args(st, ptrs), sm_count, stream), st.label.c_str());
         } break;
-        case StepKind::Raster:
-            check_cuda(launch_raster(raster_args(st, ptrs), sm_count, stream), st.label.c_str());
-            break;
+        case StepKind::Raster: {
+            ZsRasterArgs a = raster_args(st, ptrs);
+            if (patches)
+                for (const ConsPatch &p : *patches)
+                    if (p.step == k)
+                        for (size_t i = 0; i < p.cons.size() && i < 24; ++i) a.cons[i] = p.cons[i];
+            check_cuda(launch_raster(a, sm_count, stream), st.label.c_str());
+        } break;
         }
     }
 }

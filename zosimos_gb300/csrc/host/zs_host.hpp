@@ -103,10 +103,25 @@ struct Op {
     HProgram prog;               // per-pixel semantics of colour ops
     std::vector<uint8_t> data;   // BufferInit: initial bytes (zero-extended to `len`)
     uint64_t len = 0;            // BufferInit: buffer size in bytes
+    bool knob = false;           // WithKnob: the parameters can be replaced at run time
+    int32_t param_buffer = -1;   // WithBuffer: parameters read from this buffer register
 };
+
+// Bytes of the parameter block of a knob-capable op (the reference's uniform layouts):
+// bilinear 6 vec4, solid_rgba vec4, distribution_normal2d 8 f32, fractal noise
+// (vec2, f32, f32, u32) aligned to 8; 0 for ops that take no knob.
+uint64_t knob_param_bytes(OpKind kind);
+// Producer constants (ZsRasterArgs::cons) of a parameter block; throws on a bad block.
+std::vector<float> knob_cons(OpKind kind, const uint8_t *data, uint64_t len);
 
 struct Command {
     std::vector<Op> ops;
+    bool pending_knob = false;       // CommandBuffer::with_knob: applies to the next op
+    int32_t pending_buffer = -1;     // CommandBuffer::with_buffer: applies to the next op
+    void clear_pending() {
+        pending_knob = false;
+        pending_buffer = -1;
+    }
     uint32_t push(Op op);
     const Desc &describe(uint32_t reg) const;
     bool is_value(uint32_t reg) const;
@@ -173,6 +188,26 @@ struct Step {
     std::string label;
 };
 
+// Where the bytes of a knob land: the constants of a raster step's producer (step >= 0,
+// interpreted for `kind`) or a constant table slot holding the bytes (slot >= 0).
+struct KnobSite {
+    int step = -1;
+    int slot = -1;
+    OpKind kind = OpKind::BufferInit;
+};
+
+struct KnobInfo {
+    uint32_t reg = 0;            // the register the knob was declared on (RegisterKnob)
+    uint64_t len = 0;            // bytes of its parameter block
+    std::vector<KnobSite> sites;
+};
+
+// A knob value applied to one launch: new producer constants of a step.
+struct ConsPatch {
+    size_t step = 0;
+    std::vector<float> cons;
+};
+
 struct Executable {
     int device = 0;
     uint32_t mode = ZS_MODE_FUSED;
@@ -185,9 +220,16 @@ struct Executable {
     std::vector<Desc> input_desc, output_desc;
     std::vector<int> input_slot, output_slot;
     std::vector<void *> dev_buffers;                   // device allocation per slot (owned ones)
-    void *batch_scratch = nullptr;                     // batched thumbnails: image table + queue head
+    // zs_batch_thumbnails: device image/prefix tables, their pinned staging copy, the event of
+    // the last batch and its captured graph (memset + kernel) with the key it was captured for
+    void *batch_scratch = nullptr;
+    void *batch_staging = nullptr;
     size_t batch_bytes = 0;
+    cudaEvent_t batch_done = nullptr;
+    cudaGraphExec_t batch_graph = nullptr;
+    std::vector<uint64_t> batch_key;
     std::string plan_text;
+    std::vector<KnobInfo> knobs;                      // Executable::query_knob
     // CUDA graphs of the launch sequence for zs_run_device, keyed by the bound pointers
     std::map<std::vector<void *>, cudaGraphExec_t> graphs;
     std::vector<std::vector<void *>> graph_order;     // insertion order for eviction
@@ -195,7 +237,8 @@ struct Executable {
     ~Executable();
     void ensure_buffers();
     void record(cudaStream_t stream, const std::vector<void *> &ptrs);
-    void record_range(cudaStream_t stream, const std::vector<void *> &ptrs, size_t begin, size_t end);
+    void record_range(cudaStream_t stream, const std::vector<void *> &ptrs, size_t begin, size_t end,
+                      const std::vector<ConsPatch> *patches = nullptr);
 };
 
 std::unique_ptr<Executable> lower(const Program &prog, const zs_capabilities &caps);
@@ -226,6 +269,7 @@ struct Environment {
     Pool *pool = nullptr;
     std::map<uint32_t, uint64_t> binds;          // input register -> key
     std::map<uint32_t, uint64_t> output_binds;   // output register -> key
+    std::map<uint32_t, std::vector<uint8_t>> knob_data;   // Environment::knob: knob -> bytes
 };
 
 struct Execution {
@@ -238,6 +282,7 @@ struct Execution {
     size_t cursor = 0;                           // next instruction
     size_t total = 0;
     std::vector<uint64_t> input_keys;
+    std::vector<ConsPatch> patches;              // knob values of this launch
     ~Execution();
 };
 

@@ -1,18 +1,26 @@
 // k_batch.cu -- many RGBA8 sRGB images of uneven sizes turned into thumbnails by one
-// persistent launch over a device work queue (the reference's batch-reuse case runs one
-// Executable per image, lib/zosimos/tests/loop.rs:84-95).
+// launch over a static work list (the reference's batch-reuse case runs one Executable per
+// image, lib/zosimos/tests/loop.rs:84-95).
 //
 // Per image: decode -> the fused colour chain of a lowered Program (canonical form
 // M_a, [cbrt], M_b, [cube], M_c, [clamp], M_d, linear result) -> box (area coverage)
 // fit-resize so the long side is `canvas` -> centred inscribe on a transparent
 // canvas x canvas image -> exact sRGB8 encode.  The canvases are zero-filled (the
 // transparent margins) by one memset; the fitted pixels are cut into work items of 32
-// adjacent pixels of one row, one item per warp, so the 32 lanes have windows of the
-// same size.  Warps take items by static striding over all images (a prefix table and a
-// binary search find the image of an item), which spreads every image's cost over all
-// warps without atomics or barriers.  Each lane computes its output pixel from its source
-// window: the box weights are separable, the source texels of a window row go through
-// the colour chain two at a time in FP32x2 registers.
+// output columns x ZS_BATCH_ROWS output rows, one item per warp, taken by static striding
+// over all images (no atomics, no barriers), so that every image's cost spreads over all warps.
+//
+// The colour chain is nonlinear, so it runs on every source texel before the box filter;
+// the kernel is built so that each texel goes through it once:
+//  * lane l owns output column u; its box window covers texels [j0, j1) of a source row, with
+//    weight 1 inside and fractional weights only at the two ends;
+//  * on a downscale the windows tile the row, so the last texel of lane l is the first texel
+//    of lane l + 1: lane l + 1 computes it and hands its unweighted value over with a warp
+//    shuffle, lane l applies its own edge weight;
+//  * consecutive output rows share one source row: the horizontal sums of the last row of an
+//    output row are kept in registers and reused by the next one;
+//  * texels go through the chain two at a time in FP32x2 registers (decode from the
+//    lane-replicated shared table, MUFU cube roots, the rank-1 Oklab L/C form when planned).
 #include <cstring>
 #include <vector>
 
@@ -22,6 +30,7 @@
 #include "zs_kernels.h"
 
 #define ZS_BATCH_THREADS 256
+#define ZS_BATCH_ROWS 8        // output rows per work item
 
 struct ZsBatchImage {
     const uint8_t *ptr;
@@ -40,34 +49,14 @@ struct ZsBatchArgs {
     int32_t canvas;
     int32_t flags;
     int32_t pad;
-    float m[4][9];
-    float m2[4][9][2];         // the same matrices with every coefficient duplicated (f32x2 operands)
+    float m2[4][9][2];         // the chain's matrices with every coefficient duplicated (f32x2 operands)
+    float mb_v[3][2];          // ZS_CHAIN_MB_RANK1: M_b = d I + (1,1,1)^T v
+    float mb_d[2];
 };
 
-__device__ __forceinline__ void zs_batch_m3(const float *m, float &r, float &g, float &b) {
-    float x = r, y = g, z = b;
-    r = fmaf(m[0], x, fmaf(m[1], y, m[2] * z));
-    g = fmaf(m[3], x, fmaf(m[4], y, m[5] * z));
-    b = fmaf(m[6], x, fmaf(m[7], y, m[8] * z));
-}
-
-// Linear result of the canonical chain for one RGBA8 sRGB texel.
-__device__ __forceinline__ float4 zs_batch_chain(uint32_t w, const ZsBatchArgs &a) {
-    float r = zs_srgb_decode_lut[w & 255u], g = zs_srgb_decode_lut[(w >> 8) & 255u],
-          b = zs_srgb_decode_lut[(w >> 16) & 255u];
-    zs_batch_m3(a.m[0], r, g, b);
-    if (a.flags & ZS_CHAIN_CBRT) { r = zs_scbrt(r); g = zs_scbrt(g); b = zs_scbrt(b); }
-    zs_batch_m3(a.m[1], r, g, b);
-    if (a.flags & ZS_CHAIN_CUBE) { r = r * r * r; g = g * g * g; b = b * b * b; }
-    zs_batch_m3(a.m[2], r, g, b);
-    if (a.flags & ZS_CHAIN_CLAMP) { r = __saturatef(r); g = __saturatef(g); b = __saturatef(b); }
-    zs_batch_m3(a.m[3], r, g, b);
-    return make_float4(r, g, b, (float)(w >> 24) / 255.0f);
-}
-
-// The same chain on two texels at once: decode through the lane-replicated shared table
-// of the chain kernel, FP32x2 matrix products, MUFU cube roots.
-template <bool NONNEG>
+// The canonical chain on two texels at once, linear result: decode through the
+// lane-replicated shared table, FP32x2 matrix products, MUFU cube roots.
+template <bool NONNEG, bool RANK1>
 __device__ __forceinline__ void zs_batch_chain2(uint32_t w0, uint32_t w1, const unsigned char *lut, uint32_t lane4,
                                                 const ZsBatchArgs &a, float2 &r, float2 &g, float2 &b) {
     r = make_float2(zs_dec<0>(lut, w0, lane4), zs_dec<0>(lut, w1, lane4));
@@ -85,7 +74,16 @@ __device__ __forceinline__ void zs_batch_chain2(uint32_t w0, uint32_t w1, const 
             b = make_float2(zs_cbrt1<false>(b.x), zs_cbrt1<false>(b.y));
         }
     }
-    zs_m3x2<false>(a.m2[1], r, g, b);
+    if (RANK1) {
+        const float2 *v = reinterpret_cast<const float2 *>(a.mb_v);
+        const float2 d = *reinterpret_cast<const float2 *>(a.mb_d);
+        const float2 t = __ffma2_rn(v[0], r, __ffma2_rn(v[1], g, __fmul2_rn(v[2], b)));
+        r = __ffma2_rn(d, r, t);
+        g = __ffma2_rn(d, g, t);
+        b = __ffma2_rn(d, b, t);
+    } else {
+        zs_m3x2<false>(a.m2[1], r, g, b);
+    }
     if (a.flags & ZS_CHAIN_CUBE) {
         r = __fmul2_rn(__fmul2_rn(r, r), r);
         g = __fmul2_rn(__fmul2_rn(g, g), g);
@@ -105,61 +103,105 @@ __device__ __forceinline__ void zs_box_window(int u, float s, float f, int len, 
     j1 = min((int)ceilf(hi), len);
 }
 
-template <bool NONNEG>
-__global__ void __launch_bounds__(ZS_BATCH_THREADS) zs_batch_kernel(const __grid_constant__ ZsBatchArgs a) {
+// This lane's horizontally weighted sum of one source row (colour in xyz, alpha code sum in
+// w): texels [j0, jend) through the chain, weight wfirst at j0, wlast at j1 - 1, 1 between;
+// when `share`, texel j1 - 1 is the next lane's first texel and arrives by shuffle.  Every
+// lane of the warp calls this together (the shuffles use the full mask).
+template <bool NONNEG, bool RANK1>
+__device__ __forceinline__ float4 zs_batch_row(const uint32_t *row, int j0, int jend, int j1, float wfirst, float wlast,
+                                               bool share, const unsigned char *lut, uint32_t lane4,
+                                               const ZsBatchArgs &a) {
+    float2 sr = make_float2(0.f, 0.f), sg = sr, sb = sr, sa = sr;
+    float4 first = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int jx = j0; jx < jend; jx += 2) {
+        const bool two = jx + 1 < jend;
+        const uint32_t w0 = __ldg(row + jx), w1 = two ? __ldg(row + jx + 1) : w0;
+        float2 r, g, b;
+        zs_batch_chain2<NONNEG, RANK1>(w0, w1, lut, lane4, a, r, g, b);
+        const float2 al = make_float2(__uint2float_rn(w0 >> 24), __uint2float_rn(w1 >> 24));
+        if (jx == j0) first = make_float4(r.x, g.x, b.x, al.x);
+        const float2 wx = make_float2(jx == j0 ? wfirst : (jx == j1 - 1 ? wlast : 1.f),
+                                      two ? (jx + 1 == j1 - 1 ? wlast : 1.f) : 0.f);
+        sr = __ffma2_rn(wx, r, sr);
+        sg = __ffma2_rn(wx, g, sg);
+        sb = __ffma2_rn(wx, b, sb);
+        sa = __ffma2_rn(wx, al, sa);
+    }
+    float4 rs = make_float4(sr.x + sr.y, sg.x + sg.y, sb.x + sb.y, sa.x + sa.y);
+    const float nr = __shfl_down_sync(0xffffffffu, first.x, 1), ng = __shfl_down_sync(0xffffffffu, first.y, 1);
+    const float nb = __shfl_down_sync(0xffffffffu, first.z, 1), na = __shfl_down_sync(0xffffffffu, first.w, 1);
+    if (share) {
+        rs.x = fmaf(wlast, nr, rs.x);
+        rs.y = fmaf(wlast, ng, rs.y);
+        rs.z = fmaf(wlast, nb, rs.z);
+        rs.w = fmaf(wlast, na, rs.w);
+    }
+    return rs;
+}
+
+template <bool NONNEG, bool RANK1>
+__global__ void __launch_bounds__(ZS_BATCH_THREADS, 3) zs_batch_kernel(const __grid_constant__ ZsBatchArgs a) {
     extern __shared__ __align__(16) float zs_batch_lut[];      // [code][64], lanes 32..63 unused
-    for (int i = threadIdx.x; i < 256 * 32; i += blockDim.x) zs_batch_lut[(i >> 5) * 64 + (i & 31)] = zs_srgb_decode_lut[i >> 5];
+    for (int i = threadIdx.x; i < 256 * 8; i += blockDim.x) {
+        const float d = zs_srgb_decode_lut[i >> 3];
+        reinterpret_cast<float4 *>(zs_batch_lut)[(i >> 3) * 16 + (i & 7)] = make_float4(d, d, d, d);
+    }
     __syncthreads();
     const unsigned char *lut = reinterpret_cast<const unsigned char *>(zs_batch_lut);
     const int lane = threadIdx.x & 31;
     const uint32_t lane4 = (uint32_t)lane << 2;
     const int warps = (int)(gridDim.x * (blockDim.x >> 5));
     const int total = a.prefix[a.n];
-    int lo = 0;   // image of the current item: items only move forward, so scan from the last one
+    int img = 0;   // image of the current item: items only move forward, so scan from the last one
     for (int it = (int)(blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)); it < total; it += warps) {
-        while (a.prefix[lo + 1] <= it) ++lo;
-        const ZsBatchImage I = a.images[lo];
-        const int segs = (I.tw + 31) >> 5, local = it - a.prefix[lo];
-        const int v = local / segs, u = (local - v * segs) * 32 + lane;
-        if (u >= I.tw) continue;
-        uint32_t *out = reinterpret_cast<uint32_t *>(a.out + (size_t)lo * a.canvas * a.canvas * 4);
-        int jx0, jx1, jy0, jy1;
-        float lox, hix, loy, hiy;
-        zs_box_window(u, I.sx, I.fx, I.width, jx0, jx1, lox, hix);
-        zs_box_window(v, I.sy, I.fy, I.height, jy0, jy1, loy, hiy);
-        // The weights of a window sum to its length clipped to the image; per row, source
-        // texels go through the chain two at a time (the odd tail pairs with itself at weight 0).
-        const float wsum = fmaxf(fminf(hix, (float)jx1) - fmaxf(lox, (float)jx0), 0.f) *
-                           fmaxf(fminf(hiy, (float)jy1) - fmaxf(loy, (float)jy0), 0.f);
-        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-        for (int jy = jy0; jy < jy1; ++jy) {
-            const float wy = fminf(hiy, (float)jy + 1.f) - fmaxf(loy, (float)jy);
-            if (wy <= 0.f) continue;
-            const uint32_t *row = reinterpret_cast<const uint32_t *>(I.ptr + (size_t)jy * I.width * 4);
-            float2 sr = make_float2(0.f, 0.f), sg = sr, sb = sr, sa = sr;
-            for (int jx = jx0; jx < jx1; jx += 2) {
-                const bool two = jx + 1 < jx1;
-                const uint32_t w0 = __ldg(row + jx), w1 = two ? __ldg(row + jx + 1) : w0;
-                const float2 wx = make_float2(
-                    fmaxf(fminf(hix, (float)jx + 1.f) - fmaxf(lox, (float)jx), 0.f),
-                    two ? fmaxf(fminf(hix, (float)jx + 2.f) - fmaxf(lox, (float)jx + 1.f), 0.f) : 0.f);
-                float2 r, g, b;
-                zs_batch_chain2<NONNEG>(w0, w1, lut, lane4, a, r, g, b);
-                const float2 al = make_float2((float)(w0 >> 24) * (1.0f / 255.0f), (float)(w1 >> 24) * (1.0f / 255.0f));
-                sr = __ffma2_rn(wx, r, sr);
-                sg = __ffma2_rn(wx, g, sg);
-                sb = __ffma2_rn(wx, b, sb);
-                sa = __ffma2_rn(wx, al, sa);
+        while (a.prefix[img + 1] <= it) ++img;
+        const ZsBatchImage I = a.images[img];
+        const int strips = (I.tw + 31) >> 5, local = it - a.prefix[img];
+        const int band = local / strips, u = (local - band * strips) * 32 + lane;
+        const bool valid = u < I.tw;
+        // Horizontal window of this lane (none for lanes past the fitted width).
+        int jx0 = 0, jx1 = 0;
+        float lox = 0.f, hix = 0.f;
+        if (valid) zs_box_window(u, I.sx, I.fx, I.width, jx0, jx1, lox, hix);
+        const int next_j0 = __shfl_down_sync(0xffffffffu, jx0, 1);
+        const int next_valid = __shfl_down_sync(0xffffffffu, valid ? 1 : 0, 1);
+        const bool share = I.sx >= 1.f && lane < 31 && valid && next_valid && next_j0 == jx1 - 1 && jx1 - 1 > jx0;
+        const int jend = share ? jx1 - 1 : jx1;
+        const float wfirst = fmaxf(fminf(hix, (float)jx0 + 1.f) - fmaxf(lox, (float)jx0), 0.f);
+        const float wlast = fmaxf(fminf(hix, (float)jx1) - fmaxf(lox, (float)jx1 - 1.f), 0.f);
+        const float wxsum = fmaxf(fminf(hix, (float)jx1) - fmaxf(lox, (float)jx0), 0.f);
+        uint32_t *out = reinterpret_cast<uint32_t *>(a.out + (size_t)img * a.canvas * a.canvas * 4);
+        const int v0 = band * ZS_BATCH_ROWS, v1 = min(v0 + ZS_BATCH_ROWS, I.th);
+        int carry_row = -1;
+        float4 carry = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int v = v0; v < v1; ++v) {
+            int jy0, jy1;
+            float loy, hiy;
+            zs_box_window(v, I.sy, I.fy, I.height, jy0, jy1, loy, hiy);
+            float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int jy = jy0; jy < jy1; ++jy) {
+                const float wy = fmaxf(fminf(hiy, (float)jy + 1.f) - fmaxf(loy, (float)jy), 0.f);
+                float4 rs = carry;
+                if (jy != carry_row) {     // uniform across the warp
+                    const uint32_t *row = reinterpret_cast<const uint32_t *>(I.ptr + (size_t)jy * I.width * 4);
+                    rs = zs_batch_row<NONNEG, RANK1>(row, jx0, jend, jx1, wfirst, wlast, share, lut, lane4, a);
+                    carry_row = jy;
+                    carry = rs;
+                }
+                acc.x = fmaf(wy, rs.x, acc.x);
+                acc.y = fmaf(wy, rs.y, acc.y);
+                acc.z = fmaf(wy, rs.z, acc.z);
+                acc.w = fmaf(wy, rs.w, acc.w);
             }
-            acc.x = fmaf(wy, sr.x + sr.y, acc.x);
-            acc.y = fmaf(wy, sg.x + sg.y, acc.y);
-            acc.z = fmaf(wy, sb.x + sb.y, acc.z);
-            acc.w = fmaf(wy, sa.x + sa.y, acc.w);
+            if (!valid) continue;
+            const float wsum = wxsum * fmaxf(fminf(hiy, (float)jy1) - fmaxf(loy, (float)jy0), 0.f);
+            const float inv = wsum > 0.f ? 1.0f / wsum : 0.f;
+            const uint32_t code = zs_enc_srgb8(zs_srgb_encode_tab, acc.x * inv) |
+                                  (zs_enc_srgb8(zs_srgb_encode_tab, acc.y * inv) << 8) |
+                                  (zs_enc_srgb8(zs_srgb_encode_tab, acc.z * inv) << 16) |
+                                  (zs_unorm8(acc.w * inv * (1.0f / 255.0f)) << 24);
+            out[(size_t)(I.y0 + v) * a.canvas + I.x0 + u] = code;
         }
-        const float inv = wsum > 0.f ? 1.0f / wsum : 0.f;
-        const uint32_t code = zs_enc_srgb8(zs_srgb_encode_tab, acc.x * inv) | (zs_enc_srgb8(zs_srgb_encode_tab, acc.y * inv) << 8) |
-                              (zs_enc_srgb8(zs_srgb_encode_tab, acc.z * inv) << 16) | (zs_unorm8(acc.w * inv) << 24);
-        out[(size_t)(I.y0 + v) * a.canvas + I.x0 + u] = code;
     }
 }
 
@@ -204,73 +246,113 @@ int batch_thumbnails(Executable *chain, const void *const *images, const uint32_
         I.fx = I.sx > 1.f ? I.sx : 1.f;
         I.fy = I.sy > 1.f ? I.sy : 1.f;
     }
-    // Work items: 32 adjacent fitted pixels of one row.
+    // Work items: 32 output columns x ZS_BATCH_ROWS output rows.
     std::vector<int32_t> prefix(n + 1, 0);
     for (uint32_t i = 0; i < n; ++i) {
-        const int64_t items = (int64_t)host[i].th * ((host[i].tw + 31) / 32);
+        const int64_t items = (int64_t)((host[i].th + ZS_BATCH_ROWS - 1) / ZS_BATCH_ROWS) * ((host[i].tw + 31) / 32);
         if ((int64_t)prefix[i] + items > INT32_MAX) {
             set_last_error("zs_batch_thumbnails: too many output pixels in one batch");
             return ZS_ERR_INVALID_ARG;
         }
         prefix[i + 1] = prefix[i] + (int32_t)items;
     }
-    // Scratch: image table + item prefix table, kept with the executable.
+    // Scratch: image table + item prefix table, kept with the executable, uploaded from a
+    // pinned staging copy.  The previous batch of this executable must have finished with
+    // both before they are rewritten.
     const size_t table_bytes = (sizeof(ZsBatchImage) * n + 255) & ~(size_t)255;
     const size_t bytes = table_bytes + sizeof(int32_t) * (n + 1);
+    auto device_error = [](cudaError_t e) {
+        set_last_error(std::string("zs_batch_thumbnails: ") + cudaGetErrorString(e));
+        return e == cudaErrorMemoryAllocation ? ZS_ERR_OUT_OF_MEMORY : ZS_ERR_DEVICE;
+    };
+    cudaError_t e = cudaSuccess;
+    if (chain->batch_done && (e = cudaEventSynchronize(chain->batch_done)) != cudaSuccess) return device_error(e);
     if (chain->batch_bytes < bytes) {
         if (chain->batch_scratch) cudaFree(chain->batch_scratch);
-        chain->batch_scratch = nullptr;
+        if (chain->batch_staging) cudaFreeHost(chain->batch_staging);
+        chain->batch_scratch = chain->batch_staging = nullptr;
         chain->batch_bytes = 0;
-        cudaError_t e = cudaMalloc(&chain->batch_scratch, bytes);
-        if (e != cudaSuccess) {
-            set_last_error(std::string("zs_batch_thumbnails: ") + cudaGetErrorString(e));
-            return ZS_ERR_OUT_OF_MEMORY;
-        }
+        if ((e = cudaMalloc(&chain->batch_scratch, bytes)) != cudaSuccess) return device_error(e);
+        if ((e = cudaMallocHost(&chain->batch_staging, bytes)) != cudaSuccess) return device_error(e);
         chain->batch_bytes = bytes;
     }
-    uint8_t *scratch = (uint8_t *)chain->batch_scratch;
-    ZsBatchImage *table = (ZsBatchImage *)scratch;
-    int32_t *dprefix = (int32_t *)(scratch + table_bytes);
-    cudaError_t e = cudaMemcpyAsync(table, host.data(), sizeof(ZsBatchImage) * n, cudaMemcpyHostToDevice, stream);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(dprefix, prefix.data(), sizeof(int32_t) * (n + 1), cudaMemcpyHostToDevice, stream);
-    // Transparent margins: zero every canvas, the kernel writes the fitted pixels.
-    if (e == cudaSuccess) e = cudaMemsetAsync(out, 0, (size_t)n * canvas * canvas * 4, stream);
-    if (e != cudaSuccess) {
-        set_last_error(std::string("zs_batch_thumbnails: ") + cudaGetErrorString(e));
-        return ZS_ERR_DEVICE;
-    }
+    if (!chain->batch_done && (e = cudaEventCreateWithFlags(&chain->batch_done, cudaEventDisableTiming)) != cudaSuccess)
+        return device_error(e);
+    uint8_t *scratch = (uint8_t *)chain->batch_scratch, *staging = (uint8_t *)chain->batch_staging;
+    std::memcpy(staging, host.data(), sizeof(ZsBatchImage) * n);
+    std::memcpy(staging + table_bytes, prefix.data(), sizeof(int32_t) * (n + 1));
+    if ((e = cudaMemcpyAsync(scratch, staging, bytes, cudaMemcpyHostToDevice, stream)) != cudaSuccess)
+        return device_error(e);
     ZsBatchArgs a;
     std::memset(&a, 0, sizeof(a));
-    a.images = table;
-    a.prefix = dprefix;
+    a.images = (const ZsBatchImage *)scratch;
+    a.prefix = (const int32_t *)(scratch + table_bytes);
     a.out = (uint8_t *)out;
     a.n = (int)n;
     a.canvas = (int)canvas;
     a.flags = cs->chain.flags;
-    std::memcpy(a.m, cs->chain.m, sizeof(a.m));
     std::memcpy(a.m2, cs->chain.m2, sizeof(a.m2));
-    auto kernel = (a.flags & ZS_CHAIN_CBRT_NONNEG) ? zs_batch_kernel<true> : zs_batch_kernel<false>;
+    std::memcpy(a.mb_v, cs->chain.mb_v, sizeof(a.mb_v));
+    std::memcpy(a.mb_d, cs->chain.mb_d, sizeof(a.mb_d));
+    const bool nonneg = (a.flags & ZS_CHAIN_CBRT_NONNEG) || !(a.flags & ZS_CHAIN_CBRT);
+    const bool rank1 = (a.flags & ZS_CHAIN_MB_RANK1) != 0;
+    auto kernel = nonneg ? (rank1 ? zs_batch_kernel<true, true> : zs_batch_kernel<true, false>)
+                         : (rank1 ? zs_batch_kernel<false, true> : zs_batch_kernel<false, false>);
     const size_t smem = 256 * 64 * sizeof(float);
     e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int per_sm = 0;
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, ZS_BATCH_THREADS, smem);
-    if (e != cudaSuccess) {
-        set_last_error(std::string("zs_batch_thumbnails: ") + cudaGetErrorString(e));
-        return ZS_ERR_DEVICE;
-    }
+    if (e != cudaSuccess) return device_error(e);
     if (per_sm < 1) per_sm = 1;
+    // The grid covers every SM: warps stride over the items of all images.
     long long blocks = (long long)chain->sm_count * per_sm;
     const long long need = ((long long)prefix[n] + ZS_BATCH_THREADS / 32 - 1) / (ZS_BATCH_THREADS / 32);
     if (blocks > need) blocks = need;
-    if (blocks < 1) return ZS_OK;
-    kernel<<<(unsigned)blocks, ZS_BATCH_THREADS, smem, stream>>>(a);
-    g_kernel_launches.fetch_add(1);
-    e = cudaGetLastError();
-    if (e != cudaSuccess) {
-        set_last_error(std::string("zs_batch_thumbnails: ") + cudaGetErrorString(e));
-        return ZS_ERR_DEVICE;
+    if (blocks < 1) blocks = 1;
+    // The batch launch (zero the canvases, one kernel) is captured once as a CUDA graph and
+    // replayed for every later batch with the same output buffer, count and canvas: the image
+    // table the kernel reads is the per-batch data, uploaded above.
+    const std::vector<uint64_t> key = {(uint64_t)(uintptr_t)out, n, canvas, (uint64_t)(uintptr_t)kernel,
+                                       (uint64_t)blocks, (uint64_t)(uintptr_t)scratch, (uint64_t)table_bytes,
+                                       (uint64_t)a.flags};
+    auto enqueue = [&]() {
+        // Transparent margins: zero every canvas, the kernel writes the fitted pixels.
+        cudaError_t ce = cudaMemsetAsync(out, 0, (size_t)n * canvas * canvas * 4, stream);
+        if (ce == cudaSuccess) {
+            kernel<<<(unsigned)blocks, ZS_BATCH_THREADS, smem, stream>>>(a);
+            ce = cudaGetLastError();
+        }
+        return ce;
+    };
+    if (!chain->batch_graph || chain->batch_key != key) {
+        if (chain->batch_graph) cudaGraphExecDestroy(chain->batch_graph);
+        chain->batch_graph = nullptr;
+        chain->batch_key.clear();
+        if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+            // A stream that cannot be captured (the legacy default stream): launch directly.
+            cudaGetLastError();
+            if ((e = enqueue()) != cudaSuccess) return device_error(e);
+            if ((e = cudaEventRecord(chain->batch_done, stream)) != cudaSuccess) return device_error(e);
+            g_kernel_launches.fetch_add(1);
+            return ZS_OK;
+        }
+        cudaGraph_t g = nullptr;
+        const cudaError_t ce = enqueue();
+        e = cudaStreamEndCapture(stream, &g);
+        if (ce != cudaSuccess || e != cudaSuccess) {
+            if (g) cudaGraphDestroy(g);
+            return device_error(ce != cudaSuccess ? ce : e);
+        }
+        cudaGraphExec_t ge = nullptr;
+        e = cudaGraphInstantiate(&ge, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) return device_error(e);
+        chain->batch_graph = ge;
+        chain->batch_key = key;
     }
+    if ((e = cudaGraphLaunch(chain->batch_graph, stream)) != cudaSuccess) return device_error(e);
+    if ((e = cudaEventRecord(chain->batch_done, stream)) != cudaSuccess) return device_error(e);
+    g_kernel_launches.fetch_add(1);
     return ZS_OK;
 }
 
