@@ -394,6 +394,35 @@ int zs_batch_run(zs_executable *exe, zs_pool *pool, const uint64_t *keys, uint32
 int zs_resample_rgba16f_noalloc(const void *src, uint32_t src_width, uint32_t src_height, void *dst,
                                 uint32_t dst_width, uint32_t dst_height, uint32_t filter, void *stream);
 
+/* ---- autotuner (no counterpart in the reference: its render passes have no launch
+ *      parameters) ---- */
+enum {
+    ZS_TUNE_CHAIN_THREADS = 0,   /* colour-chain kernel block size: 1024 (one block per SM) or 512 */
+    ZS_TUNE_BATCH_ROWS = 1       /* batched thumbnails: output rows per work item, 1..16 */
+};
+/* Times the candidates of every tunable launch of `exe` (CUDA events, median of `reps`
+ * launches each) on the given device buffers -- which receive the result -- and keeps the
+ * fastest with the executable and in the process-wide tuning cache, keyed by kernel family,
+ * chain specialisation, size class and device; executables lowered later on the same device
+ * start from the cached value.  Every candidate computes the same bytes. */
+int zs_autotune(zs_executable *exe, const void *const *inputs, uint32_t n_inputs, void *const *outputs,
+                uint32_t n_outputs, void *stream, uint32_t reps, int32_t *chain_threads);
+/* The same for the rows per work item of zs_batch_thumbnails on this batch. */
+int zs_autotune_batch_thumbnails(zs_executable *chain, const void *const *images, const uint32_t *widths,
+                                 const uint32_t *heights, uint32_t n, uint32_t canvas, void *out, void *stream,
+                                 uint32_t reps, uint32_t *rows);
+/* Sets / reads a launch parameter (ZS_TUNE_*) of an executable directly. */
+int zs_executable_set_launch(zs_executable *exe, uint32_t param, int32_t value);
+int zs_executable_get_launch(const zs_executable *exe, uint32_t param, int32_t *value);
+/* The tuning-cache key a parameter of this executable uses (canvas: for ZS_TUNE_BATCH_ROWS). */
+int zs_executable_tune_key(const zs_executable *exe, uint32_t param, uint32_t canvas, char *buf, uint64_t len);
+/* The process-wide tuning cache: read / write one value, save to / merge from a text file
+ * ("key value" lines).  zs_tune_cache_get fails with ZS_ERR_MISSING_KEY for an unknown key. */
+int zs_tune_cache_get(const char *key, int32_t *value);
+int zs_tune_cache_put(const char *key, int32_t value);
+int zs_tune_cache_save(const char *path);
+int zs_tune_cache_load(const char *path);
+
 /* Number of kernels this library has launched since the process started. */
 uint64_t zs_kernel_launch_count(void);
 

@@ -619,3 +619,54 @@ def test_batch_run_pool_keys_two_inputs(mode):
     for (ia, ib), (ko,) in zip(pairs, outs):
         got = pool.read(ko)
         assert maxdiff(got, P.oracle_blend_resize(ia, ib, (150, 100))) <= LSB
+
+
+def test_autotune_candidates_are_byte_identical():
+    """Every candidate the autotuner times computes the same bytes: the chain kernel at 1024
+    and 512 threads per block, the batched thumbnails at 1..16 rows per work item.  The tuned
+    choice lands in the cache, so a newly lowered executable starts from it."""
+    from zosimos_gb300.synthetic import thumbnail_sizes
+    img = srgb_gradient_noise(1024, 768, seed=40)
+    c, _, _ = P.chain_commands(1024, 768)
+    exe = zs.Linker.from_included().compile(c).lower_to()
+    src, dst = zs.DeviceBuffer(img.nbytes), zs.DeviceBuffer(img.nbytes)
+    src.upload(P.rgba_bytes(img))
+    outs = []
+    for t in (1024, 512):
+        exe.set_launch(zs.Tune.ChainThreads, t)
+        exe.run_device([src.ptr], [dst.ptr])
+        zs.device_synchronize()
+        outs.append(dst.download(np.empty((768, 4096), np.uint8)))
+    assert (outs[0] == outs[1]).all()
+    chosen = exe.autotune([src.ptr], [dst.ptr], reps=5)
+    assert chosen in (1024, 512)
+    again = zs.Linker.from_included().compile(c).lower_to()
+    again.run_device([src.ptr], [dst.ptr])            # first use reads the cache
+    assert again.get_launch(zs.Tune.ChainThreads) == chosen
+    zs.device_synchronize()
+    assert (dst.download(np.empty((768, 4096), np.uint8)) == outs[0]).all()
+
+    ws, hs = thumbnail_sizes(12, seed=41, lo=40, hi=1500)
+    images = [srgb_gradient_noise(int(w), int(h), seed=41, image=i) for i, (w, h) in enumerate(zip(ws, hs))]
+    c1, _, _ = P.chain_commands(1, 1)
+    chain = zs.Linker.from_included().compile(c1).lower_to()
+    bufs = []
+    for im in images:
+        b = zs.DeviceBuffer(im.nbytes)
+        b.upload(P.rgba_bytes(im))
+        bufs.append(b)
+    out = zs.DeviceBuffer(12 * 128 * 128 * 4)
+    args = ([b.ptr for b in bufs], [im.shape[1] for im in images], [im.shape[0] for im in images], 128, out.ptr)
+    results = []
+    for rows in (1, 2, 4, 8, 16):
+        chain.set_launch(zs.Tune.BatchRows, rows)
+        chain.batch_thumbnails(*args)
+        zs.device_synchronize()
+        results.append(out.download(np.empty(out.nbytes, np.uint8)))
+    assert all((r == results[0]).all() for r in results[1:])
+    rows = chain.autotune_batch_thumbnails(*args, reps=2)
+    assert rows in (1, 2, 4, 8, 16) and chain.get_launch(zs.Tune.BatchRows) == rows
+    ref = P.oracle_thumbnails(images, 128)
+    got = results[0].reshape(12, 128, 512)
+    for k in range(12):
+        assert maxdiff(got[k], ref[k]) <= LSB

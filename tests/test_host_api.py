@@ -298,3 +298,38 @@ def test_knobs_and_buffer_parameters_host_side():
     assert e.value.code == 10
     env.knob(knob, np.zeros(24, np.float32))
     assert len(outs) == 3
+
+
+def test_tuning_cache_and_keys(tmp_path):
+    c, _, _ = color_chain(4096, 4096)
+    exe = lower(c)
+    key = exe.tune_key(zs.Tune.ChainThreads)
+    # kernel family / chain specialisation / size class / device
+    parts = key.split("/")
+    assert parts[0] == "chain" and parts[1].startswith("flags") and parts[2] == "px2^24"
+    assert exe.tune_key(zs.Tune.BatchRows, 256).startswith("batch/flags")
+    assert exe.get_launch(zs.Tune.ChainThreads) == 1024          # untuned default
+    exe.set_launch(zs.Tune.ChainThreads, 512)
+    assert exe.get_launch(zs.Tune.ChainThreads) == 512
+    with pytest.raises(ZosimosError) as e:
+        exe.set_launch(zs.Tune.ChainThreads, 300)
+    assert e.value.code == 10
+    with pytest.raises(ZosimosError) as e:
+        exe.set_launch(zs.Tune.BatchRows, 17)
+    assert e.value.code == 10
+    # the process-wide cache: values, a file round trip, and misses
+    zs.tune_cache_put("test/a/b", 7)
+    zs.tune_cache_put("test/c", 16)
+    path = tmp_path / "tune.txt"
+    zs.tune_cache_save(path)
+    zs.tune_cache_put("test/a/b", 1)
+    zs.tune_cache_load(path)
+    assert zs.tune_cache_get("test/a/b") == 7 and zs.tune_cache_get("test/c") == 16
+    assert "test/c 16" in path.read_text()
+    with pytest.raises(ZosimosError) as e:
+        zs.tune_cache_get("test/missing")
+    assert e.value.code == 7
+    bad = tmp_path / "bad.txt"
+    bad.write_text("oops\n")
+    with pytest.raises(ZosimosError):
+        zs.tune_cache_load(bad)

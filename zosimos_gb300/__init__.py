@@ -87,6 +87,11 @@ class Mode:
     Fused, PerOpF32, PerOpF16 = range(3)
 
 
+class Tune:
+    """Launch parameters the autotuner chooses (ZS_TUNE_*)."""
+    ChainThreads, BatchRows = range(2)
+
+
 STATUS = {0: "ok", 1: "type error", 2: "unimplemented", 3: "bad register", 4: "other", 5: "launch error",
           6: "mismatched descriptor", 7: "missing key", 8: "device error", 9: "timeout", 10: "invalid argument",
           11: "out of memory", 12: "step limit"}
@@ -190,6 +195,12 @@ def _lib():
             "zs_batch_run_device": ([P, P, P, U32, P], I32), "zs_batch_run": ([P, P, P, U32, P], I32),
             "zs_executable_io_count": ([P, P, P], I32),
             "zs_cmd_with_knob": ([P], I32), "zs_cmd_with_buffer": ([P, U32], I32),
+            "zs_autotune": ([P, P, U32, P, U32, P, U32, P], I32),
+            "zs_autotune_batch_thumbnails": ([P, P, P, P, U32, U32, P, P, U32, P], I32),
+            "zs_executable_set_launch": ([P, U32, I32], I32), "zs_executable_get_launch": ([P, U32, P], I32),
+            "zs_executable_tune_key": ([P, U32, U32, P, U64], I32),
+            "zs_tune_cache_get": ([ctypes.c_char_p, P], I32), "zs_tune_cache_put": ([ctypes.c_char_p, I32], I32),
+            "zs_tune_cache_save": ([ctypes.c_char_p], I32), "zs_tune_cache_load": ([ctypes.c_char_p], I32),
             "zs_executable_query_knob": ([P, U32, U32, pU32, pU64], I32),
             "zs_executable_set_knob": ([P, U32, P, U64], I32), "zs_env_knob": ([P, U32, P, U64], I32),
         }
@@ -538,9 +549,11 @@ class CommandBuffer:
         return self._reg(_lib().zs_cmd_distribution_normal2d, ctypes.byref(desc._c()), p.ctypes.data)
 
     def buffer_init(self, data) -> int:
-        """A byte buffer register holding a copy of `data` (bytes or a uint8 array)."""
-        b = np.frombuffer(bytes(data), np.uint8) if not isinstance(data, np.ndarray) else data
-        b = np.ascontiguousarray(b, dtype=np.uint8).reshape(-1)
+        """A byte buffer register holding a copy of `data` (bytes, or the raw bytes of an array)."""
+        if isinstance(data, np.ndarray):
+            b = np.ascontiguousarray(data).view(np.uint8).reshape(-1)
+        else:
+            b = np.frombuffer(bytes(data), np.uint8)
         return self._reg(_lib().zs_cmd_buffer_init, b.ctypes.data, b.nbytes)
 
     def buffer_zero(self, length: int) -> int:
@@ -700,6 +713,37 @@ class Executable:
         b = bytes(np.ascontiguousarray(data).view(np.uint8).reshape(-1)) if isinstance(data, np.ndarray) else bytes(data)
         _check(_lib().zs_executable_set_knob(self._h, knob, b, len(b)))
 
+    def autotune(self, inputs: Sequence[int], outputs: Sequence[int], stream: int = 0, reps: int = 10) -> int:
+        """zs_autotune on device buffers (which receive the result); returns the chain block size."""
+        ins = (ctypes.c_void_p * max(len(inputs), 1))(*inputs)
+        outs = (ctypes.c_void_p * max(len(outputs), 1))(*outputs)
+        t = ctypes.c_int32()
+        _check(_lib().zs_autotune(self._h, ins, len(inputs), outs, len(outputs), stream or None, reps, ctypes.byref(t)))
+        return t.value
+
+    def autotune_batch_thumbnails(self, images, widths, heights, canvas: int, out: int, stream: int = 0,
+                                  reps: int = 3) -> int:
+        """zs_autotune_batch_thumbnails: returns the chosen output rows per work item."""
+        n = len(images)
+        rows = ctypes.c_uint32()
+        _check(_lib().zs_autotune_batch_thumbnails(self._h, (ctypes.c_void_p * n)(*images), (ctypes.c_uint32 * n)(*widths),
+                                                   (ctypes.c_uint32 * n)(*heights), n, canvas, out, stream or None,
+                                                   reps, ctypes.byref(rows)))
+        return rows.value
+
+    def set_launch(self, param: int, value: int) -> None:
+        _check(_lib().zs_executable_set_launch(self._h, param, value))
+
+    def get_launch(self, param: int) -> int:
+        v = ctypes.c_int32()
+        _check(_lib().zs_executable_get_launch(self._h, param, ctypes.byref(v)))
+        return v.value
+
+    def tune_key(self, param: int, canvas: int = 0) -> str:
+        buf = ctypes.create_string_buffer(512)
+        _check(_lib().zs_executable_tune_key(self._h, param, canvas, buf, 512))
+        return buf.value.decode()
+
     def output_count(self) -> int:
         n = ctypes.c_uint32()
         _check(_lib().zs_executable_io_count(self._h, None, ctypes.byref(n)))
@@ -820,6 +864,24 @@ class PinnedBuffer:
 
 def device_synchronize() -> None:
     _check(_lib().zs_device_synchronize())
+
+
+def tune_cache_get(key: str) -> int:
+    v = ctypes.c_int32()
+    _check(_lib().zs_tune_cache_get(key.encode(), ctypes.byref(v)))
+    return v.value
+
+
+def tune_cache_put(key: str, value: int) -> None:
+    _check(_lib().zs_tune_cache_put(key.encode(), value))
+
+
+def tune_cache_save(path: str) -> None:
+    _check(_lib().zs_tune_cache_save(str(path).encode()))
+
+
+def tune_cache_load(path: str) -> None:
+    _check(_lib().zs_tune_cache_load(str(path).encode()))
 
 
 def run_executable(exe: Executable, pool: Pool, binds, knobs, outputs):

@@ -1,0 +1,208 @@
+// autotune.cpp -- the launch-parameter autotuner: candidates timed with CUDA events on the
+// caller's own buffers, the winner kept with the executable and in a process-wide cache keyed
+// by (kernel family, chain flags, shape class, device), which can be saved to and loaded from
+// a text file so that later processes start tuned.
+//
+// Tunables (every candidate runs the same arithmetic per pixel, so results are byte-identical):
+//  * the colour-chain kernel's block size: 1024 threads (one block per SM) or 512 (two);
+//  * the batched-thumbnail kernel's output rows per work item: 1, 2, 4, 8 or 16 (taller items
+//    reuse more source rows between output rows; shorter ones balance the warps better).
+//
+// The reference has no autotuner (its render passes have no launch parameters).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <fstream>
+#include <mutex>
+#include <sstream>
+
+#include "zs_host.hpp"
+
+namespace zs {
+
+const std::string &last_error();
+int batch_thumbnails(Executable *chain, const void *const *images, const uint32_t *widths, const uint32_t *heights,
+                     uint32_t n, uint32_t canvas, void *out, cudaStream_t stream);
+
+namespace {
+
+std::mutex g_tune_mutex;
+std::map<std::string, int> g_tune;
+
+}  // namespace
+
+bool tune_get(const std::string &key, int &value) {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    auto it = g_tune.find(key);
+    if (it == g_tune.end()) return false;
+    value = it->second;
+    return true;
+}
+
+void tune_put(const std::string &key, int value) {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    g_tune[key] = value;
+}
+
+void tune_save(const std::string &path) {
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    std::ofstream f(path, std::ios::trunc);
+    if (!f) fail(ZS_ERR_INVALID_ARG, "cannot write the tuning cache " + path);
+    f << "# zosimos-gb300 tuning cache: key value\n";
+    for (const auto &kv : g_tune) f << kv.first << ' ' << kv.second << '\n';
+}
+
+void tune_load(const std::string &path) {
+    std::ifstream f(path);
+    if (!f) fail(ZS_ERR_INVALID_ARG, "cannot read the tuning cache " + path);
+    std::map<std::string, int> read;
+    std::string line;
+    while (std::getline(f, line)) {
+        if (line.empty() || line[0] == '#') continue;
+        std::istringstream is(line);
+        std::string key;
+        int value;
+        if (!(is >> key >> value)) fail(ZS_ERR_INVALID_ARG, "malformed tuning cache line: " + line);
+        read[key] = value;
+    }
+    std::lock_guard<std::mutex> lock(g_tune_mutex);
+    for (const auto &kv : read) g_tune[kv.first] = kv.second;
+}
+
+// "<name>/sm<count>/cc<major>.<minor>" of a device, or "nodevice" without one.
+std::string device_key(int device) {
+    cudaDeviceProp p;
+    if (cudaGetDeviceProperties(&p, device) != cudaSuccess) {
+        cudaGetLastError();
+        return "nodevice";
+    }
+    std::string name(p.name);
+    std::replace(name.begin(), name.end(), ' ', '_');
+    std::ostringstream os;
+    os << name << "/sm" << p.multiProcessorCount << "/cc" << p.major << '.' << p.minor;
+    return os.str();
+}
+
+// Chain steps: the specialisation (flags) and the image size class (log2 of the pixels).
+std::string chain_tune_key(const Step &st, int device) {
+    std::ostringstream os;
+    const int64_t npx = std::max<int64_t>(st.chain.npx, 1);
+    os << "chain/flags" << st.chain.flags << "/px2^" << (int)std::floor(std::log2((double)npx)) << '/'
+       << device_key(device);
+    return os.str();
+}
+
+std::string batch_tune_key(const Executable &E, uint32_t canvas, int device) {
+    int flags = 0;
+    for (const Step &st : E.steps)
+        if (st.kind == StepKind::Chain) flags = st.chain.flags;
+    std::ostringstream os;
+    os << "batch/flags" << flags << "/canvas" << canvas << '/' << device_key(device);
+    return os.str();
+}
+
+// Tuned values of an executable's steps from the cache (called once its device is known).
+void apply_tuned(Executable &E) {
+    for (Step &st : E.steps) {
+        int v;
+        if (st.kind == StepKind::Chain && !st.tune_threads && tune_get(chain_tune_key(st, E.device), v)) st.tune_threads = v;
+    }
+}
+
+// Device time of one recorded step (median of `reps` launches after a warm-up).
+static float time_step(Executable &E, const std::vector<void *> &ptrs, size_t k, cudaStream_t s, uint32_t reps) {
+    cudaEvent_t e0, e1;
+    check_cuda(cudaEventCreate(&e0), "event");
+    check_cuda(cudaEventCreate(&e1), "event");
+    std::vector<float> ms;
+    try {
+        E.record_range(s, ptrs, k, k + 1);
+        for (uint32_t r = 0; r < reps; ++r) {
+            check_cuda(cudaEventRecord(e0, s), "event");
+            E.record_range(s, ptrs, k, k + 1);
+            check_cuda(cudaEventRecord(e1, s), "event");
+            check_cuda(cudaEventSynchronize(e1), "synchronize");
+            float t = 0.f;
+            check_cuda(cudaEventElapsedTime(&t, e0, e1), "elapsed");
+            ms.push_back(t);
+        }
+    } catch (...) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        throw;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    std::nth_element(ms.begin(), ms.begin() + ms.size() / 2, ms.end());
+    return ms[ms.size() / 2];
+}
+
+// Tunes every chain step of E on the given buffers; returns the chosen block size of the
+// last one (0 when E has no chain step).
+int autotune_steps(Executable &E, const std::vector<void *> &ptrs, cudaStream_t s, uint32_t reps) {
+    int chosen = 0;
+    for (size_t k = 0; k < E.steps.size(); ++k) {
+        Step &st = E.steps[k];
+        if (st.kind != StepKind::Chain) continue;
+        int best = 1024;
+        float best_ms = 0.f;
+        for (int cand : {1024, 512}) {
+            st.tune_threads = cand;
+            const float t = time_step(E, ptrs, k, s, reps);
+            if (cand == 1024 || t < best_ms) {
+                best = cand;
+                best_ms = t;
+            }
+        }
+        st.tune_threads = best;
+        tune_put(chain_tune_key(st, E.device), best);
+        chosen = best;
+    }
+    // Captured graphs hold the old launch parameters.
+    for (auto &kv : E.graphs) cudaGraphExecDestroy(kv.second);
+    E.graphs.clear();
+    E.graph_order.clear();
+    return chosen;
+}
+
+int autotune_batch(Executable *chain, const void *const *images, const uint32_t *widths, const uint32_t *heights,
+                   uint32_t n, uint32_t canvas, void *out, cudaStream_t s, uint32_t reps) {
+    cudaEvent_t e0, e1;
+    check_cuda(cudaEventCreate(&e0), "event");
+    check_cuda(cudaEventCreate(&e1), "event");
+    int best = 0;
+    float best_ms = 0.f;
+    int rc = ZS_OK;
+    for (int cand : {1, 2, 4, 8, 16}) {
+        chain->batch_rows = cand;
+        std::vector<float> ms;
+        for (uint32_t r = 0; r <= reps && rc == ZS_OK; ++r) {
+            cudaEventRecord(e0, s);
+            rc = batch_thumbnails(chain, images, widths, heights, n, canvas, out, s);
+            cudaEventRecord(e1, s);
+            if (rc != ZS_OK) break;
+            check_cuda(cudaEventSynchronize(e1), "synchronize");
+            float t = 0.f;
+            check_cuda(cudaEventElapsedTime(&t, e0, e1), "elapsed");
+            if (r > 0) ms.push_back(t);      // the first batch of a candidate captures its graph
+        }
+        if (rc != ZS_OK) break;
+        std::nth_element(ms.begin(), ms.begin() + ms.size() / 2, ms.end());
+        const float t = ms[ms.size() / 2];
+        if (!best || t < best_ms) {
+            best = cand;
+            best_ms = t;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != ZS_OK) {
+        chain->batch_rows = 0;
+        fail(rc, "autotune of the batched thumbnails: " + last_error());
+    }
+    chain->batch_rows = best;
+    tune_put(batch_tune_key(*chain, canvas, chain->device), best);
+    return best;
+}
+
+}  // namespace zs

@@ -763,7 +763,8 @@ static bool run_host_zero_copy(zs_executable *exe, const void *const *inputs, vo
     c.src = (const uint8_t *)din;
     c.dst = (uint8_t *)dout;
     cudaStream_t s = exe_stream(exe);
-    check_cuda(launch_chain(c, st.chain_src_fast, st.chain_dst_fast, E.sm_count, s), st.label.c_str());
+    check_cuda(launch_chain(c, st.chain_src_fast, st.chain_dst_fast, E.sm_count, s, st.tune_threads ? st.tune_threads : 1024),
+               st.label.c_str());
     check_cuda(cudaStreamSynchronize(s), "synchronize");
     return true;
 }
@@ -797,7 +798,9 @@ static bool run_host_striped(zs_executable *exe, const void *const *inputs, void
         c.src = din + p0 * 4;
         c.dst = dout + p0 * 4;
         c.npx = n;
-        check_cuda(launch_chain(c, st.chain_src_fast, st.chain_dst_fast, E.sm_count, t), st.label.c_str());
+        check_cuda(launch_chain(c, st.chain_src_fast, st.chain_dst_fast, E.sm_count, t,
+                                st.tune_threads ? st.tune_threads : 1024),
+                   st.label.c_str());
         check_cuda(cudaMemcpyAsync(hout + p0 * 4, dout + p0 * 4, n * 4, cudaMemcpyDeviceToHost, t), "d2h");
     }
     for (cudaStream_t t : exe->stripes) check_cuda(cudaStreamSynchronize(t), "synchronize");
@@ -1089,6 +1092,131 @@ int zs_batch_run(zs_executable *exe, zs_pool *pool, const uint64_t *keys, uint32
             pool_sync_host(img);
             out_keys[j] = made[j];
         }
+    });
+}
+
+// ---------------------------------------------------------------- autotuner
+
+int zs_autotune(zs_executable *exe, const void *const *inputs, uint32_t n_inputs, void *const *outputs,
+                uint32_t n_outputs, void *stream, uint32_t reps, int32_t *chain_threads) {
+    return guarded([&] {
+        NEED(exe);
+        Executable &E = *exe->e;
+        if (n_inputs != E.input_regs.size() || n_outputs != E.output_regs.size())
+            fail(ZS_ERR_INVALID_ARG, "wrong number of inputs or outputs");
+        if (reps == 0 || reps > 1000) fail(ZS_ERR_INVALID_ARG, "reps out of range (1..1000)");
+        E.ensure_buffers();
+        std::vector<void *> ptrs = E.dev_buffers;
+        for (uint32_t i = 0; i < n_inputs; ++i) {
+            NEED(inputs[i]);
+            ptrs[E.input_slot[i]] = const_cast<void *>(inputs[i]);
+        }
+        for (uint32_t j = 0; j < n_outputs; ++j) {
+            NEED(outputs[j]);
+            ptrs[E.output_slot[j]] = outputs[j];
+        }
+        const int t = autotune_steps(E, ptrs, stream ? (cudaStream_t)stream : exe_stream(exe), reps);
+        for (auto &kv : exe->batch_graphs) cudaGraphExecDestroy(kv.second);
+        exe->batch_graphs.clear();
+        exe->batch_order.clear();
+        if (chain_threads) *chain_threads = t;
+    });
+}
+
+int zs_autotune_batch_thumbnails(zs_executable *chain, const void *const *images, const uint32_t *widths,
+                                 const uint32_t *heights, uint32_t n, uint32_t canvas, void *out, void *stream,
+                                 uint32_t reps, uint32_t *rows) {
+    return guarded([&] {
+        NEED(chain); NEED(images); NEED(widths); NEED(heights); NEED(out);
+        if (reps == 0 || reps > 1000) fail(ZS_ERR_INVALID_ARG, "reps out of range (1..1000)");
+        cudaStream_t s = stream ? (cudaStream_t)stream : exe_stream(chain);
+        const int r = autotune_batch(chain->e.get(), images, widths, heights, n, canvas, out, s, reps);
+        if (rows) *rows = (uint32_t)r;
+    });
+}
+
+int zs_executable_set_launch(zs_executable *exe, uint32_t param, int32_t value) {
+    return guarded([&] {
+        NEED(exe);
+        Executable &E = *exe->e;
+        if (param == ZS_TUNE_CHAIN_THREADS) {
+            if (value != 1024 && value != 512) fail(ZS_ERR_INVALID_ARG, "chain block size must be 1024 or 512");
+            for (Step &st : E.steps)
+                if (st.kind == StepKind::Chain) st.tune_threads = value;
+            for (auto &kv : E.graphs) cudaGraphExecDestroy(kv.second);
+            E.graphs.clear();
+            E.graph_order.clear();
+        } else if (param == ZS_TUNE_BATCH_ROWS) {
+            if (value < 1 || value > 16) fail(ZS_ERR_INVALID_ARG, "rows per batch item must be in 1..16");
+            E.batch_rows = value;
+        } else {
+            fail(ZS_ERR_INVALID_ARG, "unknown launch parameter");
+        }
+    });
+}
+
+int zs_executable_get_launch(const zs_executable *exe, uint32_t param, int32_t *value) {
+    return guarded([&] {
+        NEED(exe); NEED(value);
+        const Executable &E = *exe->e;
+        if (param == ZS_TUNE_CHAIN_THREADS) {
+            *value = 0;
+            for (const Step &st : E.steps)
+                if (st.kind == StepKind::Chain) *value = st.tune_threads ? st.tune_threads : 1024;
+        } else if (param == ZS_TUNE_BATCH_ROWS) {
+            *value = E.batch_rows;
+        } else {
+            fail(ZS_ERR_INVALID_ARG, "unknown launch parameter");
+        }
+    });
+}
+
+static void copy_string(const std::string &s, char *buf, uint64_t len) {
+    if (!buf || len == 0) fail(ZS_ERR_INVALID_ARG, "no output buffer");
+    if (s.size() + 1 > len) fail(ZS_ERR_INVALID_ARG, "output buffer too small");
+    std::memcpy(buf, s.c_str(), s.size() + 1);
+}
+
+int zs_executable_tune_key(const zs_executable *exe, uint32_t param, uint32_t canvas, char *buf, uint64_t len) {
+    return guarded([&] {
+        NEED(exe);
+        const Executable &E = *exe->e;
+        if (param == ZS_TUNE_CHAIN_THREADS) {
+            for (const Step &st : E.steps)
+                if (st.kind == StepKind::Chain) return copy_string(chain_tune_key(st, E.device), buf, len);
+            fail(ZS_ERR_UNIMPLEMENTED, "the executable has no chain step");
+        } else if (param == ZS_TUNE_BATCH_ROWS) {
+            copy_string(batch_tune_key(E, canvas, E.device), buf, len);
+        } else {
+            fail(ZS_ERR_INVALID_ARG, "unknown launch parameter");
+        }
+    });
+}
+
+int zs_tune_cache_get(const char *key, int32_t *value) {
+    return guarded([&] {
+        NEED(key); NEED(value);
+        int v;
+        if (!tune_get(key, v)) fail(ZS_ERR_MISSING_KEY, std::string("no tuned value for ") + key);
+        *value = v;
+    });
+}
+int zs_tune_cache_put(const char *key, int32_t value) {
+    return guarded([&] {
+        NEED(key);
+        tune_put(key, value);
+    });
+}
+int zs_tune_cache_save(const char *path) {
+    return guarded([&] {
+        NEED(path);
+        tune_save(path);
+    });
+}
+int zs_tune_cache_load(const char *path) {
+    return guarded([&] {
+        NEED(path);
+        tune_load(path);
     });
 }
 

@@ -77,6 +77,7 @@ void Executable::ensure_buffers() {
     check_cuda(init_device_tables(device), "sRGB tables");
     int sms = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device) == cudaSuccess && sms > 0) sm_count = sms;
+    apply_tuned(*this);
     dev_buffers.assign(slots.size(), nullptr);
     for (size_t i = 0; i < slots.size(); ++i) {
         const Slot &s = slots[i];
@@ -158,7 +159,8 @@ void Executable::record_range(cudaStream_t stream, const std::vector<void *> &pt
             ZsChainArgs c = st.chain;
             c.src = (const uint8_t *)ptrs[st.src_slot[0]];
             c.dst = (uint8_t *)ptrs[st.dst_slot];
-            const cudaError_t e = launch_chain(c, st.chain_src_fast, st.chain_dst_fast, sm_count, stream);
+            const cudaError_t e =
+                launch_chain(c, st.chain_src_fast, st.chain_dst_fast, sm_count, stream, st.tune_threads ? st.tune_threads : 1024);
             if (e != cudaErrorNotSupported) {
                 check_cuda(e, st.label.c_str());
                 break;

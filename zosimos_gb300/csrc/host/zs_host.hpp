@@ -185,6 +185,7 @@ struct Step {
     // Copy of rows between different row strides (copy_rows > 0): copy_bytes per row.
     uint64_t copy_rows = 0;
     int64_t copy_src_pitch = 0, copy_dst_pitch = 0;
+    int tune_threads = 0;        // Chain: block size chosen by the autotuner (0: default)
     std::string label;
 };
 
@@ -228,6 +229,7 @@ struct Executable {
     cudaEvent_t batch_done = nullptr;
     cudaGraphExec_t batch_graph = nullptr;
     std::vector<uint64_t> batch_key;
+    int batch_rows = 0;                                // output rows per batch work item (0: tuned or default)
     std::string plan_text;
     std::vector<KnobInfo> knobs;                      // Executable::query_knob
     // CUDA graphs of the launch sequence for zs_run_device, keyed by the bound pointers
@@ -242,6 +244,23 @@ struct Executable {
 };
 
 std::unique_ptr<Executable> lower(const Program &prog, const zs_capabilities &caps);
+
+// ---------------------------------------------------------------- autotuner (autotune.cpp)
+
+const std::string &last_error();
+bool tune_get(const std::string &key, int &value);
+void tune_put(const std::string &key, int value);
+void tune_save(const std::string &path);
+void tune_load(const std::string &path);
+std::string device_key(int device);
+std::string chain_tune_key(const Step &st, int device);
+std::string batch_tune_key(const Executable &E, uint32_t canvas, int device);
+// Tuned values of the executable's steps from the process-wide cache.
+void apply_tuned(Executable &E);
+// Times the candidates of every tunable step on these buffers and keeps the fastest.
+int autotune_steps(Executable &E, const std::vector<void *> &ptrs, cudaStream_t s, uint32_t reps);
+int autotune_batch(Executable *chain, const void *const *images, const uint32_t *widths, const uint32_t *heights,
+                   uint32_t n, uint32_t canvas, void *out, cudaStream_t s, uint32_t reps);
 
 // ---------------------------------------------------------------- pool / runtime
 

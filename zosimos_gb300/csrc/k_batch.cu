@@ -7,7 +7,8 @@
 // fit-resize so the long side is `canvas` -> centred inscribe on a transparent
 // canvas x canvas image -> exact sRGB8 encode.  The canvases are zero-filled (the
 // transparent margins) by one memset; the fitted pixels are cut into work items of 32
-// output columns x ZS_BATCH_ROWS output rows, one item per warp, taken by static striding
+// output columns x `rows` output rows (1..16, chosen by the autotuner), one item per warp,
+// taken by static striding
 // over all images (no atomics, no barriers), so that every image's cost spreads over all warps.
 //
 // The colour chain is nonlinear, so it runs on every source texel before the box filter;
@@ -30,7 +31,7 @@
 #include "zs_kernels.h"
 
 #define ZS_BATCH_THREADS 256
-#define ZS_BATCH_ROWS 8        // output rows per work item
+#define ZS_BATCH_ROWS_DEFAULT 2   // output rows per work item until the autotuner chose
 
 struct ZsBatchImage {
     const uint8_t *ptr;
@@ -48,7 +49,7 @@ struct ZsBatchArgs {
     int32_t n;
     int32_t canvas;
     int32_t flags;
-    int32_t pad;
+    int32_t rows;              // output rows per work item
     float m2[4][9][2];         // the chain's matrices with every coefficient duplicated (f32x2 operands)
     float mb_v[3][2];          // ZS_CHAIN_MB_RANK1: M_b = d I + (1,1,1)^T v
     float mb_d[2];
@@ -171,7 +172,7 @@ __global__ void __launch_bounds__(ZS_BATCH_THREADS, 3) zs_batch_kernel(const __g
         const float wlast = fmaxf(fminf(hix, (float)jx1) - fmaxf(lox, (float)jx1 - 1.f), 0.f);
         const float wxsum = fmaxf(fminf(hix, (float)jx1) - fmaxf(lox, (float)jx0), 0.f);
         uint32_t *out = reinterpret_cast<uint32_t *>(a.out + (size_t)img * a.canvas * a.canvas * 4);
-        const int v0 = band * ZS_BATCH_ROWS, v1 = min(v0 + ZS_BATCH_ROWS, I.th);
+        const int v0 = band * a.rows, v1 = min(v0 + a.rows, I.th);
         int carry_row = -1;
         float4 carry = make_float4(0.f, 0.f, 0.f, 0.f);
         for (int v = v0; v < v1; ++v) {
@@ -246,10 +247,17 @@ int batch_thumbnails(Executable *chain, const void *const *images, const uint32_
         I.fx = I.sx > 1.f ? I.sx : 1.f;
         I.fy = I.sy > 1.f ? I.sy : 1.f;
     }
-    // Work items: 32 output columns x ZS_BATCH_ROWS output rows.
+    // Work items: 32 output columns x `rows` output rows (the tuned height for this chain,
+    // canvas and device when the autotuner has seen them).
+    if (chain->batch_rows <= 0) {
+        int tuned;
+        if (tune_get(batch_tune_key(*chain, canvas, chain->device), tuned) && tuned >= 1 && tuned <= 16)
+            chain->batch_rows = tuned;
+    }
+    const int rows = chain->batch_rows > 0 ? chain->batch_rows : ZS_BATCH_ROWS_DEFAULT;
     std::vector<int32_t> prefix(n + 1, 0);
     for (uint32_t i = 0; i < n; ++i) {
-        const int64_t items = (int64_t)((host[i].th + ZS_BATCH_ROWS - 1) / ZS_BATCH_ROWS) * ((host[i].tw + 31) / 32);
+        const int64_t items = (int64_t)((host[i].th + rows - 1) / rows) * ((host[i].tw + 31) / 32);
         if ((int64_t)prefix[i] + items > INT32_MAX) {
             set_last_error("zs_batch_thumbnails: too many output pixels in one batch");
             return ZS_ERR_INVALID_ARG;
@@ -291,6 +299,7 @@ int batch_thumbnails(Executable *chain, const void *const *images, const uint32_
     a.n = (int)n;
     a.canvas = (int)canvas;
     a.flags = cs->chain.flags;
+    a.rows = rows;
     std::memcpy(a.m2, cs->chain.m2, sizeof(a.m2));
     std::memcpy(a.mb_v, cs->chain.mb_v, sizeof(a.mb_v));
     std::memcpy(a.mb_d, cs->chain.mb_d, sizeof(a.mb_d));

@@ -171,27 +171,31 @@ __global__ void __launch_bounds__(ZS_CHAIN_THREADS, 1) zs_chain_srgb8_kernel(con
 namespace zs {
 
 template <bool CBRT, bool CUBE, bool CLAMP, bool NONNEG, bool RANK1 = false>
-static cudaError_t launch_chain_t(const ZsChainArgs &args, int sm_count, cudaStream_t stream) {
+static cudaError_t launch_chain_t(const ZsChainArgs &args, int sm_count, cudaStream_t stream, int threads) {
     auto kernel = zs_chain_srgb8_kernel<CBRT, CUBE, CLAMP, NONNEG, RANK1>;
     const size_t smem = sizeof(ZsChainSmem);
     // The shared-memory opt-in is a per-device attribute of the kernel: set it (and size the
-    // grid) once per device, on the device that is current for this launch.
-    static std::atomic<int> per_sm_of[ZS_MAX_DEVICES];
+    // grid) once per device and block size, on the device that is current for this launch.
+    // Block sizes: 1024 threads (one block per SM) or 512 (two blocks per SM), chosen by
+    // the autotuner; both run the same arithmetic per pixel.
+    static std::atomic<int> per_sm_of[ZS_MAX_DEVICES][2];
+    const int which = threads == 512 ? 1 : 0;
+    const int block = which ? 512 : ZS_CHAIN_THREADS;
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= ZS_MAX_DEVICES) return cudaErrorInvalidDevice;
-    int per_sm = per_sm_of[dev].load();
+    int per_sm = per_sm_of[dev][which].load();
     if (per_sm == 0) {
         e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, ZS_CHAIN_THREADS, smem);
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem);
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
-        per_sm_of[dev].store(per_sm);
+        per_sm_of[dev][which].store(per_sm);
     }
     const int64_t nvec = (args.npx + 3) / 4;
-    int64_t blocks = (nvec + ZS_CHAIN_THREADS - 1) / ZS_CHAIN_THREADS;
+    int64_t blocks = (nvec + block - 1) / block;
     const int64_t cap = (int64_t)(sm_count > 0 ? sm_count : 148) * per_sm;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
@@ -200,7 +204,7 @@ static cudaError_t launch_chain_t(const ZsChainArgs &args, int sm_count, cudaStr
     // griddepcontrol.wait before touching image data).
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3((unsigned)blocks);
-    cfg.blockDim = dim3(ZS_CHAIN_THREADS);
+    cfg.blockDim = dim3(block);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = stream;
     cudaLaunchAttribute attr[1];
@@ -215,32 +219,32 @@ static cudaError_t launch_chain_t(const ZsChainArgs &args, int sm_count, cudaStr
 }
 
 template <bool NONNEG>
-static cudaError_t launch_chain_n(const ZsChainArgs &args, int sm_count, cudaStream_t stream) {
+static cudaError_t launch_chain_n(const ZsChainArgs &args, int sm_count, cudaStream_t stream, int threads) {
     const bool cb = args.flags & ZS_CHAIN_CBRT, cu = args.flags & ZS_CHAIN_CUBE, cl = args.flags & ZS_CHAIN_CLAMP;
     // The Oklab form (cube root, L/C scaling, cube) with the rank-1 middle matrix.
     if (cb && cu && (args.flags & ZS_CHAIN_MB_RANK1)) {
-        if (cl) return launch_chain_t<true, true, true, NONNEG, true>(args, sm_count, stream);
-        return launch_chain_t<true, true, false, NONNEG, true>(args, sm_count, stream);
+        if (cl) return launch_chain_t<true, true, true, NONNEG, true>(args, sm_count, stream, threads);
+        return launch_chain_t<true, true, false, NONNEG, true>(args, sm_count, stream, threads);
     }
-    if (cb && cu && cl) return launch_chain_t<true, true, true, NONNEG>(args, sm_count, stream);
-    if (cb && cu && !cl) return launch_chain_t<true, true, false, NONNEG>(args, sm_count, stream);
-    if (cb && !cu && cl) return launch_chain_t<true, false, true, NONNEG>(args, sm_count, stream);
-    if (cb && !cu && !cl) return launch_chain_t<true, false, false, NONNEG>(args, sm_count, stream);
-    if (!cb && cu && cl) return launch_chain_t<false, true, true, NONNEG>(args, sm_count, stream);
-    if (!cb && cu && !cl) return launch_chain_t<false, true, false, NONNEG>(args, sm_count, stream);
-    if (!cb && !cu && cl) return launch_chain_t<false, false, true, NONNEG>(args, sm_count, stream);
-    return launch_chain_t<false, false, false, NONNEG>(args, sm_count, stream);
+    if (cb && cu && cl) return launch_chain_t<true, true, true, NONNEG>(args, sm_count, stream, threads);
+    if (cb && cu && !cl) return launch_chain_t<true, true, false, NONNEG>(args, sm_count, stream, threads);
+    if (cb && !cu && cl) return launch_chain_t<true, false, true, NONNEG>(args, sm_count, stream, threads);
+    if (cb && !cu && !cl) return launch_chain_t<true, false, false, NONNEG>(args, sm_count, stream, threads);
+    if (!cb && cu && cl) return launch_chain_t<false, true, true, NONNEG>(args, sm_count, stream, threads);
+    if (!cb && cu && !cl) return launch_chain_t<false, true, false, NONNEG>(args, sm_count, stream, threads);
+    if (!cb && !cu && cl) return launch_chain_t<false, false, true, NONNEG>(args, sm_count, stream, threads);
+    return launch_chain_t<false, false, false, NONNEG>(args, sm_count, stream, threads);
 }
 
 cudaError_t launch_chain(const ZsChainArgs &args, uint8_t src_fast, uint8_t dst_fast, int sm_count,
-                         cudaStream_t stream) {
+                         cudaStream_t stream, int threads) {
     if (src_fast != ZS_FAST_RGBA8_SRGB || dst_fast != ZS_FAST_RGBA8_SRGB) return cudaErrorNotSupported;
     if (args.npx <= 0) return cudaSuccess;
     // 16-byte vector loads and stores: other pointers take the generic raster kernel.
     if (((uintptr_t)args.src | (uintptr_t)args.dst) & 15u) return cudaErrorNotSupported;
     if ((args.flags & ZS_CHAIN_CBRT_NONNEG) || !(args.flags & ZS_CHAIN_CBRT))
-        return launch_chain_n<true>(args, sm_count, stream);
-    return launch_chain_n<false>(args, sm_count, stream);
+        return launch_chain_n<true>(args, sm_count, stream, threads);
+    return launch_chain_n<false>(args, sm_count, stream, threads);
 }
 
 }  // namespace zs

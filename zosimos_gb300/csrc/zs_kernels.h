@@ -27,9 +27,10 @@ bool resample_tc_usable(const ZsRasterArgs &args);
 cudaError_t launch_resample_tc(const ZsRasterArgs &args, int sm_count, cudaStream_t stream);
 
 // Fused colour chain in canonical form, RGBA8 in / RGBA8 out (k_chain.cu).
-// Returns cudaErrorNotSupported when no specialisation exists for the formats.
+// Returns cudaErrorNotSupported when no specialisation exists for the formats or the buffers
+// are not 16-byte aligned.  threads: 1024 (default, one block per SM) or 512 (two).
 cudaError_t launch_chain(const ZsChainArgs &args, uint8_t src_fast, uint8_t dst_fast, int sm_count,
-                         cudaStream_t stream);
+                         cudaStream_t stream, int threads = 1024);
 
 // A stack of affine-transformed layers blended in one pass (k_layers.cu).
 cudaError_t launch_layers(const ZsLayersArgs &args, int sm_count, cudaStream_t stream);
