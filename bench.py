@@ -496,6 +496,28 @@ def workload_resample(args, stream, sh):
     _line("rotate 17 deg bilinear 8192^2 RGBA16F", n * n, 2 * n * n * 8, ms0, ms1, clocks)
 
 
+def _thumbnail_parity(out, ws, hs, every=64):
+    """Checker (outside the timed region): every 64th thumbnail of the timed batch against the
+    FP64 oracle; the largest 8-bit difference."""
+    import numpy as np
+    import torch
+
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle
+    import pipelines as P
+    from zosimos_gb300.synthetic import srgb_gradient_noise
+
+    oracle.build()
+    torch.cuda.synchronize()
+    got = out.download(np.empty((len(ws), 256, 1024), np.uint8))
+    idx = list(range(0, len(ws), every))
+    ref = P.oracle_thumbnails([srgb_gradient_noise(int(ws[i]), int(hs[i]), seed=4, image=i) for i in idx], 256)
+    worst = max(int(np.abs(got[i].astype(np.int16) - r.astype(np.int16)).max()) for i, r in zip(idx, ref))
+    if worst > 1:
+        raise SystemExit(f"thumbnail parity failed: {worst} LSB against the FP64 oracle")
+    return {"max_lsb_vs_fp64_oracle": worst, "sample": f"{len(idx)} of the {len(ws)} thumbnails of the timed batch"}
+
+
 def workload_thumbnails(args, stream, sh):
     import numpy as np
 
@@ -525,6 +547,7 @@ def workload_thumbnails(args, stream, sh):
         return
     rows = exe.autotune_batch_thumbnails(ptrs, wl, hl, 256, out.ptr, sh, reps=2)
     ms, clocks = _clocked(timed, run, max(3, args.steps // 20), args.warmup)
+    parity = _thumbnail_parity(out, ws, hs)
     # The same 1024 thumbnails without batching: one ordinary program per image (chain ->
     # box fit -> inscribe onto a transparent canvas -> sRGB8), fused and plain per-op FP32.
     # Each image's executable is timed alone (1 warm-up + 2 launches, CUDA events), so its
@@ -546,6 +569,7 @@ def workload_thumbnails(args, stream, sh):
           src_px * 4 + 1024 * 256 * 256 * 4, ms, per["plain_fp32"][0], clocks,
           {"images": 1024, "source_gpx": round(src_px / 1e9, 3), "launches_per_batch": 1,
            "autotune": {"rows_per_item": rows}, "graph": "memset + kernel captured once, replayed per batch",
+           "parity": parity,
            "plain": "one per-op FP32 program per image", "plain_launches": per["plain_fp32"][1],
            "per_image_fused_ms": round(per["fused"][0], 4), "per_image_fused_launches": per["fused"][1],
            "speedup_vs_per_image_fused": round(per["fused"][0] / ms, 2)})

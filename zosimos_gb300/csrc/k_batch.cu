@@ -31,7 +31,7 @@
 #include "zs_kernels.h"
 
 #define ZS_BATCH_THREADS 256
-#define ZS_BATCH_ROWS_DEFAULT 2   // output rows per work item until the autotuner chose
+#define ZS_BATCH_ROWS_DEFAULT 1   // output rows per work item until the autotuner chose
 
 struct ZsBatchImage {
     const uint8_t *ptr;
@@ -321,9 +321,16 @@ int batch_thumbnails(Executable *chain, const void *const *images, const uint32_
     // The batch launch (zero the canvases, one kernel) is captured once as a CUDA graph and
     // replayed for every later batch with the same output buffer, count and canvas: the image
     // table the kernel reads is the per-batch data, uploaded above.
-    const std::vector<uint64_t> key = {(uint64_t)(uintptr_t)out, n, canvas, (uint64_t)(uintptr_t)kernel,
-                                       (uint64_t)blocks, (uint64_t)(uintptr_t)scratch, (uint64_t)table_bytes,
-                                       (uint64_t)a.flags};
+    // The key holds every kernel argument byte and the launch shape: a graph is replayed only
+    // for a launch it captured exactly.
+    std::vector<uint64_t> key = {(uint64_t)(uintptr_t)out, n, canvas, (uint64_t)(uintptr_t)kernel, (uint64_t)blocks};
+    {
+        static_assert(sizeof(ZsBatchArgs) % 8 == 0, "argument block in 64-bit words");
+        const size_t words = sizeof(ZsBatchArgs) / 8;
+        const size_t at = key.size();
+        key.resize(at + words);
+        std::memcpy(key.data() + at, &a, sizeof(ZsBatchArgs));
+    }
     auto enqueue = [&]() {
         // Transparent margins: zero every canvas, the kernel writes the fitted pixels.
         cudaError_t ce = cudaMemsetAsync(out, 0, (size_t)n * canvas * canvas * 4, stream);
