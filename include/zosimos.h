@@ -240,6 +240,31 @@ int zs_cmd_with_knob(zs_cmd *cmd);
  * follows the buffer's knob when it has one.  ZS_ERR_TYPE when `buffer` is not a buffer,
  * ZS_ERR_OTHER (INVALID_CALL) when it is shorter than the parameter block. */
 int zs_cmd_with_buffer(zs_cmd *cmd, uint32_t buffer);
+/* ---- custom operations (ShaderCommand, command/dynamic.rs:7-51, through
+ *      CommandBuffer::construct_dynamic / unary_dynamic / binary_dynamic, command.rs:2933-3048).
+ * The reference takes a SPIR-V fragment shader and its uniform bytes; here the compiled GPU
+ * program is a PTX or cubin module holding a kernel with this parameter block, launched with
+ * 16 x 16 blocks over the result (grid ceil(width / 16) x ceil(height / 16)).  Operands arrive
+ * as linear RGBA32F images (the values a shader samples, tightly packed rows), the kernel
+ * writes the result as linear RGBA32F, and the executor encodes it to the declared texel. */
+typedef struct zs_dyn_args {
+    const float *src[2];        /* operands (null where absent), RGBA32F, width * 16 bytes per row */
+    int32_t src_width[2], src_height[2];
+    float *dst;                 /* result, RGBA32F, width * 16 bytes per row */
+    int32_t width, height;
+    const void *uniforms;       /* the operation's uniform bytes (device memory), or null */
+    uint64_t uniform_len;
+} zs_dyn_args;
+/* Loads a module (PTX text with its terminating zero, or a cubin / fatbin image) and names its
+ * kernel `kernel_name`, whose only parameter is a zs_dyn_args; returns an op id for the
+ * *_dynamic commands.  The module is loaded on the current device at registration. */
+int zs_register_op(const void *image, uint64_t len, const char *kernel_name, uint32_t *op);
+int zs_cmd_construct_dynamic(zs_cmd *cmd, uint32_t op, const void *uniforms, uint64_t len,
+                             const zs_descriptor *desc, uint32_t *reg);
+int zs_cmd_unary_dynamic(zs_cmd *cmd, uint32_t src, uint32_t op, const void *uniforms, uint64_t len,
+                         const zs_descriptor *desc, uint32_t *reg);
+int zs_cmd_binary_dynamic(zs_cmd *cmd, uint32_t lhs, uint32_t rhs, uint32_t op, const void *uniforms,
+                          uint64_t len, const zs_descriptor *desc, uint32_t *reg);
 /* CommandBuffer::output (command.rs:1707). */
 int zs_cmd_output(zs_cmd *cmd, uint32_t src, uint32_t *reg, zs_descriptor *outformat);
 /* Describe a register (command.rs describe_reg). */

@@ -333,3 +333,12 @@ def test_tuning_cache_and_keys(tmp_path):
     bad.write_text("oops\n")
     with pytest.raises(ZosimosError):
         zs.tune_cache_load(bad)
+
+
+def test_custom_op_ids_are_checked_without_device():
+    c = CommandBuffer()
+    i = c.input(Descriptor.srgb_rgba8(8, 8))
+    with pytest.raises(ZosimosError) as e:
+        c.unary_dynamic(i, 12345, Descriptor.srgb_rgba8(8, 8))
+    assert e.value.code == 10
+    c.output(i)

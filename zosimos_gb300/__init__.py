@@ -195,6 +195,10 @@ def _lib():
             "zs_batch_run_device": ([P, P, P, U32, P], I32), "zs_batch_run": ([P, P, P, U32, P], I32),
             "zs_executable_io_count": ([P, P, P], I32),
             "zs_cmd_with_knob": ([P], I32), "zs_cmd_with_buffer": ([P, U32], I32),
+            "zs_register_op": ([P, U64, ctypes.c_char_p, pU32], I32),
+            "zs_cmd_construct_dynamic": ([P, U32, P, U64, pD, pU32], I32),
+            "zs_cmd_unary_dynamic": ([P, U32, U32, P, U64, pD, pU32], I32),
+            "zs_cmd_binary_dynamic": ([P, U32, U32, U32, P, U64, pD, pU32], I32),
             "zs_autotune": ([P, P, U32, P, U32, P, U32, P], I32),
             "zs_autotune_batch_thumbnails": ([P, P, P, P, U32, U32, P, P, U32, P], I32),
             "zs_executable_set_launch": ([P, U32, I32], I32), "zs_executable_get_launch": ([P, U32, P], I32),
@@ -588,6 +592,19 @@ class CommandBuffer:
         _check(_lib().zs_cmd_with_buffer(self._h, buffer))
         return self
 
+    def construct_dynamic(self, op: int, desc: Descriptor, uniforms=b"") -> int:
+        """CommandBuffer::construct_dynamic: a registered custom kernel with no operand."""
+        u = _uniform_bytes(uniforms)
+        return self._reg(_lib().zs_cmd_construct_dynamic, op, u, len(u), ctypes.byref(desc._c()))
+
+    def unary_dynamic(self, src: int, op: int, desc: Descriptor, uniforms=b"") -> int:
+        u = _uniform_bytes(uniforms)
+        return self._reg(_lib().zs_cmd_unary_dynamic, src, op, u, len(u), ctypes.byref(desc._c()))
+
+    def binary_dynamic(self, lhs: int, rhs: int, op: int, desc: Descriptor, uniforms=b"") -> int:
+        u = _uniform_bytes(uniforms)
+        return self._reg(_lib().zs_cmd_binary_dynamic, lhs, rhs, op, u, len(u), ctypes.byref(desc._c()))
+
     def output(self, src: int):
         reg = ctypes.c_uint32()
         d = _CDesc()
@@ -864,6 +881,23 @@ class PinnedBuffer:
 
 def device_synchronize() -> None:
     _check(_lib().zs_device_synchronize())
+
+
+def _uniform_bytes(data) -> bytes:
+    if isinstance(data, np.ndarray):
+        return bytes(np.ascontiguousarray(data).view(np.uint8).reshape(-1))
+    return bytes(data)
+
+
+def register_op(image: bytes, kernel_name: str) -> int:
+    """zs_register_op: a custom operation's compiled module (PTX text or cubin) and kernel name
+    (the analogue of a ShaderCommand's SPIR-V source); returns its op id."""
+    data = bytes(image)
+    if not data.endswith(b"\0"):
+        data += b"\0"          # PTX text must be terminated; a cubin ignores the extra byte
+    op = ctypes.c_uint32()
+    _check(_lib().zs_register_op(data, len(data), kernel_name.encode(), ctypes.byref(op)))
+    return op.value
 
 
 def tune_cache_get(key: str) -> int:

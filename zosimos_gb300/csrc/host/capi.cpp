@@ -1,6 +1,7 @@
 // capi.cpp -- the extern "C" boundary (include/zosimos.h).  Every entry point catches
 // the internal error type and returns a status code; zs_last_error() holds the text.
 #include <cstring>
+#include <mutex>
 #include <exception>
 #include <string>
 
@@ -33,6 +34,8 @@ uint32_t cmd_from_buffer(Command &c, uint32_t buffer, const Desc &target);
 void fractal_noise_with_octaves(uint32_t octaves, float p[5]);
 void fractal_noise_set_damping(float p[5], float damping);
 uint32_t cmd_output(Command &c, uint32_t src, Desc *outformat);
+uint32_t cmd_dynamic(Command &c, uint32_t nops, uint32_t a, uint32_t b, uint32_t op_id, const void *uniforms,
+                     uint64_t len, const Desc &target);
 int batch_thumbnails(Executable *chain, const void *const *images, const uint32_t *widths, const uint32_t *heights,
                      uint32_t n, uint32_t canvas, void *out, cudaStream_t stream);
 }  // namespace zs
@@ -69,6 +72,17 @@ zs_executable::~zs_executable() {
     for (cudaStream_t t : stripes)
         if (t) cudaStreamDestroy(t);
 }
+
+// Registered custom operations (zs_register_op): loaded modules and their kernels.
+namespace zs {
+static std::mutex g_dyn_mutex;
+static std::vector<std::pair<cudaLibrary_t, cudaKernel_t>> g_dyn;
+
+void *dynamic_kernel(uint32_t op) {
+    std::lock_guard<std::mutex> lock(g_dyn_mutex);
+    return op < g_dyn.size() ? (void *)g_dyn[op].second : nullptr;
+}
+}  // namespace zs
 
 static void note_graph_launch(const Executable &E) {
     uint64_t n = 0;
@@ -411,6 +425,49 @@ int zs_cmd_with_buffer(zs_cmd *cmd, uint32_t buffer) {
     });
 }
 
+int zs_register_op(const void *image, uint64_t len, const char *kernel_name, uint32_t *op) {
+    return guarded([&] {
+        NEED(image); NEED(kernel_name); NEED(op);
+        if (len == 0) fail(ZS_ERR_INVALID_ARG, "empty module image");
+        cudaLibrary_t lib = nullptr;
+        check_cuda(cudaLibraryLoadData(&lib, image, nullptr, nullptr, 0, nullptr, nullptr, 0), "module load");
+        cudaKernel_t k = nullptr;
+        const cudaError_t e = cudaLibraryGetKernel(&k, lib, kernel_name);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            cudaLibraryUnload(lib);
+            fail(ZS_ERR_INVALID_ARG, std::string("no kernel named ") + kernel_name + " in the module");
+        }
+        std::lock_guard<std::mutex> lock(g_dyn_mutex);
+        g_dyn.emplace_back(lib, k);
+        *op = (uint32_t)g_dyn.size() - 1;
+    });
+}
+
+int zs_cmd_construct_dynamic(zs_cmd *cmd, uint32_t op, const void *uniforms, uint64_t len, const zs_descriptor *desc,
+                             uint32_t *reg) {
+    return cmd_guarded(cmd, [&] {
+        NEED(cmd); NEED(desc); NEED(reg);
+        *reg = cmd_dynamic(cmd->c, 0, 0, 0, op, uniforms, len, *desc);
+    });
+}
+
+int zs_cmd_unary_dynamic(zs_cmd *cmd, uint32_t src, uint32_t op, const void *uniforms, uint64_t len,
+                         const zs_descriptor *desc, uint32_t *reg) {
+    return cmd_guarded(cmd, [&] {
+        NEED(cmd); NEED(desc); NEED(reg);
+        *reg = cmd_dynamic(cmd->c, 1, src, 0, op, uniforms, len, *desc);
+    });
+}
+
+int zs_cmd_binary_dynamic(zs_cmd *cmd, uint32_t lhs, uint32_t rhs, uint32_t op, const void *uniforms, uint64_t len,
+                          const zs_descriptor *desc, uint32_t *reg) {
+    return cmd_guarded(cmd, [&] {
+        NEED(cmd); NEED(desc); NEED(reg);
+        *reg = cmd_dynamic(cmd->c, 2, lhs, rhs, op, uniforms, len, *desc);
+    });
+}
+
 int zs_cmd_describe(const zs_cmd *cmd, uint32_t reg, zs_descriptor *out) {
     return guarded([&] { NEED(cmd); NEED(out); *out = cmd->c.describe(reg); });
 }
@@ -445,6 +502,10 @@ int zs_compile(const zs_cmd *cmd, zs_program **out) {
                 if (op.u0 == 0 || op.u0 == 4 || op.u0 == 5 || op.u0 == 7)
                     fail(ZS_ERR_UNIMPLEMENTED, "derivative method not yet implemented");
                 p.uses[op.a]++;
+                break;
+            case OpKind::Dynamic:
+                if (op.u0 > 0) p.uses[op.a]++;
+                if (op.u0 > 1) p.uses[op.b]++;
                 break;
             case OpKind::Inject:
             case OpKind::Inscribe:

@@ -34,6 +34,30 @@ std::vector<float> knob_cons(OpKind kind, const uint8_t *data, uint64_t len) {
     return f;
 }
 
+// CommandBuffer::construct_dynamic / unary_dynamic / binary_dynamic (command.rs:2933-3048):
+// a registered custom kernel over 0, 1 or 2 image operands, result described by `target`.
+uint32_t cmd_dynamic(Command &c, uint32_t nops, uint32_t a, uint32_t b, uint32_t op_id, const void *uniforms,
+                     uint64_t len, const Desc &target) {
+    if (!dynamic_kernel(op_id)) fail(ZS_ERR_INVALID_ARG, "no custom operation with this id (zs_register_op)");
+    if (!is_consistent(target)) fail(ZS_ERR_TYPE, "inconsistent descriptor: " + describe(target));
+    // Operands must be images (CommandError::INVALID_CALL otherwise).
+    if (nops > 0) c.describe(a);
+    if (nops > 1) c.describe(b);
+    Op op;
+    op.kind = OpKind::Dynamic;
+    op.a = a;
+    op.b = b;
+    op.u0 = nops;
+    op.dyn_op = op_id;
+    op.desc = target;
+    if (len) {
+        if (!uniforms) fail(ZS_ERR_INVALID_ARG, "uniform bytes missing");
+        op.data.assign((const uint8_t *)uniforms, (const uint8_t *)uniforms + len);
+    }
+    op.len = len;
+    return c.push(op);
+}
+
 uint32_t Command::push(Op op) {
     // CommandBuffer::with_knob / with_buffer apply to exactly this op (command.rs:1740-1765).
     const bool knob = pending_knob;

@@ -484,6 +484,21 @@ struct Planner {
         materialize(reg);
     }
 
+    // A buffer holding `reg` as linear RGBA32F with tight rows (the layout custom kernels
+    // read): its own buffer when it is stored that way, else a conversion launch into one.
+    int f32_operand(uint32_t reg) {
+        need(reg);
+        const Val &v = vals[reg];
+        const Slot &s = E.slots[v.slot];
+        if (format_equal(v.fmt, linear_f32_format()) && s.stride == (int64_t)s.width * 16) return v.slot;
+        const Desc &d = desc(reg);
+        auto p = new_pending(ZS_PR_LOAD, d.width, d.height, "operand to RGBA32F");
+        set_src(*p, 0, reg);
+        const int slot = new_slot(SlotKind::Intermediate, d.width, d.height, linear_f32_format());
+        emit_step(*p, slot);
+        return slot;
+    }
+
     // A register that is a still-pending solid colour whose program is empty (its
     // declared texel does not quantise it): its value is the constant itself.
     bool solid_value(uint32_t reg, float out[4]) {
@@ -868,6 +883,29 @@ struct Planner {
                 for (int k = 0; k < 9; ++k) p->a.cons[k] = op.fparams[k];
                 set_pending(r, std::move(p));
             } break;
+            case OpKind::Dynamic: {
+                // A custom kernel: operands as linear RGBA32F buffers, result into an RGBA32F
+                // buffer, then read back like any stored value (its declared texel quantises it).
+                int srcs[2] = {-1, -1};
+                for (uint32_t i = 0; i < op.u0; ++i) {
+                    const uint32_t reg = i == 0 ? op.a : op.b;
+                    use(reg);
+                    srcs[i] = f32_operand(reg);
+                }
+                const int out = new_slot(SlotKind::Intermediate, d.width, d.height, linear_f32_format());
+                Step st;
+                st.kind = StepKind::Dynamic;
+                st.dyn_op = op.dyn_op;
+                st.src_slot[0] = srcs[0];
+                st.src_slot[1] = srcs[1];
+                st.dst_slot = out;
+                if (!op.data.empty()) st.dyn_uniform_slot = table_slot(op.data.data(), op.data.size());
+                st.label = "custom op " + std::to_string(op.dyn_op);
+                E.steps.push_back(st);
+                auto p = new_pending(ZS_PR_LOAD, d.width, d.height, "custom op result");
+                set_src_slot(*p, 0, out);
+                set_pending(r, std::move(p));
+            } break;
             case OpKind::Blend: {
                 use(op.a);
                 use(op.b);
@@ -1147,7 +1185,7 @@ std::unique_ptr<Executable> lower(const Program &prog, const zs_capabilities &ca
         const Step &s = E->steps[i];
         os << "  [" << i << "] "
            << (s.kind == StepKind::Chain ? "chain" : s.kind == StepKind::Copy ? "copy"
-               : s.kind == StepKind::Layers ? "layers" : "raster")
+               : s.kind == StepKind::Layers ? "layers" : s.kind == StepKind::Dynamic ? "custom" : "raster")
            << " " << s.label << " -> slot " << s.dst_slot;
         if (s.kind == StepKind::Raster) os << " (" << s.raster.width << "x" << s.raster.height << ", " << s.raster.prog.n
                                            << " ops" << (s.raster.raw_copy ? ", raw" : "") << ")";

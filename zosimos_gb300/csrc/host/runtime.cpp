@@ -170,6 +170,29 @@ void Executable::record_range(cudaStream_t stream, const std::vector<void *> &pt
             cudaGetLastError();
             check_cuda(launch_raster(raster_args(st, ptrs), sm_count, stream), st.label.c_str());
         } break;
+        case StepKind::Dynamic: {
+            void *kernel = dynamic_kernel(st.dyn_op);
+            if (!kernel) fail(ZS_ERR_INVALID_ARG, "custom operation is no longer registered");
+            zs_dyn_args a{};
+            for (int i = 0; i < 2; ++i)
+                if (st.src_slot[i] >= 0) {
+                    a.src[i] = (const float *)ptrs[st.src_slot[i]];
+                    a.src_width[i] = slots[st.src_slot[i]].width;
+                    a.src_height[i] = slots[st.src_slot[i]].height;
+                }
+            const Slot &d = slots[st.dst_slot];
+            a.dst = (float *)ptrs[st.dst_slot];
+            a.width = d.width;
+            a.height = d.height;
+            if (st.dyn_uniform_slot >= 0) {
+                a.uniforms = ptrs[st.dyn_uniform_slot];
+                a.uniform_len = slots[st.dyn_uniform_slot].bytes;
+            }
+            void *params[] = {&a};
+            const dim3 block(16, 16), grid((unsigned)(d.width + 15) / 16, (unsigned)(d.height + 15) / 16);
+            check_cuda(cudaLaunchKernel(kernel, grid, block, params, 0, stream), st.label.c_str());
+            add_kernel_launches(1);
+        } break;
         case StepKind::Raster: {
             ZsRasterArgs a = raster_args(st, ptrs);
             if (patches)

@@ -89,7 +89,7 @@ struct HProgram {
 enum class OpKind {
     Input, Output, Crop, ColorConvert, ChromaticAdaptation, ColorMatrix, Extract, Inject,
     Transmute, Inscribe, InscribePlaced, Palette, Bilinear, Solid, Affine, Resize,
-    ResizeFiltered, Blend, Derivative, Normal2d, FractalNoise, BufferInit, FromBuffer
+    ResizeFiltered, Blend, Derivative, Normal2d, FractalNoise, BufferInit, FromBuffer, Dynamic
 };
 
 struct Op {
@@ -103,6 +103,7 @@ struct Op {
     HProgram prog;               // per-pixel semantics of colour ops
     std::vector<uint8_t> data;   // BufferInit: initial bytes (zero-extended to `len`)
     uint64_t len = 0;            // BufferInit: buffer size in bytes
+    uint32_t dyn_op = 0;         // Dynamic: registered op id; u0 = number of operands (0, 1, 2)
     bool knob = false;           // WithKnob: the parameters can be replaced at run time
     int32_t param_buffer = -1;   // WithBuffer: parameters read from this buffer register
 };
@@ -157,7 +158,10 @@ struct SrcRef {
     int64_t stride = 0;
 };
 
-enum class StepKind { Raster, Chain, Copy, Layers };
+enum class StepKind { Raster, Chain, Copy, Layers, Dynamic };
+
+// A registered custom operation: its loaded module's kernel (cudaKernel_t) per registration.
+void *dynamic_kernel(uint32_t op);
 
 // One layer of a fused layer stack: its source buffer and the sampling/blend setup.
 struct LayerRef {
@@ -186,6 +190,8 @@ struct Step {
     uint64_t copy_rows = 0;
     int64_t copy_src_pitch = 0, copy_dst_pitch = 0;
     int tune_threads = 0;        // Chain: block size chosen by the autotuner (0: default)
+    uint32_t dyn_op = 0;         // Dynamic: registered op; src_slot[0..1] RGBA32F operands,
+    int dyn_uniform_slot = -1;   //   dst_slot an RGBA32F result, uniforms in this table slot
     std::string label;
 };
 
