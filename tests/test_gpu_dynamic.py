@@ -44,15 +44,14 @@ def test_unary_and_binary_custom_ops(ops, mode):
     lin = zs.Descriptor.linear_rgba_f32(97, 61)
     inv = c.unary_dynamic(ia, ops["invert"], lin)
     mixed = c.binary_dynamic(inv, ib, ops["mix"], lin, np.array([0.25], np.float32))
-    adapted = c.chromatic_adaptation(mixed, zs.ChromaticAdaptationMethod.VonKries, zs.Whitepoint.D50)
-    o, _ = c.output(c.color_convert(adapted, zs.Descriptor.srgb_rgba8(97, 61)))
+    scaled = c.color_matrix(mixed, [0.9, 0.05, 0.0, 0.0, 1.0, 0.1, 0.02, 0.0, 0.95])
+    o, _ = c.output(c.color_convert(scaled, zs.Descriptor.srgb_rgba8(97, 61)))
     got = P.run(c, pool, [(ia, ka), (ib, kb)], [o], mode)[0]
     la, lb = decode(a), decode(b)
     x = la.copy()
     x[..., :3] = 1.0 - la[..., :3]
     x = x + 0.25 * (lb - x)
-    m = np.linalg.inv(O.rgb_to_xyz("Bt709", "D50")) @ O.adaptation("VonKries", "D65", "D50") @ O.rgb_to_xyz()
-    O.mat3(x, m)
+    O.mat3(x, np.array([0.9, 0.05, 0.0, 0.0, 1.0, 0.1, 0.02, 0.0, 0.95]).reshape(3, 3))
     want = O.encode(O.SRGB_RGBA8, np.ascontiguousarray(x))
     assert np.abs(got.astype(int) - want.astype(int)).max() <= 1
 
