@@ -270,10 +270,42 @@ int zs_cmd_output(zs_cmd *cmd, uint32_t src, uint32_t *reg, zs_descriptor *outfo
 /* Describe a register (command.rs describe_reg). */
 int zs_cmd_describe(const zs_cmd *cmd, uint32_t reg, zs_descriptor *out);
 
+/* ---- generic functions (command.rs:756-922) ------------------------------ */
+/* CommandBuffer::generic (command.rs:768): declares a generic descriptor parameter; returns
+ * the descriptor variable (DescriptorVar) standing for it. */
+int zs_cmd_generic(zs_cmd *cmd, uint32_t *ty);
+/* CommandBuffer::input_generic (command.rs:756): an input whose descriptor is the variable's. */
+int zs_cmd_input_generic(zs_cmd *cmd, uint32_t ty, uint32_t *reg);
+/* CommandBuffer::derive_descriptor (command.rs:786-805): variable `base` with its size replaced
+ * by width x height (both 0: kept). */
+int zs_cmd_derive_descriptor(zs_cmd *cmd, uint32_t base, uint32_t width, uint32_t height, uint32_t *ty);
+/* CommandBuffer::register_descriptor (command.rs:808): a descriptor variable of a register. */
+int zs_cmd_register_descriptor(zs_cmd *cmd, uint32_t reg, uint32_t *ty);
+/* CommandBuffer::computed_signature (command.rs:821): counts of generics, inputs, outputs. */
+int zs_cmd_signature(const zs_cmd *cmd, uint32_t *n_generics, uint32_t *n_inputs, uint32_t *n_outputs);
+/* CommandBuffer::function (command.rs:856): declares a function with the signature computed
+ * from `signature` (a snapshot is kept); its definition is supplied to zs_link. */
+int zs_cmd_function(zs_cmd *cmd, const zs_cmd *signature, uint32_t *function);
+/* CommandBuffer::invoke (command.rs:863-922): calls `function` with descriptor variables for its
+ * generics and argument registers (checked against its inputs: ZS_ERR_OTHER, INVALID_CALL,
+ * on a mismatch); writes the n_results result registers. */
+int zs_cmd_invoke(zs_cmd *cmd, uint32_t function, const uint32_t *generics, uint32_t n_generics, const uint32_t *args,
+                  uint32_t n_args, uint32_t *results, uint32_t n_results);
+
 /* ---- Linker / Program (command.rs:2063-2185, program.rs:1284-1423) -------- */
 typedef struct zs_program zs_program;
 /* Linker::compile (command.rs:2069). */
 int zs_compile(const zs_cmd *cmd, zs_program **out);
+/* Linker::link (command.rs:2083-2185): `main` (its generic parameters given by the n_tys
+ * descriptors `tys`) and the function definitions; links[i] (of
+ * link_counts[i] entries) names, for each function declared in buffer i (0 = main, i = function
+ * i - 1), the buffer defining it.  Every invocation is monomorphised for its generics and
+ * inlined, so the program is planned (and fused) as a whole.  Registers of main keep their
+ * numbers for binding and retiring; a function's registers are reached with its link index
+ * (zs_executable_query_knob). */
+int zs_link(const zs_cmd *main, const zs_descriptor *tys, uint32_t n_tys, const zs_cmd *const *functions,
+            uint32_t n_functions, const uint32_t *const *links, const uint32_t *link_counts, uint32_t n_links,
+            zs_program **out);
 void zs_program_free(zs_program *program);
 
 /* Capabilities / lowering options (program.rs:1304 lower_to). */

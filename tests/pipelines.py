@@ -211,6 +211,53 @@ def oracle_palette(bg):
     return rgba_bytes(bg[iy, ix])
 
 
+# ---------------------------------------------------------------- generic.rs:16-134 generic palette
+
+GENERIC_IDX = dict(u_min=[0.0] * 4, u_max=[0.0] * 4, v_min=[0.0] * 4, v_max=[0.0] * 4, uv_min=[0.0] * 4,
+                   uv_max=[1.0, 1.0, 0.0, 0.0])
+
+
+def generic_palette_function() -> CommandBuffer:
+    """The generic function of generic.rs:34-68: palette of a generic input indexed by a
+    2048x2048 RGBA-u8 scalar bilinear grid, height from R and width from G."""
+    f = CommandBuffer()
+    a = f.generic()
+    img = f.input_generic(a)
+    idx_desc = Descriptor.srgb_rgba8(2048, 2048).with_color(color=ColorKind.Scalars, transfer=Transfer.Linear)
+    idx = f.bilinear(idx_desc, **GENERIC_IDX)
+    pal = f.palette(img, 1, 0, idx)
+    f.output(pal)
+    return f
+
+
+def ours_generic(bg, mode=zs.Mode.Fused):
+    pool = Pool()
+    kb = pool.insert_srgb(bg)
+    fn = generic_palette_function()
+    c = CommandBuffer()
+    conv = c.function(fn)
+    i = c.input(pool.descriptor(kb))
+    ty = c.register_descriptor(i)
+    (res,) = c.invoke(conv, generics=[ty], arguments=[i])
+    o, _ = c.output(res)
+    prog = zs.Linker.from_included().link(c, [], [fn], [[1], []])
+    exe = prog.lower_to(Capabilities(mode=mode))
+    env = exe.from_pool(pool)
+    env.bind(i, kb)
+    ex = exe.launch(env)
+    while ex.is_running():
+        ex.step()
+    return pool.read(ex.retire_output(o))
+
+
+def oracle_generic(bg):
+    idx = O.bilinear_construct(2048, 2048, **GENERIC_IDX, f32=True).astype(np.float64)
+    ib = O.encode(O.LINEAR_RGBA8, idx)
+    idd = O.decode(O.LINEAR_RGBA8, ib, 2048, 2048).astype(np.float32)
+    ix, iy = O.palette_index(bg.shape[1], bg.shape[0], idd[..., 1], idd[..., 0])
+    return rgba_bytes(bg[iy, ix])
+
+
 # ---------------------------------------------------------------- blend.rs:449-575 oklab / srlab2
 
 GRID = dict(u_min=[0.4, 0.0, 0.0, 1.0], v_min=[0.4, 0.0, 0.0, 1.0], u_max=[0.4, 0.0, 1.0, 1.0],

@@ -172,6 +172,53 @@ def test_palette(background, goldens):
     assert min(bin(int(h, 16) ^ int(g, 16)).count("1") for g in goldens["palette"]) <= 8
 
 
+@pytest.mark.parametrize("mode", [zs.Mode.Fused, zs.Mode.PerOpF32])
+def test_generic_palette(background, goldens, mode):
+    # lib/zosimos/tests/generic.rs: a generic palette function invoked on the background and
+    # linked; the 2048^2 output is a byte-exact gather of the oracle's indices.
+    ours = P.ours_generic(background, mode)
+    assert (ours == P.oracle_generic(background)).all()
+    h = blockhash256(ours.reshape(2048, 2048, 4))
+    assert min(bin(int(h, 16) ^ int(g, 16)).count("1") for g in goldens["generic"]) <= 8
+
+
+def test_linked_instantiations_equal_flat_program():
+    # one generic resize function called for two descriptors; the linked program's outputs are
+    # the flat program's, byte for byte (both run on the device)
+    img = srgb_gradient_noise(300, 200, seed=7)
+    pool = zs.Pool()
+    ka = pool.insert_srgb(img)
+    kb = pool.insert(zs.Descriptor.linear_rgba_f32(300, 200), img.astype(np.float32) / 255.0)
+
+    f = zs.CommandBuffer()
+    a = f.generic()
+    f.output(f.resize_filtered(f.input_generic(a), (96, 64), zs.Filter.Lanczos3))
+    c = zs.CommandBuffer()
+    fn = c.function(f)
+    x = c.input(pool.descriptor(ka))
+    y = c.input(pool.descriptor(kb))
+    (rx,) = c.invoke(fn, generics=[c.register_descriptor(x)], arguments=[x])
+    (ry,) = c.invoke(fn, generics=[c.register_descriptor(y)], arguments=[y])
+    ox, _ = c.output(rx)
+    oy, _ = c.output(ry)
+    exe = zs.Linker.from_included().link(c, [], [f], [[1], []]).lower_to()
+    env = exe.from_pool(pool)
+    env.bind(x, ka)
+    env.bind(y, kb)
+    ex = exe.launch(env)
+    while ex.is_running():
+        ex.step()
+    linked = [pool.read(ex.retire_output(o)) for o in (ox, oy)]
+
+    flat = zs.CommandBuffer()
+    x2 = flat.input(pool.descriptor(ka))
+    y2 = flat.input(pool.descriptor(kb))
+    o2 = [flat.output(flat.resize_filtered(r, (96, 64), zs.Filter.Lanczos3))[0] for r in (x2, y2)]
+    keys = zs.run_pipeline(flat, pool, [(x2, ka), (y2, kb)], o2)
+    for got, key in zip(linked, keys):
+        assert (got == pool.read(key)).all()
+
+
 @pytest.mark.parametrize("space", ["oklab", "srlab2"])
 def test_lab_grid(space, goldens):
     ours = P.ours_lab_grid(space)

@@ -63,6 +63,13 @@ def test_transmute_golden(background, goldens):
     assert blockhash256(img) in goldens["transmute"]
 
 
+def test_oracle_generic_palette_close_to_goldens(background, goldens):
+    # lib/zosimos/tests/generic.rs: the palette of the background indexed by a 2048^2 grid.
+    # The two accepted goldens differ from each other by 15 bits (device variance).
+    h = blockhash256(P.oracle_generic(background).reshape(2048, 2048, 4))
+    assert min(hamming(h, g) for g in goldens["generic"]) <= 8
+
+
 def test_oracle_palette_close_to_goldens(background, goldens):
     h = blockhash256(P.oracle_palette(background).reshape(400, 400, 4))
     # The two accepted goldens differ from each other by 8 bits (device variance).

@@ -13,7 +13,7 @@ import ctypes
 import math
 import os
 from dataclasses import dataclass, field, replace
-from typing import Optional, Sequence
+from typing import List, Optional, Sequence
 
 import numpy as np
 
@@ -207,6 +207,12 @@ def _lib():
             "zs_tune_cache_save": ([ctypes.c_char_p], I32), "zs_tune_cache_load": ([ctypes.c_char_p], I32),
             "zs_executable_query_knob": ([P, U32, U32, pU32, pU64], I32),
             "zs_executable_set_knob": ([P, U32, P, U64], I32), "zs_env_knob": ([P, U32, P, U64], I32),
+            "zs_cmd_generic": ([P, pU32], I32), "zs_cmd_input_generic": ([P, U32, pU32], I32),
+            "zs_cmd_derive_descriptor": ([P, U32, U32, U32, pU32], I32),
+            "zs_cmd_register_descriptor": ([P, U32, pU32], I32),
+            "zs_cmd_signature": ([P, pU32, pU32, pU32], I32), "zs_cmd_function": ([P, P, pU32], I32),
+            "zs_cmd_invoke": ([P, U32, pU32, U32, pU32, U32, pU32, U32], I32),
+            "zs_link": ([P, pD, U32, ctypes.POINTER(P), U32, ctypes.POINTER(pU32), pU32, U32, ctypes.POINTER(P)], I32),
         }
         for name, (args, res) in sig.items():
             fn = getattr(lib, name)
@@ -605,6 +611,54 @@ class CommandBuffer:
         u = _uniform_bytes(uniforms)
         return self._reg(_lib().zs_cmd_binary_dynamic, lhs, rhs, op, u, len(u), ctypes.byref(desc._c()))
 
+    # -- generic functions (command.rs:756-922)
+
+    def generic(self) -> int:
+        """CommandBuffer::generic: a generic descriptor parameter; returns its descriptor variable."""
+        ty = ctypes.c_uint32()
+        _check(_lib().zs_cmd_generic(self._h, ctypes.byref(ty)))
+        return ty.value
+
+    def input_generic(self, ty: int) -> int:
+        return self._reg(_lib().zs_cmd_input_generic, ty)
+
+    def derive_descriptor(self, base: int, size=None) -> int:
+        """CommandBuffer::derive_descriptor: variable `base` with its size replaced (None: kept)."""
+        w, h = size if size is not None else (0, 0)
+        return self._reg(_lib().zs_cmd_derive_descriptor, base, w, h)
+
+    def register_descriptor(self, reg: int) -> int:
+        return self._reg(_lib().zs_cmd_register_descriptor, reg)
+
+    def computed_signature(self):
+        """(generics, inputs, outputs) counts of this buffer as a function."""
+        g, i, o = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+        _check(_lib().zs_cmd_signature(self._h, ctypes.byref(g), ctypes.byref(i), ctypes.byref(o)))
+        return g.value, i.value, o.value
+
+    def function(self, signature: "CommandBuffer") -> int:
+        """CommandBuffer::function: declares a function with `signature`'s computed signature."""
+        f = self._reg(_lib().zs_cmd_function, signature._h)
+        if not hasattr(self, "_fn_outputs"):
+            self._fn_outputs = {}
+        self._fn_outputs[f] = signature.computed_signature()[2]
+        return f
+
+    def invoke(self, function: int, generics: Sequence[int] = (), arguments: Sequence[int] = ()) -> List[int]:
+        """CommandBuffer::invoke: returns the result registers."""
+        sig = self._functions_outputs(function)
+        g = (ctypes.c_uint32 * max(len(generics), 1))(*generics)
+        a = (ctypes.c_uint32 * max(len(arguments), 1))(*arguments)
+        r = (ctypes.c_uint32 * max(sig, 1))()
+        _check(_lib().zs_cmd_invoke(self._h, function, g, len(generics), a, len(arguments), r, sig))
+        return list(r[:sig])
+
+    def _functions_outputs(self, function: int) -> int:
+        outs = getattr(self, "_fn_outputs", {})
+        if function not in outs:
+            raise ZosimosError(3, "no such function")
+        return outs[function]
+
     def output(self, src: int):
         reg = ctypes.c_uint32()
         d = _CDesc()
@@ -630,6 +684,21 @@ class Linker:
     def compile(self, commands: CommandBuffer) -> "Program":
         h = ctypes.c_void_p()
         _check(_lib().zs_compile(commands._h, ctypes.byref(h)))
+        return Program(h)
+
+    def link(self, main: CommandBuffer, tys: Sequence[Descriptor] = (), functions: Sequence[CommandBuffer] = (),
+             links: Sequence[Sequence[int]] = ()) -> "Program":
+        """Linker::link: links[i] lists, for each function declared in buffer i (0 = main, then
+        `functions`), the buffer index (0 = main) that defines it."""
+        nt = len(tys)
+        ct = (_CDesc * max(nt, 1))(*[d._c() for d in tys])
+        fs = (ctypes.c_void_p * max(len(functions), 1))(*[f._h for f in functions])
+        rows = [(ctypes.c_uint32 * max(len(l), 1))(*l) for l in links]
+        lp = (ctypes.POINTER(ctypes.c_uint32) * max(len(links), 1))(
+            *[ctypes.cast(r, ctypes.POINTER(ctypes.c_uint32)) for r in rows])
+        lc = (ctypes.c_uint32 * max(len(links), 1))(*[len(l) for l in links])
+        h = ctypes.c_void_p()
+        _check(_lib().zs_link(main._h, ct, nt, fs, len(functions), lp, lc, len(links), ctypes.byref(h)))
         return Program(h)
 
 

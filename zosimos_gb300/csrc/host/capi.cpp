@@ -425,6 +425,94 @@ int zs_cmd_with_buffer(zs_cmd *cmd, uint32_t buffer) {
     });
 }
 
+int zs_cmd_generic(zs_cmd *cmd, uint32_t *ty) {
+    return guarded([&] {
+        NEED(cmd); NEED(ty);
+        TyVar t;
+        t.var = cmd->c.nvars++;
+        cmd->c.tys.push_back(t);
+        *ty = (uint32_t)cmd->c.tys.size() - 1;
+    });
+}
+
+int zs_cmd_input_generic(zs_cmd *cmd, uint32_t ty, uint32_t *reg) {
+    return cmd_guarded(cmd, [&] {
+        NEED(cmd); NEED(reg);
+        if (ty >= cmd->c.tys.size()) fail(ZS_ERR_BAD_REGISTER, "no such descriptor variable");
+        Op op{OpKind::Input};
+        op.desc = ty_descriptor(cmd->c, ty);
+        op.generic_var = (int32_t)ty;
+        *reg = cmd->c.push(op);
+    });
+}
+
+int zs_cmd_derive_descriptor(zs_cmd *cmd, uint32_t base, uint32_t width, uint32_t height, uint32_t *ty) {
+    return guarded([&] {
+        NEED(cmd); NEED(ty);
+        if (base >= cmd->c.tys.size()) fail(ZS_ERR_BAD_REGISTER, "no such descriptor variable");
+        if ((width == 0) != (height == 0)) fail(ZS_ERR_INVALID_ARG, "give both sides of the size or neither");
+        TyVar t;
+        t.base = (int32_t)base;
+        t.width = width;
+        t.height = height;
+        cmd->c.tys.push_back(t);
+        *ty = (uint32_t)cmd->c.tys.size() - 1;
+    });
+}
+
+int zs_cmd_register_descriptor(zs_cmd *cmd, uint32_t reg, uint32_t *ty) {
+    return guarded([&] {
+        NEED(cmd); NEED(ty);
+        cmd->c.describe(reg);
+        TyVar t;
+        t.reg = (int32_t)reg;
+        cmd->c.tys.push_back(t);
+        *ty = (uint32_t)cmd->c.tys.size() - 1;
+    });
+}
+
+int zs_cmd_signature(const zs_cmd *cmd, uint32_t *n_generics, uint32_t *n_inputs, uint32_t *n_outputs) {
+    return guarded([&] {
+        NEED(cmd);
+        uint32_t ni = 0, no = 0;
+        for (const Op &op : cmd->c.ops) {
+            ni += op.kind == OpKind::Input;
+            no += op.kind == OpKind::Output;
+        }
+        if (n_generics) *n_generics = (uint32_t)cmd->c.nvars;
+        if (n_inputs) *n_inputs = ni;
+        if (n_outputs) *n_outputs = no;
+    });
+}
+
+int zs_cmd_function(zs_cmd *cmd, const zs_cmd *signature, uint32_t *function) {
+    return guarded([&] {
+        NEED(cmd); NEED(signature); NEED(function);
+        if (signature == cmd) fail(ZS_ERR_OTHER, "a command buffer cannot declare itself");
+        cmd->c.functions.push_back(std::make_shared<const Command>(signature->c));
+        *function = (uint32_t)cmd->c.functions.size() - 1;
+    });
+}
+
+int zs_cmd_invoke(zs_cmd *cmd, uint32_t function, const uint32_t *generics, uint32_t n_generics, const uint32_t *args,
+                  uint32_t n_args, uint32_t *results, uint32_t n_results) {
+    return cmd_guarded(cmd, [&] {
+        NEED(cmd);
+        if (n_generics) NEED(generics);
+        if (n_args) NEED(args);
+        std::vector<uint32_t> tys(generics, generics + n_generics), as(args, args + n_args);
+        // Check the result count before recording the call.
+        if (function < cmd->c.functions.size()) {
+            uint32_t no = 0;
+            for (const Op &op : cmd->c.functions[function]->ops) no += op.kind == OpKind::Output;
+            if (no != n_results) fail(ZS_ERR_OTHER, "wrong number of result registers");
+            if (no) NEED(results);
+        }
+        const std::vector<uint32_t> res = cmd_invoke(cmd->c, function, tys, as);
+        for (size_t k = 0; k < res.size(); ++k) results[k] = res[k];
+    });
+}
+
 int zs_register_op(const void *image, uint64_t len, const char *kernel_name, uint32_t *op) {
     return guarded([&] {
         NEED(image); NEED(kernel_name); NEED(op);
@@ -478,48 +566,36 @@ int zs_compile(const zs_cmd *cmd, zs_program **out) {
     return guarded([&] {
         NEED(cmd); NEED(out);
         auto prog = std::make_unique<zs_program>();
-        Program &p = prog->p;
-        p.ops = cmd->c.ops;
-        p.uses.assign(p.ops.size(), 0);
-        for (uint32_t r = 0; r < p.ops.size(); ++r) {
-            const Op &op = p.ops[r];
-            switch (op.kind) {
-            case OpKind::Input: p.inputs.push_back(r); break;
-            case OpKind::Output:
-                p.outputs.push_back(op.a);
-                p.output_regs.push_back(r);
-                p.uses[op.a]++;
-                break;
-            case OpKind::Bilinear:
-            case OpKind::Normal2d:
-            case OpKind::FractalNoise:
-            case OpKind::BufferInit:
-            case OpKind::Solid: break;
-            case OpKind::FromBuffer: p.uses[op.a]++; break;
-            case OpKind::Derivative:
-                // DerivativeMethod::to_shader: Roberts, Scharr4, Scharr5, Scharr5Tab are
-                // CompileError::NotYetImplemented (command.rs:3397-3402).
-                if (op.u0 == 0 || op.u0 == 4 || op.u0 == 5 || op.u0 == 7)
-                    fail(ZS_ERR_UNIMPLEMENTED, "derivative method not yet implemented");
-                p.uses[op.a]++;
-                break;
-            case OpKind::Dynamic:
-                if (op.u0 > 0) p.uses[op.a]++;
-                if (op.u0 > 1) p.uses[op.b]++;
-                break;
-            case OpKind::Inject:
-            case OpKind::Inscribe:
-            case OpKind::InscribePlaced:
-            case OpKind::Palette:
-            case OpKind::Affine:
-            case OpKind::Blend:
-                p.uses[op.a]++;
-                p.uses[op.b]++;
-                break;
-            default: p.uses[op.a]++; break;
+        prog->p = compile_command(cmd->c);
+        *out = prog.release();
+    });
+}
+
+int zs_link(const zs_cmd *main, const zs_descriptor *tys, uint32_t n_tys, const zs_cmd *const *functions,
+            uint32_t n_functions, const uint32_t *const *links, const uint32_t *link_counts, uint32_t n_links,
+            zs_program **out) {
+    return guarded([&] {
+        NEED(main); NEED(out);
+        std::vector<Desc> gen;
+        for (uint32_t i = 0; i < n_tys; ++i) {
+            NEED(tys);
+            gen.push_back(tys[i]);
+        }
+        std::vector<const Command *> buffers{&main->c};
+        for (uint32_t i = 0; i < n_functions; ++i) {
+            NEED(functions); NEED(functions[i]);
+            buffers.push_back(&functions[i]->c);
+        }
+        std::vector<std::vector<uint32_t>> table(n_links);
+        for (uint32_t i = 0; i < n_links; ++i) {
+            NEED(link_counts);
+            if (link_counts[i]) {
+                NEED(links); NEED(links[i]);
+                table[i].assign(links[i], links[i] + link_counts[i]);
             }
         }
-        if (p.output_regs.empty()) fail(ZS_ERR_OTHER, "program has no output");
+        auto prog = std::make_unique<zs_program>();
+        prog->p = link_commands(buffers, gen, table);
         *out = prog.release();
     });
 }
@@ -532,6 +608,7 @@ int zs_lower(const zs_program *program, const zs_capabilities *caps, zs_executab
         if (caps) c = *caps;
         auto exe = std::make_unique<zs_executable>();
         exe->e = lower(program->p, c);
+        exe->e->alias = program->p.alias;
         *out = exe.release();
     });
 }
@@ -555,12 +632,20 @@ int zs_executable_io_count(const zs_executable *exe, uint32_t *inputs, uint32_t 
     });
 }
 
+// A register of the linked command buffers (link index 0: the entry point) in the executable.
+static uint32_t flat_reg(const Executable &E, uint32_t link_idx, uint32_t reg) {
+    auto it = E.alias.find({link_idx, reg});
+    if (it != E.alias.end()) return it->second;
+    if (link_idx != 0) fail(ZS_ERR_BAD_REGISTER, "register of a linked function that was not instantiated");
+    return reg;
+}
+
 int zs_executable_query_knob(const zs_executable *exe, uint32_t link_idx, uint32_t reg, uint32_t *knob,
                              uint64_t *len) {
     return guarded([&] {
         NEED(exe); NEED(knob);
-        if (link_idx != 0) fail(ZS_ERR_BAD_REGISTER, "only link index 0 (the program itself) has knobs");
         const Executable &E = *exe->e;
+        reg = flat_reg(E, link_idx, reg);
         for (size_t i = 0; i < E.knobs.size(); ++i)
             if (E.knobs[i].reg == reg) {
                 *knob = (uint32_t)i;
@@ -624,6 +709,7 @@ int zs_env_bind(zs_environment *env, uint32_t reg, uint64_t key) {
     return guarded([&] {
         NEED(env);
         Executable &E = *env->env.exe;
+        reg = flat_reg(E, 0, reg);
         size_t i = 0;
         for (; i < E.input_regs.size(); ++i)
             if (E.input_regs[i] == reg) break;
@@ -652,6 +738,7 @@ int zs_env_bind_output(zs_environment *env, uint32_t reg, uint64_t key) {
     return guarded([&] {
         NEED(env);
         Executable &E = *env->env.exe;
+        reg = flat_reg(E, 0, reg);
         size_t i = 0;
         for (; i < E.output_regs.size(); ++i)
             if (E.output_regs[i] == reg) break;
@@ -758,6 +845,7 @@ int zs_retire_output(zs_execution *exec, uint32_t reg, uint64_t *key) {
         NEED(exec); NEED(key);
         Execution &X = exec->x;
         Executable &E = *X.exe;
+        reg = flat_reg(E, 0, reg);
         while (X.cursor < X.total) {
             int rc = zs_exec_step(exec);
             if (rc != ZS_OK) fail(rc, last_error());

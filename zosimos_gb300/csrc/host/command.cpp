@@ -79,7 +79,9 @@ uint32_t Command::push(Op op) {
     return (uint32_t)ops.size() - 1;
 }
 
-bool Command::is_value(uint32_t reg) const { return reg < ops.size() && ops[reg].kind != OpKind::Output; }
+bool Command::is_value(uint32_t reg) const {
+    return reg < ops.size() && ops[reg].kind != OpKind::Output && ops[reg].kind != OpKind::Invoke;
+}
 
 const Desc &Command::describe(uint32_t reg) const {
     if (!is_value(reg)) fail(ZS_ERR_BAD_REGISTER, "register does not name an image value");
@@ -264,6 +266,7 @@ uint32_t cmd_inject(Command &c, uint32_t below, uint32_t channel, uint32_t above
     Op op{OpKind::Inject};
     op.a = below;
     op.b = above;
+    op.u0 = channel;
     op.desc = b;
     op.desc.row_stride = 0;
     HInstr i;

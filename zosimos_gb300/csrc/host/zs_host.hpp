@@ -89,7 +89,8 @@ struct HProgram {
 enum class OpKind {
     Input, Output, Crop, ColorConvert, ChromaticAdaptation, ColorMatrix, Extract, Inject,
     Transmute, Inscribe, InscribePlaced, Palette, Bilinear, Solid, Affine, Resize,
-    ResizeFiltered, Blend, Derivative, Normal2d, FractalNoise, BufferInit, FromBuffer, Dynamic
+    ResizeFiltered, Blend, Derivative, Normal2d, FractalNoise, BufferInit, FromBuffer, Dynamic,
+    Invoke, InvokedResult
 };
 
 struct Op {
@@ -104,6 +105,9 @@ struct Op {
     std::vector<uint8_t> data;   // BufferInit: initial bytes (zero-extended to `len`)
     uint64_t len = 0;            // BufferInit: buffer size in bytes
     uint32_t dyn_op = 0;         // Dynamic: registered op id; u0 = number of operands (0, 1, 2)
+    int32_t generic_var = -1;    // Input: the descriptor variable it is declared with (input_generic)
+    std::vector<uint32_t> regs;  // Invoke: argument registers
+    std::vector<uint32_t> tyvars;// Invoke: descriptor variables given for the callee's generics
     bool knob = false;           // WithKnob: the parameters can be replaced at run time
     int32_t param_buffer = -1;   // WithBuffer: parameters read from this buffer register
 };
@@ -115,8 +119,25 @@ uint64_t knob_param_bytes(OpKind kind);
 // Producer constants (ZsRasterArgs::cons) of a parameter block; throws on a bad block.
 std::vector<float> knob_cons(OpKind kind, const uint8_t *data, uint64_t len);
 
+// A descriptor variable of a command buffer (command.rs DescriptorVar): a generic parameter
+// (var >= 0, its descriptor a placeholder until instantiation) or the descriptor of a register.
+struct TyVar {
+    int32_t var = -1;
+    int32_t reg = -1;
+    int32_t base = -1;           // derive_descriptor: the variable this one modifies
+    uint32_t width = 0, height = 0;   // derive_descriptor: the replaced size (0: kept)
+};
+
+struct Command;
+// CommandBuffer::computed_signature (command.rs:821-853): the declared function, kept as a
+// snapshot of the command buffer it was computed from.
+using Signature = std::shared_ptr<const Command>;
+
 struct Command {
     std::vector<Op> ops;
+    std::vector<TyVar> tys;              // descriptor variables
+    int32_t nvars = 0;                   // generic parameters declared
+    std::vector<Signature> functions;    // CommandBuffer::function declarations
     bool pending_knob = false;       // CommandBuffer::with_knob: applies to the next op
     int32_t pending_buffer = -1;     // CommandBuffer::with_buffer: applies to the next op
     void clear_pending() {
@@ -131,6 +152,9 @@ struct Command {
 // ---------------------------------------------------------------- program
 
 struct Program {
+    // Registers of the linked command buffers (link index, register) -> register of `ops`
+    // (only where they differ: after inlining of invoked functions).
+    std::map<std::pair<uint32_t, uint32_t>, uint32_t> alias;
     std::vector<Op> ops;
     std::vector<uint32_t> inputs, outputs;   // registers (outputs: the value registers)
     std::vector<uint32_t> output_regs;       // the Output op registers
@@ -225,6 +249,7 @@ struct Executable {
     std::vector<Step> steps;
     std::vector<uint32_t> input_regs, output_regs;     // value registers in declaration order
     std::vector<Desc> input_desc, output_desc;
+    std::map<std::pair<uint32_t, uint32_t>, uint32_t> alias;   // Program::alias
     std::vector<int> input_slot, output_slot;
     std::vector<void *> dev_buffers;                   // device allocation per slot (owned ones)
     // zs_batch_thumbnails: device image/prefix tables, their pinned staging copy, the event of
@@ -250,6 +275,23 @@ struct Executable {
 };
 
 std::unique_ptr<Executable> lower(const Program &prog, const zs_capabilities &caps);
+
+// ---------------------------------------------------------------- linking (link.cpp)
+
+// Linker::compile (command.rs:2069): use counts, inputs and outputs of a flat command buffer.
+Program compile_command(const Command &c);
+// Linker::link (command.rs:2083-2893): `buffers` = main then the function definitions, `tys`
+// the descriptors of main's generic parameters,
+// links[i][f] = the buffer defining function f of buffer i; invoked functions are
+// monomorphised and inlined, so the whole program is one op list for the planner.
+Program link_commands(const std::vector<const Command *> &buffers, const std::vector<Desc> &tys,
+                      const std::vector<std::vector<uint32_t>> &links);
+// CommandBuffer::invoke (command.rs:863-922): checks the arguments and records the call;
+// returns the result registers.
+std::vector<uint32_t> cmd_invoke(Command &c, uint32_t function, const std::vector<uint32_t> &tyvars,
+                                 const std::vector<uint32_t> &args);
+// Descriptor of descriptor variable `ty` of `c` (a placeholder for a generic parameter).
+Desc ty_descriptor(const Command &c, uint32_t ty);
 
 // ---------------------------------------------------------------- autotuner (autotune.cpp)
 
