@@ -250,10 +250,15 @@ def ours_generic(bg, mode=zs.Mode.Fused):
     return pool.read(ex.retire_output(o))
 
 
+# The index grid's Scalars texels are not a native texture format (program.rs:781-946): they
+# are staged, i.e. quantised by truncation (stage.frag).
+SCALARS_U8 = O.Format(O.BITS["UInt8x4"], O.PARTS["RgbA"], O.TRANSFER["Linear"], False)
+
+
 def oracle_generic(bg):
     idx = O.bilinear_construct(2048, 2048, **GENERIC_IDX, f32=True).astype(np.float64)
-    ib = O.encode(O.LINEAR_RGBA8, idx)
-    idd = O.decode(O.LINEAR_RGBA8, ib, 2048, 2048).astype(np.float32)
+    ib = O.encode(SCALARS_U8, idx)
+    idd = O.decode(SCALARS_U8, ib, 2048, 2048).astype(np.float32)
     ix, iy = O.palette_index(bg.shape[1], bg.shape[0], idd[..., 1], idd[..., 0])
     return rgba_bytes(bg[iy, ix])
 

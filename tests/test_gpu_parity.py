@@ -178,8 +178,7 @@ def test_generic_palette(background, goldens, mode):
     # linked; the 2048^2 output is a byte-exact gather of the oracle's indices.
     ours = P.ours_generic(background, mode)
     assert (ours == P.oracle_generic(background)).all()
-    h = blockhash256(ours.reshape(2048, 2048, 4))
-    assert min(bin(int(h, 16) ^ int(g, 16)).count("1") for g in goldens["generic"]) <= 8
+    assert blockhash256(ours.reshape(2048, 2048, 4)) in goldens["generic"]
 
 
 def test_linked_instantiations_equal_flat_program():
