@@ -568,7 +568,7 @@ def workload_thumbnails(args, stream, sh):
     _line("thumbnails 1024 uneven RGBA8 -> colour chain -> box fit 256 -> centred 256^2", src_px,
           src_px * 4 + 1024 * 256 * 256 * 4, ms, per["plain_fp32"][0], clocks,
           {"images": 1024, "source_gpx": round(src_px / 1e9, 3), "launches_per_batch": 1,
-           "autotune": {"rows_per_item": rows}, "graph": "memset + kernel captured once, replayed per batch",
+           "autotune": {"rows_per_item": rows, "threads_per_block": exe.get_launch(zs.Tune.BatchThreads)}, "graph": "memset + kernel captured once, replayed per batch",
            "parity": parity,
            "plain": "one per-op FP32 program per image", "plain_launches": per["plain_fp32"][1],
            "per_image_fused_ms": round(per["fused"][0], 4), "per_image_fused_launches": per["fused"][1],

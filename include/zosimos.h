@@ -455,7 +455,9 @@ int zs_resample_rgba16f_noalloc(const void *src, uint32_t src_width, uint32_t sr
  *      parameters) ---- */
 enum {
     ZS_TUNE_CHAIN_THREADS = 0,   /* colour-chain kernel block size: 1024 (one block per SM) or 512 */
-    ZS_TUNE_BATCH_ROWS = 1       /* batched thumbnails: output rows per work item, 1..16 */
+    ZS_TUNE_BATCH_ROWS = 1,      /* batched thumbnails: work-item height, 1..16 (about 16 x value
+                                    source rows per item; value output rows for upscaled images) */
+    ZS_TUNE_BATCH_THREADS = 2    /* batched thumbnails: block size, 768 or 640 (one block per SM) */
 };
 /* Times the candidates of every tunable launch of `exe` (CUDA events, median of `reps`
  * launches each) on the given device buffers -- which receive the result -- and keeps the
@@ -464,14 +466,15 @@ enum {
  * start from the cached value.  Every candidate computes the same bytes. */
 int zs_autotune(zs_executable *exe, const void *const *inputs, uint32_t n_inputs, void *const *outputs,
                 uint32_t n_outputs, void *stream, uint32_t reps, int32_t *chain_threads);
-/* The same for the rows per work item of zs_batch_thumbnails on this batch. */
+/* The same for the work-item height and block size of zs_batch_thumbnails on this batch;
+ * returns the height (the block size is read with zs_executable_get_launch). */
 int zs_autotune_batch_thumbnails(zs_executable *chain, const void *const *images, const uint32_t *widths,
                                  const uint32_t *heights, uint32_t n, uint32_t canvas, void *out, void *stream,
                                  uint32_t reps, uint32_t *rows);
 /* Sets / reads a launch parameter (ZS_TUNE_*) of an executable directly. */
 int zs_executable_set_launch(zs_executable *exe, uint32_t param, int32_t value);
 int zs_executable_get_launch(const zs_executable *exe, uint32_t param, int32_t *value);
-/* The tuning-cache key a parameter of this executable uses (canvas: for ZS_TUNE_BATCH_ROWS). */
+/* The tuning-cache key a parameter of this executable uses (canvas: for the ZS_TUNE_BATCH_*). */
 int zs_executable_tune_key(const zs_executable *exe, uint32_t param, uint32_t canvas, char *buf, uint64_t len);
 /* The process-wide tuning cache: read / write one value, save to / merge from a text file
  * ("key value" lines).  zs_tune_cache_get fails with ZS_ERR_MISSING_KEY for an unknown key. */

@@ -707,17 +707,19 @@ def test_autotune_candidates_are_byte_identical():
     args = ([b.ptr for b in bufs], [im.shape[1] for im in images], [im.shape[0] for im in images], 256, out.ptr)
     ref = P.oracle_thumbnails(images, 256)
     results = []
-    for rows in (1, 2, 4, 8, 16, 2):
+    for threads, rows in [(t, r) for t in (768, 640) for r in (1, 2, 4, 8, 16)] + [(768, 2)]:
+        chain.set_launch(zs.Tune.BatchThreads, threads)
         chain.set_launch(zs.Tune.BatchRows, rows)
         chain.batch_thumbnails(*args)
         zs.device_synchronize()
         got = out.download(np.empty((40, 256, 1024), np.uint8))
         for k in range(40):
-            assert maxdiff(got[k], ref[k]) <= LSB, (rows, k)
+            assert maxdiff(got[k], ref[k]) <= LSB, (threads, rows, k)
         results.append(got)
     assert all((r == results[0]).all() for r in results[1:])
     rows = chain.autotune_batch_thumbnails(*args, reps=2)
     assert rows in (1, 2, 4, 8, 16) and chain.get_launch(zs.Tune.BatchRows) == rows
+    assert chain.get_launch(zs.Tune.BatchThreads) in (768, 640)
     chain.batch_thumbnails(*args)
     zs.device_synchronize()
     assert (out.download(np.empty((40, 256, 1024), np.uint8)) == results[0]).all()

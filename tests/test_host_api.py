@@ -317,6 +317,12 @@ def test_tuning_cache_and_keys(tmp_path):
     with pytest.raises(ZosimosError) as e:
         exe.set_launch(zs.Tune.BatchRows, 17)
     assert e.value.code == 10
+    assert exe.tune_key(zs.Tune.BatchThreads, 256).startswith("batch_threads/flags")
+    exe.set_launch(zs.Tune.BatchThreads, 640)
+    assert exe.get_launch(zs.Tune.BatchThreads) == 640
+    with pytest.raises(ZosimosError) as e:
+        exe.set_launch(zs.Tune.BatchThreads, 1024)
+    assert e.value.code == 10
     # the process-wide cache: values, a file round trip, and misses
     zs.tune_cache_put("test/a/b", 7)
     zs.tune_cache_put("test/c", 16)

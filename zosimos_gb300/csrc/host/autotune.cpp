@@ -5,8 +5,10 @@
 //
 // Tunables (every candidate runs the same arithmetic per pixel, so results are byte-identical):
 //  * the colour-chain kernel's block size: 1024 threads (one block per SM) or 512 (two);
-//  * the batched-thumbnail kernel's output rows per work item: 1, 2, 4, 8 or 16 (taller items
-//    reuse more source rows between output rows; shorter ones balance the warps better).
+//  * the batched-thumbnail kernel's work-item height, 1, 2, 4, 8 or 16 (a streaming item covers
+//    about 16 x that many source rows: taller items share fewer boundary rows between items,
+//    shorter ones balance the warps better), and its block size, 768 or 640 threads (one block
+//    per SM either way: 24 warps with a few registers spilled, or 20 warps without).
 //
 // The reference has no autotuner (its render passes have no launch parameters).
 #include <algorithm>
@@ -92,12 +94,12 @@ std::string chain_tune_key(const Step &st, int device) {
     return os.str();
 }
 
-std::string batch_tune_key(const Executable &E, uint32_t canvas, int device) {
+std::string batch_tune_key(const Executable &E, uint32_t canvas, int device, const char *family) {
     int flags = 0;
     for (const Step &st : E.steps)
         if (st.kind == StepKind::Chain) flags = st.chain.flags;
     std::ostringstream os;
-    os << "batch/flags" << flags << "/canvas" << canvas << '/' << device_key(device);
+    os << family << "/flags" << flags << "/canvas" << canvas << '/' << device_key(device);
     return os.str();
 }
 
@@ -170,38 +172,46 @@ int autotune_batch(Executable *chain, const void *const *images, const uint32_t 
     cudaEvent_t e0, e1;
     check_cuda(cudaEventCreate(&e0), "event");
     check_cuda(cudaEventCreate(&e1), "event");
-    int best = 0;
+    int best = 0, best_threads = 0;
     float best_ms = 0.f;
     int rc = ZS_OK;
-    for (int cand : {1, 2, 4, 8, 16}) {
-        chain->batch_rows = cand;
-        std::vector<float> ms;
-        for (uint32_t r = 0; r <= reps && rc == ZS_OK; ++r) {
-            cudaEventRecord(e0, s);
-            rc = batch_thumbnails(chain, images, widths, heights, n, canvas, out, s);
-            cudaEventRecord(e1, s);
+    for (int threads : {768, 640}) {
+        for (int cand : {1, 2, 4, 8, 16}) {
+            chain->batch_threads = threads;
+            chain->batch_rows = cand;
+            std::vector<float> ms;
+            for (uint32_t r = 0; r <= reps && rc == ZS_OK; ++r) {
+                cudaEventRecord(e0, s);
+                rc = batch_thumbnails(chain, images, widths, heights, n, canvas, out, s);
+                cudaEventRecord(e1, s);
+                if (rc != ZS_OK) break;
+                check_cuda(cudaEventSynchronize(e1), "synchronize");
+                float t = 0.f;
+                check_cuda(cudaEventElapsedTime(&t, e0, e1), "elapsed");
+                if (r > 0) ms.push_back(t);      // the first batch of a candidate captures its graph
+            }
             if (rc != ZS_OK) break;
-            check_cuda(cudaEventSynchronize(e1), "synchronize");
-            float t = 0.f;
-            check_cuda(cudaEventElapsedTime(&t, e0, e1), "elapsed");
-            if (r > 0) ms.push_back(t);      // the first batch of a candidate captures its graph
+            std::nth_element(ms.begin(), ms.begin() + ms.size() / 2, ms.end());
+            const float t = ms[ms.size() / 2];
+            if (!best || t < best_ms) {
+                best = cand;
+                best_threads = threads;
+                best_ms = t;
+            }
         }
         if (rc != ZS_OK) break;
-        std::nth_element(ms.begin(), ms.begin() + ms.size() / 2, ms.end());
-        const float t = ms[ms.size() / 2];
-        if (!best || t < best_ms) {
-            best = cand;
-            best_ms = t;
-        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc != ZS_OK) {
         chain->batch_rows = 0;
+        chain->batch_threads = 0;
         fail(rc, "autotune of the batched thumbnails: " + last_error());
     }
     chain->batch_rows = best;
+    chain->batch_threads = best_threads;
     tune_put(batch_tune_key(*chain, canvas, chain->device), best);
+    tune_put(batch_tune_key(*chain, canvas, chain->device, "batch_threads"), best_threads);
     return best;
 }
 

@@ -1298,6 +1298,9 @@ int zs_executable_set_launch(zs_executable *exe, uint32_t param, int32_t value) 
         } else if (param == ZS_TUNE_BATCH_ROWS) {
             if (value < 1 || value > 16) fail(ZS_ERR_INVALID_ARG, "rows per batch item must be in 1..16");
             E.batch_rows = value;
+        } else if (param == ZS_TUNE_BATCH_THREADS) {
+            if (value != 768 && value != 640) fail(ZS_ERR_INVALID_ARG, "batch block size must be 768 or 640");
+            E.batch_threads = value;
         } else {
             fail(ZS_ERR_INVALID_ARG, "unknown launch parameter");
         }
@@ -1314,6 +1317,8 @@ int zs_executable_get_launch(const zs_executable *exe, uint32_t param, int32_t *
                 if (st.kind == StepKind::Chain) *value = st.tune_threads ? st.tune_threads : 1024;
         } else if (param == ZS_TUNE_BATCH_ROWS) {
             *value = E.batch_rows;
+        } else if (param == ZS_TUNE_BATCH_THREADS) {
+            *value = E.batch_threads;
         } else {
             fail(ZS_ERR_INVALID_ARG, "unknown launch parameter");
         }
@@ -1336,6 +1341,8 @@ int zs_executable_tune_key(const zs_executable *exe, uint32_t param, uint32_t ca
             fail(ZS_ERR_UNIMPLEMENTED, "the executable has no chain step");
         } else if (param == ZS_TUNE_BATCH_ROWS) {
             copy_string(batch_tune_key(E, canvas, E.device), buf, len);
+        } else if (param == ZS_TUNE_BATCH_THREADS) {
+            copy_string(batch_tune_key(E, canvas, E.device, "batch_threads"), buf, len);
         } else {
             fail(ZS_ERR_INVALID_ARG, "unknown launch parameter");
         }

@@ -260,7 +260,8 @@ struct Executable {
     cudaEvent_t batch_done = nullptr;
     cudaGraphExec_t batch_graph = nullptr;
     std::vector<uint64_t> batch_key;
-    int batch_rows = 0;                                // output rows per batch work item (0: tuned or default)
+    int batch_rows = 0;                                // batch work-item height (0: tuned or default)
+    int batch_threads = 0;                             // batch kernel block size (0: tuned or default)
     std::string plan_text;
     std::vector<KnobInfo> knobs;                      // Executable::query_knob
     // CUDA graphs of the launch sequence for zs_run_device, keyed by the bound pointers
@@ -302,7 +303,8 @@ void tune_save(const std::string &path);
 void tune_load(const std::string &path);
 std::string device_key(int device);
 std::string chain_tune_key(const Step &st, int device);
-std::string batch_tune_key(const Executable &E, uint32_t canvas, int device);
+// `family`: "batch" (work-item height) or "batch_threads" (block size).
+std::string batch_tune_key(const Executable &E, uint32_t canvas, int device, const char *family = "batch");
 // Tuned values of the executable's steps from the process-wide cache.
 void apply_tuned(Executable &E);
 // Times the candidates of every tunable step on these buffers and keeps the fastest.

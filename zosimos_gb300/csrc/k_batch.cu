@@ -6,22 +6,29 @@
 // M_a, [cbrt], M_b, [cube], M_c, [clamp], M_d, linear result) -> box (area coverage)
 // fit-resize so the long side is `canvas` -> centred inscribe on a transparent
 // canvas x canvas image -> exact sRGB8 encode.  The canvases are zero-filled (the
-// transparent margins) by one memset; the fitted pixels are cut into work items of 32
-// output columns x `rows` output rows (1..16, chosen by the autotuner), one item per warp,
-// taken by static striding
-// over all images (no atomics, no barriers), so that every image's cost spreads over all warps.
+// transparent margins) by one memset; the fitted pixels are cut into work items, one item per
+// warp, taken by static striding over all images (no atomics, no block barriers), so that
+// every image's cost spreads over all warps.
 //
-// The colour chain is nonlinear, so it runs on every source texel before the box filter;
-// the kernel is built so that each texel goes through it once:
-//  * lane l owns output column u; its box window covers texels [j0, j1) of a source row, with
-//    weight 1 inside and fractional weights only at the two ends;
-//  * on a downscale the windows tile the row, so the last texel of lane l is the first texel
-//    of lane l + 1: lane l + 1 computes it and hands its unweighted value over with a warp
-//    shuffle, lane l applies its own edge weight;
-//  * consecutive output rows share one source row: the horizontal sums of the last row of an
-//    output row are kept in registers and reused by the next one;
-//  * texels go through the chain two at a time in FP32x2 registers (decode from the
-//    lane-replicated shared table, MUFU cube roots, the rank-1 Oklab L/C form when planned).
+// The colour chain is nonlinear, so it runs on every source texel before the box filter.
+// Downscaled images (both scale factors >= 1, the bulk of the work) use streaming items that
+// put each texel through the chain exactly once, reading source rows coalesced:
+//  * an item is a band of output rows x a run of output columns whose box windows span at most
+//    128 source columns; lane l owns source columns c0 + l + 32 k, k = 0..3, so every row load
+//    of the warp is 128 contiguous bytes;
+//  * the warp walks the band's source rows top to bottom, texels go through the chain two
+//    at a time in FP32x2 registers (decode from the lane-replicated shared table, MUFU cube
+//    roots, the rank-1 Oklab L/C form when planned), and each lane keeps the vertical box sums
+//    of its four columns in registers; the next row's loads are issued before this row's
+//    arithmetic;
+//  * when the last row of an output row's window has been added, the column sums go to the
+//    warp's 2 KiB slice of shared memory and the lanes owning output columns apply the
+//    horizontal box weights, normalise, encode and store; a boundary row shared with the next
+//    output row seeds the next sums with its own weight.
+// Upscaled images (few texels) use per-output items: lane l owns one output column of 32 and
+// walks its 2 x 2 (or wider) window directly.
+#include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -30,8 +37,8 @@
 #include "zs_device.cuh"
 #include "zs_kernels.h"
 
-#define ZS_BATCH_THREADS 256
-#define ZS_BATCH_ROWS_DEFAULT 1   // output rows per work item until the autotuner chose
+#define ZS_BATCH_SPAN 128         // source columns of a streaming item: 4 per lane
+#define ZS_BATCH_ROWS_DEFAULT 4   // work-item height until the autotuner chose (see batch_thumbnails)
 
 struct ZsBatchImage {
     const uint8_t *ptr;
@@ -40,6 +47,10 @@ struct ZsBatchImage {
     int32_t x0, y0;            // placement on the canvas
     float sx, sy;              // source pixels per fitted pixel
     float fx, fy;              // filter widths: max(sx, 1), max(sy, 1)
+    int32_t stream;            // 1: streaming items, 0: per-output items
+    int32_t kx;                // output columns per item
+    int32_t chunks;            // items across the fitted width
+    int32_t ry;                // output rows per item
 };
 
 struct ZsBatchArgs {
@@ -49,7 +60,7 @@ struct ZsBatchArgs {
     int32_t n;
     int32_t canvas;
     int32_t flags;
-    int32_t rows;              // output rows per work item
+    int32_t pad;
     float m2[4][9][2];         // the chain's matrices with every coefficient duplicated (f32x2 operands)
     float mb_v[3][2];          // ZS_CHAIN_MB_RANK1: M_b = d I + (1,1,1)^T v
     float mb_d[2];
@@ -104,51 +115,184 @@ __device__ __forceinline__ void zs_box_window(int u, float s, float f, int len, 
     j1 = min((int)ceilf(hi), len);
 }
 
-// This lane's horizontally weighted sum of one source row (colour in xyz, alpha code sum in
-// w): texels [j0, jend) through the chain, weight wfirst at j0, wlast at j1 - 1, 1 between;
-// when `share`, texel j1 - 1 is the next lane's first texel and arrives by shuffle.  Every
-// lane of the warp calls this together (the shuffles use the full mask).
-template <bool NONNEG, bool RANK1>
-__device__ __forceinline__ float4 zs_batch_row(const uint32_t *row, int j0, int jend, int j1, float wfirst, float wlast,
-                                               bool share, const unsigned char *lut, uint32_t lane4,
-                                               const ZsBatchArgs &a) {
-    float2 sr = make_float2(0.f, 0.f), sg = sr, sb = sr, sa = sr;
-    float4 first = make_float4(0.f, 0.f, 0.f, 0.f);
-    for (int jx = j0; jx < jend; jx += 2) {
-        const bool two = jx + 1 < jend;
-        const uint32_t w0 = __ldg(row + jx), w1 = two ? __ldg(row + jx + 1) : w0;
-        float2 r, g, b;
-        zs_batch_chain2<NONNEG, RANK1>(w0, w1, lut, lane4, a, r, g, b);
-        const float2 al = make_float2(__uint2float_rn(w0 >> 24), __uint2float_rn(w1 >> 24));
-        if (jx == j0) first = make_float4(r.x, g.x, b.x, al.x);
-        const float2 wx = make_float2(jx == j0 ? wfirst : (jx == j1 - 1 ? wlast : 1.f),
-                                      two ? (jx + 1 == j1 - 1 ? wlast : 1.f) : 0.f);
-        sr = __ffma2_rn(wx, r, sr);
-        sg = __ffma2_rn(wx, g, sg);
-        sb = __ffma2_rn(wx, b, sb);
-        sa = __ffma2_rn(wx, al, sa);
-    }
-    float4 rs = make_float4(sr.x + sr.y, sg.x + sg.y, sb.x + sb.y, sa.x + sa.y);
-    const float nr = __shfl_down_sync(0xffffffffu, first.x, 1), ng = __shfl_down_sync(0xffffffffu, first.y, 1);
-    const float nb = __shfl_down_sync(0xffffffffu, first.z, 1), na = __shfl_down_sync(0xffffffffu, first.w, 1);
-    if (share) {
-        rs.x = fmaf(wlast, nr, rs.x);
-        rs.y = fmaf(wlast, ng, rs.y);
-        rs.z = fmaf(wlast, nb, rs.z);
-        rs.w = fmaf(wlast, na, rs.w);
-    }
-    return rs;
+// Coverage of texel j by the window [lo, hi).
+__device__ __forceinline__ float zs_cover(float lo, float hi, int j) {
+    return fmaxf(fminf(hi, (float)j + 1.f) - fmaxf(lo, (float)j), 0.f);
 }
 
+__device__ __forceinline__ uint32_t zs_batch_encode(float4 acc, float inv) {
+    return zs_enc_srgb8(zs_srgb_encode_tab, acc.x * inv) | (zs_enc_srgb8(zs_srgb_encode_tab, acc.y * inv) << 8) |
+           (zs_enc_srgb8(zs_srgb_encode_tab, acc.z * inv) << 16) | (zs_unorm8(acc.w * inv * (1.0f / 255.0f)) << 24);
+}
+
+// A streaming item: output rows [v0, v1) x output columns [u0, u1) of image I.
 template <bool NONNEG, bool RANK1>
-__global__ void __launch_bounds__(ZS_BATCH_THREADS, 3) zs_batch_kernel(const __grid_constant__ ZsBatchArgs a) {
-    extern __shared__ __align__(16) float zs_batch_lut[];      // [code][64], lanes 32..63 unused
+__device__ __forceinline__ void zs_batch_stream(const ZsBatchImage &I, int band, int chunk, float4 *hb,
+                                                const unsigned char *lut, uint32_t lane4, int lane,
+                                                const ZsBatchArgs &a, uint32_t *out) {
+    const int u0 = chunk * I.kx, u1 = min(u0 + I.kx, I.tw);
+    int xs, xe, t0, t1;
+    float tlo, thi;
+    zs_box_window(u0, I.sx, I.fx, I.width, xs, t1, tlo, thi);
+    zs_box_window(u1 - 1, I.sx, I.fx, I.width, t0, xe, tlo, thi);
+    xe = min(xe, xs + ZS_BATCH_SPAN);
+    const int v0 = band * I.ry, v1 = min(v0 + I.ry, I.th);
+    int jy0, jy1, ye;
+    float loy, hiy;
+    zs_box_window(v1 - 1, I.sy, I.fy, I.height, t0, ye, tlo, thi);
+    zs_box_window(v0, I.sy, I.fy, I.height, jy0, jy1, loy, hiy);
+    const uint32_t *img = reinterpret_cast<const uint32_t *>(I.ptr);
+    const int c0 = xs + lane;
+    const bool in0 = c0 < xe, in1 = c0 + 32 < xe, in2 = c0 + 64 < xe, in3 = c0 + 96 < xe;
+    // Column sums: pair 0 = columns (c0, c0 + 32), pair 1 = (c0 + 64, c0 + 96).
+    float2 sr0 = make_float2(0.f, 0.f), sg0 = sr0, sb0 = sr0, sa0 = sr0, sr1 = sr0, sg1 = sr0, sb1 = sr0, sa1 = sr0;
+    int v = v0;
+    int y = jy0;
+    const uint32_t *row = img + (size_t)y * I.width + c0;   // this lane's first column of row y
+    uint32_t w0 = in0 ? __ldg(row) : 0u, w1 = in1 ? __ldg(row + 32) : 0u;
+    uint32_t w2 = in2 ? __ldg(row + 64) : 0u, w3 = in3 ? __ldg(row + 96) : 0u;
+    // The band ends when its last output row is stored (ye, the end of that row's window,
+    // only bounds the prefetch); y stays inside the image.
+    for (;;) {
+        // Next row's texels in flight during this row's arithmetic.
+        uint32_t n0 = 0u, n1 = 0u, n2 = 0u, n3 = 0u;
+        const bool ahead = y + 1 < ye && y + 1 < I.height;
+        if (ahead) {
+            const uint32_t *nrow = row + I.width;
+            n0 = in0 ? __ldg(nrow) : 0u;
+            n1 = in1 ? __ldg(nrow + 32) : 0u;
+            n2 = in2 ? __ldg(nrow + 64) : 0u;
+            n3 = in3 ? __ldg(nrow + 96) : 0u;
+        }
+        float2 r0, g0, b0, r1, g1, b1;
+        zs_batch_chain2<NONNEG, RANK1>(w0, w1, lut, lane4, a, r0, g0, b0);
+        zs_batch_chain2<NONNEG, RANK1>(w2, w3, lut, lane4, a, r1, g1, b1);
+        const float2 al0 = make_float2(__uint2float_rn(w0 >> 24), __uint2float_rn(w1 >> 24));
+        const float2 al1 = make_float2(__uint2float_rn(w2 >> 24), __uint2float_rn(w3 >> 24));
+        const float wy = zs_cover(loy, hiy, y);
+        const float2 wy2 = make_float2(wy, wy);
+        sr0 = __ffma2_rn(wy2, r0, sr0);
+        sg0 = __ffma2_rn(wy2, g0, sg0);
+        sb0 = __ffma2_rn(wy2, b0, sb0);
+        sa0 = __ffma2_rn(wy2, al0, sa0);
+        sr1 = __ffma2_rn(wy2, r1, sr1);
+        sg1 = __ffma2_rn(wy2, g1, sg1);
+        sb1 = __ffma2_rn(wy2, b1, sb1);
+        sa1 = __ffma2_rn(wy2, al1, sa1);
+        // Output rows whose window ends with this row (uniform across the warp).
+        while (y == jy1 - 1 && v < v1) {
+            hb[lane] = make_float4(sr0.x, sg0.x, sb0.x, sa0.x);
+            hb[lane + 32] = make_float4(sr0.y, sg0.y, sb0.y, sa0.y);
+            hb[lane + 64] = make_float4(sr1.x, sg1.x, sb1.x, sa1.x);
+            hb[lane + 96] = make_float4(sr1.y, sg1.y, sb1.y, sa1.y);
+            const int vd = v, dy0 = jy0, dy1 = jy1;
+            const float dlo = loy, dhi = hiy;
+            // The next output row starts with this row's share of it.
+            ++v;
+            float wn = 0.f;
+            if (v < v1) {
+                zs_box_window(v, I.sy, I.fy, I.height, jy0, jy1, loy, hiy);
+                wn = zs_cover(loy, hiy, y);
+            }
+            const float2 wn2 = make_float2(wn, wn);
+            sr0 = __fmul2_rn(wn2, r0);
+            sg0 = __fmul2_rn(wn2, g0);
+            sb0 = __fmul2_rn(wn2, b0);
+            sa0 = __fmul2_rn(wn2, al0);
+            sr1 = __fmul2_rn(wn2, r1);
+            sg1 = __fmul2_rn(wn2, g1);
+            sb1 = __fmul2_rn(wn2, b1);
+            sa1 = __fmul2_rn(wn2, al1);
+            __syncwarp();
+            for (int k = lane; k < u1 - u0; k += 32) {
+                const int u = u0 + k;
+                int jx0, jx1;
+                float lox, hix;
+                zs_box_window(u, I.sx, I.fx, I.width, jx0, jx1, lox, hix);
+                const float wxsum = fmaxf(fminf(hix, (float)jx1) - fmaxf(lox, (float)jx0), 0.f);
+                jx0 = max(jx0, xs);
+                jx1 = min(jx1, xe);
+                float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+                for (int j = jx0; j < jx1; ++j) {
+                    const float wx = zs_cover(lox, hix, j);
+                    const float4 c = hb[j - xs];
+                    acc.x = fmaf(wx, c.x, acc.x);
+                    acc.y = fmaf(wx, c.y, acc.y);
+                    acc.z = fmaf(wx, c.z, acc.z);
+                    acc.w = fmaf(wx, c.w, acc.w);
+                }
+                const float wsum = wxsum * fmaxf(fminf(dhi, (float)dy1) - fmaxf(dlo, (float)dy0), 0.f);
+                out[(size_t)(I.y0 + vd) * a.canvas + I.x0 + u] = zs_batch_encode(acc, wsum > 0.f ? 1.0f / wsum : 0.f);
+            }
+            __syncwarp();
+        }
+        if (v >= v1 || y + 1 >= I.height) break;
+        ++y;
+        row += I.width;
+        if (!ahead) {
+            n0 = in0 ? __ldg(row) : 0u;
+            n1 = in1 ? __ldg(row + 32) : 0u;
+            n2 = in2 ? __ldg(row + 64) : 0u;
+            n3 = in3 ? __ldg(row + 96) : 0u;
+        }
+        w0 = n0;
+        w1 = n1;
+        w2 = n2;
+        w3 = n3;
+    }
+}
+
+// A per-output item (upscaled images): lane l owns output column u of 32, rows [v0, v1).
+template <bool NONNEG, bool RANK1>
+__device__ __forceinline__ void zs_batch_direct(const ZsBatchImage &I, int band, int chunk, const unsigned char *lut,
+                                                uint32_t lane4, int lane, const ZsBatchArgs &a, uint32_t *out) {
+    const int u = chunk * I.kx + lane;
+    if (u >= I.tw) return;
+    int jx0, jx1;
+    float lox, hix;
+    zs_box_window(u, I.sx, I.fx, I.width, jx0, jx1, lox, hix);
+    const float wxsum = fmaxf(fminf(hix, (float)jx1) - fmaxf(lox, (float)jx0), 0.f);
+    const uint32_t *img = reinterpret_cast<const uint32_t *>(I.ptr);
+    const int v0 = band * I.ry, v1 = min(v0 + I.ry, I.th);
+    for (int v = v0; v < v1; ++v) {
+        int jy0, jy1;
+        float loy, hiy;
+        zs_box_window(v, I.sy, I.fy, I.height, jy0, jy1, loy, hiy);
+        float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int jy = jy0; jy < jy1; ++jy) {
+            const float wy = zs_cover(loy, hiy, jy);
+            const uint32_t *row = img + (size_t)jy * I.width;
+            for (int jx = jx0; jx < jx1; jx += 2) {
+                const bool two = jx + 1 < jx1;
+                const uint32_t t0 = __ldg(row + jx), t1 = two ? __ldg(row + jx + 1) : t0;
+                float2 r, g, b;
+                zs_batch_chain2<NONNEG, RANK1>(t0, t1, lut, lane4, a, r, g, b);
+                const float wa = wy * zs_cover(lox, hix, jx), wb = two ? wy * zs_cover(lox, hix, jx + 1) : 0.f;
+                acc.x = fmaf(wb, r.y, fmaf(wa, r.x, acc.x));
+                acc.y = fmaf(wb, g.y, fmaf(wa, g.x, acc.y));
+                acc.z = fmaf(wb, b.y, fmaf(wa, b.x, acc.z));
+                acc.w = fmaf(wb, __uint2float_rn(t1 >> 24), fmaf(wa, __uint2float_rn(t0 >> 24), acc.w));
+            }
+        }
+        const float wsum = wxsum * fmaxf(fminf(hiy, (float)jy1) - fmaxf(loy, (float)jy0), 0.f);
+        out[(size_t)(I.y0 + v) * a.canvas + I.x0 + u] = zs_batch_encode(acc, wsum > 0.f ? 1.0f / wsum : 0.f);
+    }
+}
+
+// One block per SM (the 64 KiB decode table once per SM); THREADS is 768 or 640 (autotuned:
+// 24 warps with a few spilled registers or 20 warps without).
+template <int THREADS, bool NONNEG, bool RANK1>
+__global__ void __launch_bounds__(THREADS, 1) zs_batch_kernel(const __grid_constant__ ZsBatchArgs a) {
+    // [0, 64 KiB): decode table, [code][64] floats (lanes 32..63 unused);
+    // then one 128-column slice of float4 column sums per warp.
+    extern __shared__ __align__(16) float zs_batch_smem[];
     for (int i = threadIdx.x; i < 256 * 8; i += blockDim.x) {
         const float d = zs_srgb_decode_lut[i >> 3];
-        reinterpret_cast<float4 *>(zs_batch_lut)[(i >> 3) * 16 + (i & 7)] = make_float4(d, d, d, d);
+        reinterpret_cast<float4 *>(zs_batch_smem)[(i >> 3) * 16 + (i & 7)] = make_float4(d, d, d, d);
     }
     __syncthreads();
-    const unsigned char *lut = reinterpret_cast<const unsigned char *>(zs_batch_lut);
+    const unsigned char *lut = reinterpret_cast<const unsigned char *>(zs_batch_smem);
+    float4 *hb = reinterpret_cast<float4 *>(zs_batch_smem + 256 * 64) + (threadIdx.x >> 5) * ZS_BATCH_SPAN;
     const int lane = threadIdx.x & 31;
     const uint32_t lane4 = (uint32_t)lane << 2;
     const int warps = (int)(gridDim.x * (blockDim.x >> 5));
@@ -157,52 +301,11 @@ __global__ void __launch_bounds__(ZS_BATCH_THREADS, 3) zs_batch_kernel(const __g
     for (int it = (int)(blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)); it < total; it += warps) {
         while (a.prefix[img + 1] <= it) ++img;
         const ZsBatchImage I = a.images[img];
-        const int strips = (I.tw + 31) >> 5, local = it - a.prefix[img];
-        const int band = local / strips, u = (local - band * strips) * 32 + lane;
-        const bool valid = u < I.tw;
-        // Horizontal window of this lane (none for lanes past the fitted width).
-        int jx0 = 0, jx1 = 0;
-        float lox = 0.f, hix = 0.f;
-        if (valid) zs_box_window(u, I.sx, I.fx, I.width, jx0, jx1, lox, hix);
-        const int next_j0 = __shfl_down_sync(0xffffffffu, jx0, 1);
-        const int next_valid = __shfl_down_sync(0xffffffffu, valid ? 1 : 0, 1);
-        const bool share = I.sx >= 1.f && lane < 31 && valid && next_valid && next_j0 == jx1 - 1 && jx1 - 1 > jx0;
-        const int jend = share ? jx1 - 1 : jx1;
-        const float wfirst = fmaxf(fminf(hix, (float)jx0 + 1.f) - fmaxf(lox, (float)jx0), 0.f);
-        const float wlast = fmaxf(fminf(hix, (float)jx1) - fmaxf(lox, (float)jx1 - 1.f), 0.f);
-        const float wxsum = fmaxf(fminf(hix, (float)jx1) - fmaxf(lox, (float)jx0), 0.f);
+        const int local = it - a.prefix[img];
+        const int band = local / I.chunks, chunk = local - band * I.chunks;
         uint32_t *out = reinterpret_cast<uint32_t *>(a.out + (size_t)img * a.canvas * a.canvas * 4);
-        const int v0 = band * a.rows, v1 = min(v0 + a.rows, I.th);
-        int carry_row = -1;
-        float4 carry = make_float4(0.f, 0.f, 0.f, 0.f);
-        for (int v = v0; v < v1; ++v) {
-            int jy0, jy1;
-            float loy, hiy;
-            zs_box_window(v, I.sy, I.fy, I.height, jy0, jy1, loy, hiy);
-            float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-            for (int jy = jy0; jy < jy1; ++jy) {
-                const float wy = fmaxf(fminf(hiy, (float)jy + 1.f) - fmaxf(loy, (float)jy), 0.f);
-                float4 rs = carry;
-                if (jy != carry_row) {     // uniform across the warp
-                    const uint32_t *row = reinterpret_cast<const uint32_t *>(I.ptr + (size_t)jy * I.width * 4);
-                    rs = zs_batch_row<NONNEG, RANK1>(row, jx0, jend, jx1, wfirst, wlast, share, lut, lane4, a);
-                    carry_row = jy;
-                    carry = rs;
-                }
-                acc.x = fmaf(wy, rs.x, acc.x);
-                acc.y = fmaf(wy, rs.y, acc.y);
-                acc.z = fmaf(wy, rs.z, acc.z);
-                acc.w = fmaf(wy, rs.w, acc.w);
-            }
-            if (!valid) continue;
-            const float wsum = wxsum * fmaxf(fminf(hiy, (float)jy1) - fmaxf(loy, (float)jy0), 0.f);
-            const float inv = wsum > 0.f ? 1.0f / wsum : 0.f;
-            const uint32_t code = zs_enc_srgb8(zs_srgb_encode_tab, acc.x * inv) |
-                                  (zs_enc_srgb8(zs_srgb_encode_tab, acc.y * inv) << 8) |
-                                  (zs_enc_srgb8(zs_srgb_encode_tab, acc.z * inv) << 16) |
-                                  (zs_unorm8(acc.w * inv * (1.0f / 255.0f)) << 24);
-            out[(size_t)(I.y0 + v) * a.canvas + I.x0 + u] = code;
-        }
+        if (I.stream) zs_batch_stream<NONNEG, RANK1>(I, band, chunk, hb, lut, lane4, lane, a, out);
+        else zs_batch_direct<NONNEG, RANK1>(I, band, chunk, lut, lane4, lane, a, out);
     }
 }
 
@@ -247,8 +350,10 @@ int batch_thumbnails(Executable *chain, const void *const *images, const uint32_
         I.fx = I.sx > 1.f ? I.sx : 1.f;
         I.fy = I.sy > 1.f ? I.sy : 1.f;
     }
-    // Work items: 32 output columns x `rows` output rows (the tuned height for this chain,
-    // canvas and device when the autotuner has seen them).
+    // Work-item height `rows` (the tuned value for this chain, canvas and device when the
+    // autotuner has seen them): a streaming item covers about 16 x rows source rows, a
+    // per-output item `rows` output rows.  Every choice gives the same bytes: each output
+    // pixel's sums run over the same texels in the same order.
     if (chain->batch_rows <= 0) {
         int tuned;
         if (tune_get(batch_tune_key(*chain, canvas, chain->device), tuned) && tuned >= 1 && tuned <= 16)
@@ -257,7 +362,20 @@ int batch_thumbnails(Executable *chain, const void *const *images, const uint32_
     const int rows = chain->batch_rows > 0 ? chain->batch_rows : ZS_BATCH_ROWS_DEFAULT;
     std::vector<int32_t> prefix(n + 1, 0);
     for (uint32_t i = 0; i < n; ++i) {
-        const int64_t items = (int64_t)((host[i].th + rows - 1) / rows) * ((host[i].tw + 31) / 32);
+        ZsBatchImage &I = host[i];
+        // Streaming when both axes shrink and the box windows of at least one output column
+        // fit the 128-column span (2 columns of slack for the window rounding).
+        const int kx = (int)std::floor((ZS_BATCH_SPAN - 4) / (double)I.sx);
+        I.stream = I.sx >= 1.f && I.sy >= 1.f && kx >= 1;
+        if (I.stream) {
+            I.kx = std::min(kx, I.tw);
+            I.ry = std::max(1, (int)std::lround(16.0 * rows / I.sy));
+        } else {
+            I.kx = 32;
+            I.ry = rows;
+        }
+        I.chunks = (I.tw + I.kx - 1) / I.kx;
+        const int64_t items = (int64_t)((I.th + I.ry - 1) / I.ry) * I.chunks;
         if ((int64_t)prefix[i] + items > INT32_MAX) {
             set_last_error("zs_batch_thumbnails: too many output pixels in one batch");
             return ZS_ERR_INVALID_ARG;
@@ -299,23 +417,34 @@ int batch_thumbnails(Executable *chain, const void *const *images, const uint32_
     a.n = (int)n;
     a.canvas = (int)canvas;
     a.flags = cs->chain.flags;
-    a.rows = rows;
     std::memcpy(a.m2, cs->chain.m2, sizeof(a.m2));
     std::memcpy(a.mb_v, cs->chain.mb_v, sizeof(a.mb_v));
     std::memcpy(a.mb_d, cs->chain.mb_d, sizeof(a.mb_d));
     const bool nonneg = (a.flags & ZS_CHAIN_CBRT_NONNEG) || !(a.flags & ZS_CHAIN_CBRT);
     const bool rank1 = (a.flags & ZS_CHAIN_MB_RANK1) != 0;
-    auto kernel = nonneg ? (rank1 ? zs_batch_kernel<true, true> : zs_batch_kernel<true, false>)
-                         : (rank1 ? zs_batch_kernel<false, true> : zs_batch_kernel<false, false>);
-    const size_t smem = 256 * 64 * sizeof(float);
+    if (chain->batch_threads <= 0) {
+        int tuned;
+        if (tune_get(batch_tune_key(*chain, canvas, chain->device, "batch_threads"), tuned) &&
+            (tuned == 768 || tuned == 640))
+            chain->batch_threads = tuned;
+    }
+    const int threads = chain->batch_threads > 0 ? chain->batch_threads : 768;
+    void (*kernel)(ZsBatchArgs);
+    if (threads == 640)
+        kernel = nonneg ? (rank1 ? zs_batch_kernel<640, true, true> : zs_batch_kernel<640, true, false>)
+                        : (rank1 ? zs_batch_kernel<640, false, true> : zs_batch_kernel<640, false, false>);
+    else
+        kernel = nonneg ? (rank1 ? zs_batch_kernel<768, true, true> : zs_batch_kernel<768, true, false>)
+                        : (rank1 ? zs_batch_kernel<768, false, true> : zs_batch_kernel<768, false, false>);
+    const size_t smem = 256 * 64 * sizeof(float) + (size_t)(threads / 32) * ZS_BATCH_SPAN * sizeof(float4);
     e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int per_sm = 0;
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, ZS_BATCH_THREADS, smem);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
     if (e != cudaSuccess) return device_error(e);
     if (per_sm < 1) per_sm = 1;
     // The grid covers every SM: warps stride over the items of all images.
     long long blocks = (long long)chain->sm_count * per_sm;
-    const long long need = ((long long)prefix[n] + ZS_BATCH_THREADS / 32 - 1) / (ZS_BATCH_THREADS / 32);
+    const long long need = ((long long)prefix[n] + threads / 32 - 1) / (threads / 32);
     if (blocks > need) blocks = need;
     if (blocks < 1) blocks = 1;
     // The batch launch (zero the canvases, one kernel) is captured once as a CUDA graph and
@@ -335,7 +464,7 @@ int batch_thumbnails(Executable *chain, const void *const *images, const uint32_
         // Transparent margins: zero every canvas, the kernel writes the fitted pixels.
         cudaError_t ce = cudaMemsetAsync(out, 0, (size_t)n * canvas * canvas * 4, stream);
         if (ce == cudaSuccess) {
-            kernel<<<(unsigned)blocks, ZS_BATCH_THREADS, smem, stream>>>(a);
+            kernel<<<(unsigned)blocks, threads, smem, stream>>>(a);
             ce = cudaGetLastError();
         }
         return ce;
