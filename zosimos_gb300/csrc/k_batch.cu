@@ -66,44 +66,93 @@ struct ZsBatchArgs {
     float mb_d[2];
 };
 
-// The canonical chain on two texels at once, linear result: decode through the
-// lane-replicated shared table, FP32x2 matrix products, MUFU cube roots.
-template <bool NONNEG, bool RANK1>
-__device__ __forceinline__ void zs_batch_chain2(uint32_t w0, uint32_t w1, const unsigned char *lut, uint32_t lane4,
-                                                const ZsBatchArgs &a, float2 &r, float2 &g, float2 &b) {
-    r = make_float2(zs_dec<0>(lut, w0, lane4), zs_dec<0>(lut, w1, lane4));
-    g = make_float2(zs_dec<1>(lut, w0, lane4), zs_dec<1>(lut, w1, lane4));
-    b = make_float2(zs_dec<2>(lut, w0, lane4), zs_dec<2>(lut, w1, lane4));
-    zs_m3x2<false>(a.m2[0], r, g, b);
-    if (a.flags & ZS_CHAIN_CBRT) {
-        if (NONNEG) {
-            zs_cbrt2(r);
-            zs_cbrt2(g);
-            zs_cbrt2(b);
-        } else {
-            r = make_float2(zs_cbrt1<false>(r.x), zs_cbrt1<false>(r.y));
-            g = make_float2(zs_cbrt1<false>(g.x), zs_cbrt1<false>(g.y));
-            b = make_float2(zs_cbrt1<false>(b.x), zs_cbrt1<false>(b.y));
-        }
+// Chain specialisations: LAB = cube root, cube and clamp all present (the Oklab / SrLab2
+// chains), NONNEG and RANK1 as in the chain kernel; GENERIC reads the flags at run time.
+enum { ZS_BATCH_GENERIC = 0, ZS_BATCH_LAB = 1, ZS_BATCH_LAB_NONNEG = 2, ZS_BATCH_LAB_RANK1 = 3,
+       ZS_BATCH_LAB_NONNEG_RANK1 = 4 };
+
+template <int SPEC> struct ZsBatchSpec {
+    static constexpr bool generic = SPEC == ZS_BATCH_GENERIC;
+    static constexpr bool nonneg = SPEC == ZS_BATCH_LAB_NONNEG || SPEC == ZS_BATCH_LAB_NONNEG_RANK1;
+    static constexpr bool rank1 = SPEC == ZS_BATCH_LAB_RANK1 || SPEC == ZS_BATCH_LAB_NONNEG_RANK1;
+};
+
+// rgb' = M rgb on two pixel pairs, every coefficient read once for both.
+template <bool SAT>
+__device__ __forceinline__ void zs_m3x2x2(const float (*m)[2], float2 (&v)[2][3]) {
+    const float2 *c = reinterpret_cast<const float2 *>(m);
+    const float2 x0 = v[0][0], y0 = v[0][1], z0 = v[0][2], x1 = v[1][0], y1 = v[1][1], z1 = v[1][2];
+#pragma unroll
+    for (int row = 0; row < 3; ++row) {
+        v[0][row] = zs_row2<SAT>(c + 3 * row, x0, y0, z0);
+        v[1][row] = zs_row2<SAT>(c + 3 * row, x1, y1, z1);
     }
-    if (RANK1) {
-        const float2 *v = reinterpret_cast<const float2 *>(a.mb_v);
+}
+
+template <bool NONNEG>
+__device__ __forceinline__ void zs_cbrt_pair(float2 &x) {
+    if (NONNEG) zs_cbrt2(x);
+    else x = make_float2(zs_cbrt1<false>(x.x), zs_cbrt1<false>(x.y));
+}
+
+// The canonical chain on four texels (two FP32x2 pairs: (w0, w1) and (w2, w3)), linear
+// result in v[pair][channel]: decode through the lane-replicated shared table, matrix
+// products, MUFU cube roots.
+template <int SPEC>
+__device__ __forceinline__ void zs_batch_chain4(uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3,
+                                                const unsigned char *lut, uint32_t lane4, const ZsBatchArgs &a,
+                                                float2 (&v)[2][3]) {
+    using S = ZsBatchSpec<SPEC>;
+    v[0][0] = make_float2(zs_dec<0>(lut, w0, lane4), zs_dec<0>(lut, w1, lane4));
+    v[0][1] = make_float2(zs_dec<1>(lut, w0, lane4), zs_dec<1>(lut, w1, lane4));
+    v[0][2] = make_float2(zs_dec<2>(lut, w0, lane4), zs_dec<2>(lut, w1, lane4));
+    v[1][0] = make_float2(zs_dec<0>(lut, w2, lane4), zs_dec<0>(lut, w3, lane4));
+    v[1][1] = make_float2(zs_dec<1>(lut, w2, lane4), zs_dec<1>(lut, w3, lane4));
+    v[1][2] = make_float2(zs_dec<2>(lut, w2, lane4), zs_dec<2>(lut, w3, lane4));
+    zs_m3x2x2<false>(a.m2[0], v);
+    const bool cbrt = S::generic ? (a.flags & ZS_CHAIN_CBRT) != 0 : true;
+    if (cbrt) {
+        const bool nonneg = S::generic ? ((a.flags & ZS_CHAIN_CBRT_NONNEG) != 0) : S::nonneg;
+#pragma unroll
+        for (int p = 0; p < 2; ++p)
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) {
+                if (nonneg) zs_cbrt_pair<true>(v[p][ch]);
+                else zs_cbrt_pair<false>(v[p][ch]);
+            }
+    }
+    if (!S::generic && S::rank1) {
+        const float2 *mv = reinterpret_cast<const float2 *>(a.mb_v);
         const float2 d = *reinterpret_cast<const float2 *>(a.mb_d);
-        const float2 t = __ffma2_rn(v[0], r, __ffma2_rn(v[1], g, __fmul2_rn(v[2], b)));
-        r = __ffma2_rn(d, r, t);
-        g = __ffma2_rn(d, g, t);
-        b = __ffma2_rn(d, b, t);
+#pragma unroll
+        for (int p = 0; p < 2; ++p) {
+            const float2 t = __ffma2_rn(mv[0], v[p][0], __ffma2_rn(mv[1], v[p][1], __fmul2_rn(mv[2], v[p][2])));
+            v[p][0] = __ffma2_rn(d, v[p][0], t);
+            v[p][1] = __ffma2_rn(d, v[p][1], t);
+            v[p][2] = __ffma2_rn(d, v[p][2], t);
+        }
     } else {
-        zs_m3x2<false>(a.m2[1], r, g, b);
+        zs_m3x2x2<false>(a.m2[1], v);
     }
-    if (a.flags & ZS_CHAIN_CUBE) {
-        r = __fmul2_rn(__fmul2_rn(r, r), r);
-        g = __fmul2_rn(__fmul2_rn(g, g), g);
-        b = __fmul2_rn(__fmul2_rn(b, b), b);
+    const bool cube = S::generic ? (a.flags & ZS_CHAIN_CUBE) != 0 : true;
+    if (cube) {
+#pragma unroll
+        for (int p = 0; p < 2; ++p)
+#pragma unroll
+            for (int ch = 0; ch < 3; ++ch) v[p][ch] = __fmul2_rn(__fmul2_rn(v[p][ch], v[p][ch]), v[p][ch]);
     }
-    if (a.flags & ZS_CHAIN_CLAMP) zs_m3x2<true>(a.m2[2], r, g, b);
-    else zs_m3x2<false>(a.m2[2], r, g, b);
-    zs_m3x2<false>(a.m2[3], r, g, b);
+    const bool clamp = S::generic ? (a.flags & ZS_CHAIN_CLAMP) != 0 : true;
+    if (clamp) zs_m3x2x2<true>(a.m2[2], v);
+    else zs_m3x2x2<false>(a.m2[2], v);
+    zs_m3x2x2<false>(a.m2[3], v);
+}
+
+// Alpha codes of a texel pair as floats: byte 3 of each texel under the exponent of 2^23
+// (one byte permute), minus 2^23 by one packed add.
+__device__ __forceinline__ float2 zs_alpha2(uint32_t w0, uint32_t w1) {
+    const float2 biased = make_float2(__uint_as_float(__byte_perm(w0, 0x4B000000u, 0x7443u)),
+                                      __uint_as_float(__byte_perm(w1, 0x4B000000u, 0x7443u)));
+    return __fadd2_rn(biased, make_float2(-8388608.0f, -8388608.0f));
 }
 
 // Box (area coverage) window of output index u along one axis.
@@ -126,7 +175,7 @@ __device__ __forceinline__ uint32_t zs_batch_encode(float4 acc, float inv) {
 }
 
 // A streaming item: output rows [v0, v1) x output columns [u0, u1) of image I.
-template <bool NONNEG, bool RANK1>
+template <int SPEC>
 __device__ __forceinline__ void zs_batch_stream(const ZsBatchImage &I, int band, int chunk, float4 *hb,
                                                 const unsigned char *lut, uint32_t lane4, int lane,
                                                 const ZsBatchArgs &a, uint32_t *out) {
@@ -149,26 +198,34 @@ __device__ __forceinline__ void zs_batch_stream(const ZsBatchImage &I, int band,
     int v = v0;
     int y = jy0;
     const uint32_t *row = img + (size_t)y * I.width + c0;   // this lane's first column of row y
+    const int W = I.width;
     uint32_t w0 = in0 ? __ldg(row) : 0u, w1 = in1 ? __ldg(row + 32) : 0u;
     uint32_t w2 = in2 ? __ldg(row + 64) : 0u, w3 = in3 ? __ldg(row + 96) : 0u;
-    // The band ends when its last output row is stored (ye, the end of that row's window,
-    // only bounds the prefetch); y stays inside the image.
+    // Rows y + 1 and y + 2 are in flight during row y's arithmetic.  The band ends when its
+    // last output row is stored (ye, the end of that row's window, only bounds the prefetch);
+    // y stays inside the image.
+    bool hn = y + 1 < ye && y + 1 < I.height;
+    uint32_t n0 = 0u, n1 = 0u, n2 = 0u, n3 = 0u;
+    if (hn) {
+        n0 = in0 ? __ldg(row + W) : 0u;
+        n1 = in1 ? __ldg(row + W + 32) : 0u;
+        n2 = in2 ? __ldg(row + W + 64) : 0u;
+        n3 = in3 ? __ldg(row + W + 96) : 0u;
+    }
     for (;;) {
-        // Next row's texels in flight during this row's arithmetic.
-        uint32_t n0 = 0u, n1 = 0u, n2 = 0u, n3 = 0u;
-        const bool ahead = y + 1 < ye && y + 1 < I.height;
-        if (ahead) {
-            const uint32_t *nrow = row + I.width;
-            n0 = in0 ? __ldg(nrow) : 0u;
-            n1 = in1 ? __ldg(nrow + 32) : 0u;
-            n2 = in2 ? __ldg(nrow + 64) : 0u;
-            n3 = in3 ? __ldg(nrow + 96) : 0u;
+        uint32_t m0 = 0u, m1 = 0u, m2 = 0u, m3 = 0u;
+        const bool hm = y + 2 < ye && y + 2 < I.height;
+        if (hm) {
+            const uint32_t *mrow = row + 2 * W;
+            m0 = in0 ? __ldg(mrow) : 0u;
+            m1 = in1 ? __ldg(mrow + 32) : 0u;
+            m2 = in2 ? __ldg(mrow + 64) : 0u;
+            m3 = in3 ? __ldg(mrow + 96) : 0u;
         }
-        float2 r0, g0, b0, r1, g1, b1;
-        zs_batch_chain2<NONNEG, RANK1>(w0, w1, lut, lane4, a, r0, g0, b0);
-        zs_batch_chain2<NONNEG, RANK1>(w2, w3, lut, lane4, a, r1, g1, b1);
-        const float2 al0 = make_float2(__uint2float_rn(w0 >> 24), __uint2float_rn(w1 >> 24));
-        const float2 al1 = make_float2(__uint2float_rn(w2 >> 24), __uint2float_rn(w3 >> 24));
+        float2 cv[2][3];
+        zs_batch_chain4<SPEC>(w0, w1, w2, w3, lut, lane4, a, cv);
+        const float2 r0 = cv[0][0], g0 = cv[0][1], b0 = cv[0][2], r1 = cv[1][0], g1 = cv[1][1], b1 = cv[1][2];
+        const float2 al0 = zs_alpha2(w0, w1), al1 = zs_alpha2(w2, w3);
         const float wy = zs_cover(loy, hiy, y);
         const float2 wy2 = make_float2(wy, wy);
         sr0 = __ffma2_rn(wy2, r0, sr0);
@@ -228,8 +285,8 @@ __device__ __forceinline__ void zs_batch_stream(const ZsBatchImage &I, int band,
         }
         if (v >= v1 || y + 1 >= I.height) break;
         ++y;
-        row += I.width;
-        if (!ahead) {
+        row += W;
+        if (!hn) {
             n0 = in0 ? __ldg(row) : 0u;
             n1 = in1 ? __ldg(row + 32) : 0u;
             n2 = in2 ? __ldg(row + 64) : 0u;
@@ -239,11 +296,16 @@ __device__ __forceinline__ void zs_batch_stream(const ZsBatchImage &I, int band,
         w1 = n1;
         w2 = n2;
         w3 = n3;
+        n0 = m0;
+        n1 = m1;
+        n2 = m2;
+        n3 = m3;
+        hn = hm;
     }
 }
 
 // A per-output item (upscaled images): lane l owns output column u of 32, rows [v0, v1).
-template <bool NONNEG, bool RANK1>
+template <int SPEC>
 __device__ __forceinline__ void zs_batch_direct(const ZsBatchImage &I, int band, int chunk, const unsigned char *lut,
                                                 uint32_t lane4, int lane, const ZsBatchArgs &a, uint32_t *out) {
     const int u = chunk * I.kx + lane;
@@ -265,13 +327,14 @@ __device__ __forceinline__ void zs_batch_direct(const ZsBatchImage &I, int band,
             for (int jx = jx0; jx < jx1; jx += 2) {
                 const bool two = jx + 1 < jx1;
                 const uint32_t t0 = __ldg(row + jx), t1 = two ? __ldg(row + jx + 1) : t0;
-                float2 r, g, b;
-                zs_batch_chain2<NONNEG, RANK1>(t0, t1, lut, lane4, a, r, g, b);
+                float2 v[2][3];
+                zs_batch_chain4<SPEC>(t0, t1, t0, t1, lut, lane4, a, v);
+                const float2 al = zs_alpha2(t0, t1);
                 const float wa = wy * zs_cover(lox, hix, jx), wb = two ? wy * zs_cover(lox, hix, jx + 1) : 0.f;
-                acc.x = fmaf(wb, r.y, fmaf(wa, r.x, acc.x));
-                acc.y = fmaf(wb, g.y, fmaf(wa, g.x, acc.y));
-                acc.z = fmaf(wb, b.y, fmaf(wa, b.x, acc.z));
-                acc.w = fmaf(wb, __uint2float_rn(t1 >> 24), fmaf(wa, __uint2float_rn(t0 >> 24), acc.w));
+                acc.x = fmaf(wb, v[0][0].y, fmaf(wa, v[0][0].x, acc.x));
+                acc.y = fmaf(wb, v[0][1].y, fmaf(wa, v[0][1].x, acc.y));
+                acc.z = fmaf(wb, v[0][2].y, fmaf(wa, v[0][2].x, acc.z));
+                acc.w = fmaf(wb, al.y, fmaf(wa, al.x, acc.w));
             }
         }
         const float wsum = wxsum * fmaxf(fminf(hiy, (float)jy1) - fmaxf(loy, (float)jy0), 0.f);
@@ -281,7 +344,7 @@ __device__ __forceinline__ void zs_batch_direct(const ZsBatchImage &I, int band,
 
 // One block per SM (the 64 KiB decode table once per SM); THREADS is 768 or 640 (autotuned:
 // 24 warps with a few spilled registers or 20 warps without).
-template <int THREADS, bool NONNEG, bool RANK1>
+template <int THREADS, int SPEC>
 __global__ void __launch_bounds__(THREADS, 1) zs_batch_kernel(const __grid_constant__ ZsBatchArgs a) {
     // [0, 64 KiB): decode table, [code][64] floats (lanes 32..63 unused);
     // then one 128-column slice of float4 column sums per warp.
@@ -304,8 +367,8 @@ __global__ void __launch_bounds__(THREADS, 1) zs_batch_kernel(const __grid_const
         const int local = it - a.prefix[img];
         const int band = local / I.chunks, chunk = local - band * I.chunks;
         uint32_t *out = reinterpret_cast<uint32_t *>(a.out + (size_t)img * a.canvas * a.canvas * 4);
-        if (I.stream) zs_batch_stream<NONNEG, RANK1>(I, band, chunk, hb, lut, lane4, lane, a, out);
-        else zs_batch_direct<NONNEG, RANK1>(I, band, chunk, lut, lane4, lane, a, out);
+        if (I.stream) zs_batch_stream<SPEC>(I, band, chunk, hb, lut, lane4, lane, a, out);
+        else zs_batch_direct<SPEC>(I, band, chunk, lut, lane4, lane, a, out);
     }
 }
 
@@ -420,22 +483,25 @@ int batch_thumbnails(Executable *chain, const void *const *images, const uint32_
     std::memcpy(a.m2, cs->chain.m2, sizeof(a.m2));
     std::memcpy(a.mb_v, cs->chain.mb_v, sizeof(a.mb_v));
     std::memcpy(a.mb_d, cs->chain.mb_d, sizeof(a.mb_d));
-    const bool nonneg = (a.flags & ZS_CHAIN_CBRT_NONNEG) || !(a.flags & ZS_CHAIN_CBRT);
+    const bool lab = (a.flags & ZS_CHAIN_CBRT) && (a.flags & ZS_CHAIN_CUBE) && (a.flags & ZS_CHAIN_CLAMP);
+    const bool nonneg = (a.flags & ZS_CHAIN_CBRT_NONNEG) != 0;
     const bool rank1 = (a.flags & ZS_CHAIN_MB_RANK1) != 0;
+    const int spec = !lab ? ZS_BATCH_GENERIC
+                          : (nonneg ? (rank1 ? ZS_BATCH_LAB_NONNEG_RANK1 : ZS_BATCH_LAB_NONNEG)
+                                    : (rank1 ? ZS_BATCH_LAB_RANK1 : ZS_BATCH_LAB));
     if (chain->batch_threads <= 0) {
         int tuned;
         if (tune_get(batch_tune_key(*chain, canvas, chain->device, "batch_threads"), tuned) &&
             (tuned == 768 || tuned == 640))
             chain->batch_threads = tuned;
     }
-    const int threads = chain->batch_threads > 0 ? chain->batch_threads : 768;
-    void (*kernel)(ZsBatchArgs);
-    if (threads == 640)
-        kernel = nonneg ? (rank1 ? zs_batch_kernel<640, true, true> : zs_batch_kernel<640, true, false>)
-                        : (rank1 ? zs_batch_kernel<640, false, true> : zs_batch_kernel<640, false, false>);
-    else
-        kernel = nonneg ? (rank1 ? zs_batch_kernel<768, true, true> : zs_batch_kernel<768, true, false>)
-                        : (rank1 ? zs_batch_kernel<768, false, true> : zs_batch_kernel<768, false, false>);
+    const int threads = chain->batch_threads > 0 ? chain->batch_threads : 640;
+    static void (*const kernels[2][5])(ZsBatchArgs) = {
+        {zs_batch_kernel<768, 0>, zs_batch_kernel<768, 1>, zs_batch_kernel<768, 2>, zs_batch_kernel<768, 3>,
+         zs_batch_kernel<768, 4>},
+        {zs_batch_kernel<640, 0>, zs_batch_kernel<640, 1>, zs_batch_kernel<640, 2>, zs_batch_kernel<640, 3>,
+         zs_batch_kernel<640, 4>}};
+    void (*kernel)(ZsBatchArgs) = kernels[threads == 640 ? 1 : 0][spec];
     const size_t smem = 256 * 64 * sizeof(float) + (size_t)(threads / 32) * ZS_BATCH_SPAN * sizeof(float4);
     e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int per_sm = 0;
