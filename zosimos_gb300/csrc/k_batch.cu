@@ -191,37 +191,28 @@ __device__ __forceinline__ void zs_batch_stream(const ZsBatchImage &I, int band,
     zs_box_window(v1 - 1, I.sy, I.fy, I.height, t0, ye, tlo, thi);
     zs_box_window(v0, I.sy, I.fy, I.height, jy0, jy1, loy, hiy);
     const uint32_t *img = reinterpret_cast<const uint32_t *>(I.ptr);
+    const int W = I.width;
+    // This lane's columns xs + lane + 32 k; those past the span re-read its last column
+    // (computed, never used), so every load is unconditional.
     const int c0 = xs + lane;
-    const bool in0 = c0 < xe, in1 = c0 + 32 < xe, in2 = c0 + 64 < xe, in3 = c0 + 96 < xe;
+    const int o0 = min(c0, xe - 1), o1 = min(c0 + 32, xe - 1), o2 = min(c0 + 64, xe - 1), o3 = min(c0 + 96, xe - 1);
     // Column sums: pair 0 = columns (c0, c0 + 32), pair 1 = (c0 + 64, c0 + 96).
     float2 sr0 = make_float2(0.f, 0.f), sg0 = sr0, sb0 = sr0, sa0 = sr0, sr1 = sr0, sg1 = sr0, sb1 = sr0, sa1 = sr0;
     int v = v0;
     int y = jy0;
-    const uint32_t *row = img + (size_t)y * I.width + c0;   // this lane's first column of row y
-    const int W = I.width;
-    uint32_t w0 = in0 ? __ldg(row) : 0u, w1 = in1 ? __ldg(row + 32) : 0u;
-    uint32_t w2 = in2 ? __ldg(row + 64) : 0u, w3 = in3 ? __ldg(row + 96) : 0u;
-    // Rows y + 1 and y + 2 are in flight during row y's arithmetic.  The band ends when its
-    // last output row is stored (ye, the end of that row's window, only bounds the prefetch);
-    // y stays inside the image.
-    bool hn = y + 1 < ye && y + 1 < I.height;
-    uint32_t n0 = 0u, n1 = 0u, n2 = 0u, n3 = 0u;
-    if (hn) {
-        n0 = in0 ? __ldg(row + W) : 0u;
-        n1 = in1 ? __ldg(row + W + 32) : 0u;
-        n2 = in2 ? __ldg(row + W + 64) : 0u;
-        n3 = in3 ? __ldg(row + W + 96) : 0u;
-    }
+    // Rows y + 1 and y + 2 are in flight during row y's arithmetic; prefetches stop at the
+    // band's last row (ylast).  The band ends when its last output row is stored; should it
+    // run past ylast, the row is loaded when it is needed (ny tracks the prefetched row).
+    const int ylast = max(min(ye, I.height) - 1, jy0);
+    const uint32_t *p = img + (size_t)y * W;
+    uint32_t w0 = __ldg(p + o0), w1 = __ldg(p + o1), w2 = __ldg(p + o2), w3 = __ldg(p + o3);
+    int ny = min(y + 1, ylast);
+    p = img + (size_t)ny * W;
+    uint32_t n0 = __ldg(p + o0), n1 = __ldg(p + o1), n2 = __ldg(p + o2), n3 = __ldg(p + o3);
     for (;;) {
-        uint32_t m0 = 0u, m1 = 0u, m2 = 0u, m3 = 0u;
-        const bool hm = y + 2 < ye && y + 2 < I.height;
-        if (hm) {
-            const uint32_t *mrow = row + 2 * W;
-            m0 = in0 ? __ldg(mrow) : 0u;
-            m1 = in1 ? __ldg(mrow + 32) : 0u;
-            m2 = in2 ? __ldg(mrow + 64) : 0u;
-            m3 = in3 ? __ldg(mrow + 96) : 0u;
-        }
+        const int my = min(y + 2, ylast);
+        p = img + (size_t)my * W;
+        const uint32_t m0 = __ldg(p + o0), m1 = __ldg(p + o1), m2 = __ldg(p + o2), m3 = __ldg(p + o3);
         float2 cv[2][3];
         zs_batch_chain4<SPEC>(w0, w1, w2, w3, lut, lane4, a, cv);
         const float2 r0 = cv[0][0], g0 = cv[0][1], b0 = cv[0][2], r1 = cv[1][0], g1 = cv[1][1], b1 = cv[1][2];
@@ -285,12 +276,12 @@ __device__ __forceinline__ void zs_batch_stream(const ZsBatchImage &I, int band,
         }
         if (v >= v1 || y + 1 >= I.height) break;
         ++y;
-        row += W;
-        if (!hn) {
-            n0 = in0 ? __ldg(row) : 0u;
-            n1 = in1 ? __ldg(row + 32) : 0u;
-            n2 = in2 ? __ldg(row + 64) : 0u;
-            n3 = in3 ? __ldg(row + 96) : 0u;
+        if (ny != y) {
+            p = img + (size_t)y * W;
+            n0 = __ldg(p + o0);
+            n1 = __ldg(p + o1);
+            n2 = __ldg(p + o2);
+            n3 = __ldg(p + o3);
         }
         w0 = n0;
         w1 = n1;
@@ -300,7 +291,7 @@ __device__ __forceinline__ void zs_batch_stream(const ZsBatchImage &I, int band,
         n1 = m1;
         n2 = m2;
         n3 = m3;
-        hn = hm;
+        ny = my;
     }
 }
 
