@@ -7,8 +7,9 @@
 // fit-resize so the long side is `canvas` -> centred inscribe on a transparent
 // canvas x canvas image -> exact sRGB8 encode.  The canvases are zero-filled (the
 // transparent margins) by one memset; the fitted pixels are cut into work items, one item per
-// warp, taken by static striding over all images (no atomics, no block barriers), so that
-// every image's cost spreads over all warps.
+// warp at a time, which warps take from a queue (one atomic add per item, no block barriers)
+// over all images, ordered largest items first, so that every image's cost spreads over all
+// warps and they finish together.
 //
 // The colour chain is nonlinear, so it runs on every source texel before the box filter.
 // Downscaled images (both scale factors >= 1, the bulk of the work) use streaming items that
@@ -51,11 +52,14 @@ struct ZsBatchImage {
     int32_t kx;                // output columns per item
     int32_t chunks;            // items across the fitted width
     int32_t ry;                // output rows per item
+    int32_t index;             // the image's position in the caller's list (its canvas)
+    int32_t pad;
 };
 
 struct ZsBatchArgs {
     const ZsBatchImage *images;
     const int32_t *prefix;     // [n + 1]: first work item of each image, total at [n]
+    int32_t *queue;            // next work item (zeroed before every batch)
     uint8_t *out;
     int32_t n;
     int32_t canvas;
@@ -349,15 +353,20 @@ __global__ void __launch_bounds__(THREADS, 1) zs_batch_kernel(const __grid_const
     float4 *hb = reinterpret_cast<float4 *>(zs_batch_smem + 256 * 64) + (threadIdx.x >> 5) * ZS_BATCH_SPAN;
     const int lane = threadIdx.x & 31;
     const uint32_t lane4 = (uint32_t)lane << 2;
-    const int warps = (int)(gridDim.x * (blockDim.x >> 5));
     const int total = a.prefix[a.n];
-    int img = 0;   // image of the current item: items only move forward, so scan from the last one
-    for (int it = (int)(blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5)); it < total; it += warps) {
+    int img = 0;   // entry of the current item: a warp's items only move forward, so scan on
+    for (;;) {
+        // Each warp takes the next item of the queue: the images are ordered by item cost,
+        // largest first, so the last items handed out are the cheapest.
+        int it = 0;
+        if (lane == 0) it = atomicAdd(a.queue, 1);
+        it = __shfl_sync(0xffffffffu, it, 0);
+        if (it >= total) break;
         while (a.prefix[img + 1] <= it) ++img;
         const ZsBatchImage I = a.images[img];
         const int local = it - a.prefix[img];
         const int band = local / I.chunks, chunk = local - band * I.chunks;
-        uint32_t *out = reinterpret_cast<uint32_t *>(a.out + (size_t)img * a.canvas * a.canvas * 4);
+        uint32_t *out = reinterpret_cast<uint32_t *>(a.out + (size_t)I.index * a.canvas * a.canvas * 4);
         if (I.stream) zs_batch_stream<SPEC>(I, band, chunk, hb, lut, lane4, lane, a, out);
         else zs_batch_direct<SPEC>(I, band, chunk, lut, lane4, lane, a, out);
     }
@@ -414,9 +423,11 @@ int batch_thumbnails(Executable *chain, const void *const *images, const uint32_
             chain->batch_rows = tuned;
     }
     const int rows = chain->batch_rows > 0 ? chain->batch_rows : ZS_BATCH_ROWS_DEFAULT;
-    std::vector<int32_t> prefix(n + 1, 0);
+    std::vector<double> cost(n);
     for (uint32_t i = 0; i < n; ++i) {
         ZsBatchImage &I = host[i];
+        I.index = (int32_t)i;
+        I.pad = 0;
         // Streaming when both axes shrink and the box windows of at least one output column
         // fit the 128-column span (2 columns of slack for the window rounding).
         const int kx = (int)std::floor((ZS_BATCH_SPAN - 4) / (double)I.sx);
@@ -429,18 +440,33 @@ int batch_thumbnails(Executable *chain, const void *const *images, const uint32_
             I.ry = rows;
         }
         I.chunks = (I.tw + I.kx - 1) / I.kx;
+        // Texels one item puts through the chain.
+        cost[i] = I.stream ? std::min((double)ZS_BATCH_SPAN, I.kx * (double)I.sx + 2.0) * (I.ry * (double)I.sy + 1.0)
+                           : 32.0 * I.ry * (std::ceil(I.fx) + 1.0) * (std::ceil(I.fy) + 1.0);
+    }
+    // Work list: images by item cost, largest first (ties in the caller's order), so that the
+    // queue ends with its cheapest items and the warps finish together.
+    std::vector<uint32_t> order(n);
+    for (uint32_t i = 0; i < n; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t x, uint32_t y) { return cost[x] > cost[y]; });
+    std::vector<ZsBatchImage> sorted(n);
+    std::vector<int32_t> prefix(n + 1, 0);
+    for (uint32_t k = 0; k < n; ++k) {
+        const ZsBatchImage &I = host[order[k]];
+        sorted[k] = I;
         const int64_t items = (int64_t)((I.th + I.ry - 1) / I.ry) * I.chunks;
-        if ((int64_t)prefix[i] + items > INT32_MAX) {
+        if ((int64_t)prefix[k] + items > INT32_MAX) {
             set_last_error("zs_batch_thumbnails: too many output pixels in one batch");
             return ZS_ERR_INVALID_ARG;
         }
-        prefix[i + 1] = prefix[i] + (int32_t)items;
+        prefix[k + 1] = prefix[k] + (int32_t)items;
     }
     // Scratch: image table + item prefix table, kept with the executable, uploaded from a
     // pinned staging copy.  The previous batch of this executable must have finished with
     // both before they are rewritten.
     const size_t table_bytes = (sizeof(ZsBatchImage) * n + 255) & ~(size_t)255;
-    const size_t bytes = table_bytes + sizeof(int32_t) * (n + 1);
+    const size_t prefix_bytes = (sizeof(int32_t) * (n + 1) + 15) & ~(size_t)15;
+    const size_t bytes = table_bytes + prefix_bytes + 16;   // + the queue counter
     auto device_error = [](cudaError_t e) {
         set_last_error(std::string("zs_batch_thumbnails: ") + cudaGetErrorString(e));
         return e == cudaErrorMemoryAllocation ? ZS_ERR_OUT_OF_MEMORY : ZS_ERR_DEVICE;
@@ -459,14 +485,16 @@ int batch_thumbnails(Executable *chain, const void *const *images, const uint32_
     if (!chain->batch_done && (e = cudaEventCreateWithFlags(&chain->batch_done, cudaEventDisableTiming)) != cudaSuccess)
         return device_error(e);
     uint8_t *scratch = (uint8_t *)chain->batch_scratch, *staging = (uint8_t *)chain->batch_staging;
-    std::memcpy(staging, host.data(), sizeof(ZsBatchImage) * n);
+    std::memcpy(staging, sorted.data(), sizeof(ZsBatchImage) * n);
     std::memcpy(staging + table_bytes, prefix.data(), sizeof(int32_t) * (n + 1));
-    if ((e = cudaMemcpyAsync(scratch, staging, bytes, cudaMemcpyHostToDevice, stream)) != cudaSuccess)
+    if ((e = cudaMemcpyAsync(scratch, staging, table_bytes + prefix_bytes, cudaMemcpyHostToDevice, stream)) !=
+        cudaSuccess)
         return device_error(e);
     ZsBatchArgs a;
     std::memset(&a, 0, sizeof(a));
     a.images = (const ZsBatchImage *)scratch;
     a.prefix = (const int32_t *)(scratch + table_bytes);
+    a.queue = (int32_t *)(scratch + table_bytes + prefix_bytes);
     a.out = (uint8_t *)out;
     a.n = (int)n;
     a.canvas = (int)canvas;
@@ -499,7 +527,7 @@ int batch_thumbnails(Executable *chain, const void *const *images, const uint32_
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);
     if (e != cudaSuccess) return device_error(e);
     if (per_sm < 1) per_sm = 1;
-    // The grid covers every SM: warps stride over the items of all images.
+    // The grid covers every SM: warps take items of all images from the queue.
     long long blocks = (long long)chain->sm_count * per_sm;
     const long long need = ((long long)prefix[n] + threads / 32 - 1) / (threads / 32);
     if (blocks > need) blocks = need;
@@ -518,8 +546,10 @@ int batch_thumbnails(Executable *chain, const void *const *images, const uint32_
         std::memcpy(key.data() + at, &a, sizeof(ZsBatchArgs));
     }
     auto enqueue = [&]() {
-        // Transparent margins: zero every canvas, the kernel writes the fitted pixels.
-        cudaError_t ce = cudaMemsetAsync(out, 0, (size_t)n * canvas * canvas * 4, stream);
+        // The work queue starts at item 0; transparent margins: zero every canvas, the kernel
+        // writes the fitted pixels.
+        cudaError_t ce = cudaMemsetAsync(a.queue, 0, sizeof(int32_t), stream);
+        if (ce == cudaSuccess) ce = cudaMemsetAsync(out, 0, (size_t)n * canvas * canvas * 4, stream);
         if (ce == cudaSuccess) {
             kernel<<<(unsigned)blocks, threads, smem, stream>>>(a);
             ce = cudaGetLastError();
