@@ -1,0 +1,205 @@
+"""Measured error against the FP64 oracle, per op and per configuration, for the fused
+executor (FP16 storage where a fused program must store an intermediate), the plain per-op
+FP32 programs and the per-op FP16-storage programs.
+
+Every row is also a parity check: 8-bit outputs within 1 LSB, RGBA16F outputs within 2e-3,
+FP32 outputs of the colour stages within the bound written beside them.  With ZS_ERROR_TABLE
+set to a path, the measured values are written there as a markdown table.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+import pipelines as P
+import zosimos_gb300 as zs
+from zosimos_gb300 import Bits, ChromaticAdaptationMethod, ColorKind, CommandBuffer, Descriptor, Parts, Pool
+from zosimos_gb300 import Transfer, Whitepoint
+from zosimos_gb300.synthetic import (layer_transforms, linear_gradient_gauss, premultiplied_layer,
+                                     srgb_gradient_noise, thumbnail_sizes)
+from zosimos_gb300.workloads import OKLAB_SCALE
+
+pytestmark = pytest.mark.gpu
+
+MODES = [("fused", zs.Mode.Fused), ("per-op FP32", zs.Mode.PerOpF32), ("per-op FP16", zs.Mode.PerOpF16)]
+F16_TOL = 2.0e-3
+ROWS = []
+
+
+@pytest.fixture(scope="module", autouse=True)
+def table():
+    yield
+    path = os.environ.get("ZS_ERROR_TABLE")
+    if not path:
+        return
+    with open(path, "w") as f:
+        f.write("| config | op (output) | mode | error vs FP64 | bound |\n|---|---|---|---|---|\n")
+        for r in ROWS:
+            f.write("| " + " | ".join(str(x) for x in r) + " |\n")
+
+
+def record(config, op, mode, err, unit, bound):
+    shown = f"{err} LSB" if unit == "lsb" else f"{err:.3g}"
+    ROWS.append((config, op, mode, shown, f"{bound} LSB" if unit == "lsb" else f"{bound:g}"))
+    assert err <= bound, (config, op, mode, err)
+
+
+def lsb(a, b):
+    return int(np.abs(a.astype(np.int16) - b.astype(np.int16)).max())
+
+
+# ---------------------------------------------------------------- config 2: the colour chain, stage by stage
+
+LAB = dict(bits=Bits.Float32x4, parts=Parts.LabA, color=ColorKind.Oklab, transfer=Transfer.Linear)
+
+
+def chain_prefix(w, h, stages):
+    """The chain's first `stages` ops (1..7); stages < 7 end with an FP32 output."""
+    c = CommandBuffer()
+    i = c.input(Descriptor.srgb_rgba8(w, h))
+    r = c.color_convert(i, Descriptor.linear_rgba_f32(w, h))
+    steps = [
+        lambda r: c.chromatic_adaptation(r, ChromaticAdaptationMethod.BradfordVonKries, Whitepoint.D50),
+        lambda r: c.color_convert(r, Descriptor(w, h, **LAB)),
+        lambda r: c.color_matrix(r, OKLAB_SCALE),
+        lambda r: c.color_convert(r, Descriptor.linear_rgba_f32(w, h, whitepoint=Whitepoint.D50)),
+        lambda r: c.chromatic_adaptation(r, ChromaticAdaptationMethod.BradfordVonKries, Whitepoint.D65),
+        lambda r: c.color_convert(r, Descriptor.srgb_rgba8(w, h)),
+    ]
+    for s in steps[:stages - 1]:
+        r = s(r)
+    o, _ = c.output(r)
+    return c, i, o
+
+
+def oracle_stages(img):
+    """FP64 values after each of the seven ops."""
+    h, w = img.shape[:2]
+    x = O.decode(O.SRGB_RGBA8, P.rgba_bytes(img), w, h)
+    out = [x.copy()]
+    a1 = np.linalg.inv(O.rgb_to_xyz("Bt709", "D50")) @ O.adaptation("BradfordVonKries", "D65", "D50") @ O.rgb_to_xyz()
+    O.mat3(x, a1)
+    out.append(x.copy())
+    O.oklab_encode(x, O.rgb_to_xyz("Bt709", "D50"))
+    out.append(x.copy())
+    O.mat3(x, np.asarray(OKLAB_SCALE).reshape(3, 3))
+    out.append(x.copy())
+    O.oklab_decode(x, np.linalg.inv(O.rgb_to_xyz("Bt709", "D50")))
+    out.append(x.copy())
+    a2 = np.linalg.inv(O.rgb_to_xyz()) @ O.adaptation("BradfordVonKries", "D50", "D65") @ O.rgb_to_xyz("Bt709", "D50")
+    O.mat3(x, a2)
+    out.append(x.copy())
+    out.append(O.encode(O.SRGB_RGBA8, x))
+    return out
+
+
+STAGES = ["sRGB8 decode (linear FP32)", "+ Bradford D65->D50 (linear FP32)", "+ Oklab encode, cube root (Lab FP32)",
+          "+ L x1.1, C x0.9 (Lab FP32)", "+ Oklab decode, cube (linear FP32)", "+ Bradford D50->D65 (linear FP32)",
+          "+ sRGB8 encode (the whole chain)"]
+# FP32 arithmetic bounds of the colour stages (max-abs, values of order 1).
+STAGE_TOL = [1e-6, 2e-6, 2e-5, 2e-5, 5e-5, 5e-5]
+STAGE_TOL_F16 = 2e-3
+
+
+@pytest.fixture(scope="module")
+def chain_case():
+    img = P.rgb_cube_image()[:512]          # 512 x 4096: 2^21 of the 2^24 RGB triples
+    return img, oracle_stages(img)
+
+
+@pytest.mark.parametrize("stage", range(1, 8))
+@pytest.mark.parametrize("name,mode", MODES)
+def test_chain_stage_error(chain_case, stage, name, mode):
+    img, ref = chain_case
+    h, w = img.shape[:2]
+    c, i, o = chain_prefix(w, h, stage)
+    pool = Pool()
+    k = pool.insert_srgb(img)
+    got = P.run(c, pool, [(i, k)], [o], mode)[0]
+    if stage == 7:
+        record("2 colour chain", STAGES[stage - 1], name, lsb(got.reshape(h, w * 4), ref[6].reshape(h, w * 4)), "lsb", 1)
+        return
+    got = np.frombuffer(got, np.float32).reshape(h, w, 4).astype(np.float64)
+    err = float(np.abs(got[..., :3] - ref[stage - 1][..., :3]).max())
+    # A program that ends in an FP32 output stores nothing else in fused mode; the per-op FP16
+    # programs store every intermediate as FP16.
+    bound = STAGE_TOL_F16 if (mode == zs.Mode.PerOpF16 and stage > 1) else STAGE_TOL[stage - 1]
+    record("2 colour chain", STAGES[stage - 1], name, err, "abs", bound)
+
+
+# ---------------------------------------------------------------- config 1: decode, blend, bilinear resize
+
+
+@pytest.mark.parametrize("name,mode", MODES)
+def test_blend_resize_error(name, mode):
+    a = srgb_gradient_noise(512, 512, seed=1, image=0)
+    b = srgb_gradient_noise(512, 512, seed=1, image=1)
+    got = P.ours_blend_resize(a, b, mode=mode)
+    record("1 blend + resize", "over + bilinear 512->384 (sRGB8)", name, lsb(got, P.oracle_blend_resize(a, b)), "lsb", 1)
+
+
+# ---------------------------------------------------------------- config 3: resample sweep and rotation
+
+
+@pytest.fixture(scope="module")
+def img2k():
+    img = linear_gradient_gauss(2048, 2048, seed=3)
+    return img, img.astype(np.float64)
+
+
+RESAMPLE_MODES = [("fused, tensor cores", zs.Mode.Fused, False), ("fused, FP32 SIMT", zs.Mode.Fused, True),
+                  ("per-op FP32", zs.Mode.PerOpF32, False), ("per-op FP16", zs.Mode.PerOpF16, False)]
+
+
+@pytest.mark.parametrize("filt,fname", [(zs.Filter.Lanczos3, "Lanczos-3"), (zs.Filter.Box, "box")])
+@pytest.mark.parametrize("factor", [2.0, 3.7, 8.0])
+@pytest.mark.parametrize("name,mode,simt", RESAMPLE_MODES)
+def test_resample_error(img2k, filt, fname, factor, name, mode, simt):
+    img, img64 = img2k
+    ow = int(round(2048 / factor))
+    got = P.ours_resample(img, (ow, ow), filt, mode, simt)
+    err = float(np.abs(got - O.resample(img64, ow, ow, filt)).max())
+    record("3 resample (RGBA16F 2048^2)", f"{fname} /{factor:g}", name, err, "abs", F16_TOL)
+
+
+@pytest.mark.parametrize("name,mode", MODES)
+def test_rotation_error(img2k, name, mode):
+    img, _ = img2k
+    got = P.ours_rotation(img, 17.0, mode)
+    err = float(np.abs(got - P.oracle_rotation(img, 17.0)).max())
+    record("3 resample (RGBA16F 2048^2)", "17 deg bilinear rotation", name, err, "abs", F16_TOL)
+
+
+# ---------------------------------------------------------------- config 4: thumbnails
+
+
+def test_thumbnail_batch_error():
+    ws, hs = thumbnail_sizes(1024, seed=4)
+    images = [srgb_gradient_noise(int(w), int(h), seed=4, image=i) for i, (w, h) in enumerate(zip(ws[:64], hs[:64]))]
+    got = P.ours_thumbnails(images)
+    ref = P.oracle_thumbnails(images)
+    record("4 thumbnails (64 of the 1024)", "chain + box fit + canvas (sRGB8)", "fused batch kernel",
+           max(lsb(g, r) for g, r in zip(got, ref)), "lsb", 1)
+
+
+@pytest.mark.parametrize("name,mode", MODES)
+def test_thumbnail_program_error(name, mode):
+    ws, hs = thumbnail_sizes(1024, seed=4)
+    images = [srgb_gradient_noise(int(w), int(h), seed=4, image=i) for i, (w, h) in enumerate(zip(ws[:8], hs[:8]))]
+    ref = P.oracle_thumbnails(images)
+    err = max(lsb(P.ours_thumbnail_program(im, mode=mode), r) for im, r in zip(images, ref))
+    record("4 thumbnails (8 of the 1024)", "one program per image (sRGB8)", name, err, "lsb", 1)
+
+
+# ---------------------------------------------------------------- config 5: layer stack
+
+
+@pytest.mark.parametrize("name,mode", MODES)
+def test_layer_stack_error(name, mode):
+    n, w = 8, 1024
+    layers = [premultiplied_layer(w, w, seed=5, image=i) for i in range(n)]
+    transforms = layer_transforms(n, seed=5)
+    got = P.ours_layer_stack(layers, transforms, mode)
+    err = float(np.abs(got - P.oracle_layer_stack(layers, transforms)).max())
+    record("5 layers (8 x 1024^2)", "affine bilinear + over/multiply/screen/add (RGBA16F)", name, err, "abs", F16_TOL)
