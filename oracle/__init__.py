@@ -27,10 +27,12 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 _LIB_PATH = os.path.join(_HERE, "_build", "liboracle.so")
 _lib = None
 
-# Codes follow lib/std/src/stage.frag:102-176 of the zosimos project.
+# Codes follow lib/std/src/stage.frag:102-176 of the zosimos project, reached from the
+# SampleBits names through ShaderData::serialize_bits (lib/zosimos/src/shaders/stage.rs:98-118),
+# which maps UInt1010102 to stage.frag's Int2101010 (15) and UInt2101010 to Int1010102 (14).
 BITS = dict(UInt8=0, UInt332=1, UInt233=2, UInt16=3, UInt4x4=4, UInt_444=5, UInt444_=6, UInt565=7,
             UInt8x2=8, UInt8x3=9, UInt8x4=10, UInt16x2=11, UInt16x3=12, UInt16x4=13,
-            UInt1010102=14, UInt2101010=15, UInt101010_=16, UInt_101010=17, Float16x4=18,
+            UInt1010102=15, UInt2101010=14, UInt101010_=16, UInt_101010=17, Float16x4=18,
             Float32x4=19)
 PARTS = dict(A=0, R=1, G=2, B=3, Luma=4, LumaA=5, Rgb=6, Bgr=7, RgbA=8, Rgbx=9, BgrA=10, Bgrx=11,
              ARgb=12, Xrgb=13, ABgr=14, Xbgr=15, Yuv=16, Lab=17, LabA=18, Lch=19, LchA=20)

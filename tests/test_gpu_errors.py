@@ -99,7 +99,9 @@ STAGES = ["sRGB8 decode (linear FP32)", "+ Bradford D65->D50 (linear FP32)", "+ 
           "+ sRGB8 encode (the whole chain)"]
 # FP32 arithmetic bounds of the colour stages (max-abs, values of order 1).
 STAGE_TOL = [1e-6, 2e-6, 2e-5, 2e-5, 5e-5, 5e-5]
-STAGE_TOL_F16 = 2e-3
+# Per-op FP16 storage: each stored value carries a relative error up to 2^-11; the cube after
+# the Lab stages triples it (d(x^3) = 3 x^2 dx), so the linear stages after it get 4e-3.
+STAGE_TOL_F16 = [1e-6, 2e-3, 2e-3, 2e-3, 4e-3, 4e-3]
 
 
 @pytest.fixture(scope="module")
@@ -124,7 +126,7 @@ def test_chain_stage_error(chain_case, stage, name, mode):
     err = float(np.abs(got[..., :3] - ref[stage - 1][..., :3]).max())
     # A program that ends in an FP32 output stores nothing else in fused mode; the per-op FP16
     # programs store every intermediate as FP16.
-    bound = STAGE_TOL_F16 if (mode == zs.Mode.PerOpF16 and stage > 1) else STAGE_TOL[stage - 1]
+    bound = (STAGE_TOL_F16 if mode == zs.Mode.PerOpF16 else STAGE_TOL)[stage - 1]
     record("2 colour chain", STAGES[stage - 1], name, err, "abs", bound)
 
 

@@ -126,6 +126,21 @@ def test_transfer_from_srgb8_within_one_code(transfer, mode):
     assert np.abs(got_v - want_v).max() <= 1.0001 / 65535
 
 
+def test_packed_10bit_layouts_follow_serialize_bits():
+    """SampleBits::UInt1010102 is stage.frag's Int2101010 layout and UInt2101010 its
+    Int1010102 (ShaderData::serialize_bits, lib/zosimos/src/shaders/stage.rs:113-114): in
+    UInt1010102 the first sample is bits 0-9 and alpha bits 30-31."""
+    texels = np.array([[0x000003FF, 0xC0000000, 0x00000003, 0xFFFFFFFF]], dtype=np.uint32)
+    got = convert(desc("UInt1010102", "RgbA", "Linear", 4, 1), texels.view(np.uint8),
+                  Descriptor.linear_rgba_f32(4, 1), zs.Mode.Fused)
+    rgba = np.frombuffer(got, np.float32).reshape(4, 4)
+    assert np.allclose(rgba, [[1, 0, 0, 0], [0, 0, 0, 1], [3 / 1023, 0, 0, 0], [1, 1, 1, 1]])
+    got = convert(desc("UInt2101010", "RgbA", "Linear", 4, 1), texels.view(np.uint8),
+                  Descriptor.linear_rgba_f32(4, 1), zs.Mode.Fused)
+    rgba = np.frombuffer(got, np.float32).reshape(4, 4)
+    assert np.allclose(rgba, [[1, 255 / 1023, 0, 0], [0, 0, 0, 768 / 1023], [1, 0, 0, 0], [1, 1, 1, 1]])
+
+
 def test_int444i_green_is_bits_8_to_11():
     """UInt444_ (stage.frag's Int444i): mux writes R, G, B at bits 4, 8, 12 (stage.frag:608);
     the demux here reads G back from bit 8, so the layout round-trips (stage.frag:547-548

@@ -184,6 +184,18 @@ def test_fractal_noise_damping_sums_to_one():
     assert abs(1.0 - float(total)) < 1e-6
 
 
+def test_oracle_packed_10bit_layouts_follow_serialize_bits():
+    """UInt1010102 decodes with stage.frag's Int2101010 layout, UInt2101010 with Int1010102
+    (lib/zosimos/src/shaders/stage.rs:113-114)."""
+    texels = np.array([[0x000003FF, 0xC0000000, 0x00000003, 0xFFFFFFFF]], dtype=np.uint32).view(np.uint8)
+    f = O.Format(O.BITS["UInt1010102"], O.PARTS["RgbA"], O.TRANSFER["Linear"], False)
+    assert np.allclose(O.decode(f, texels, 4, 1).reshape(4, 4), [[1, 0, 0, 0], [0, 0, 0, 1], [3 / 1023, 0, 0, 0],
+                                                                  [1, 1, 1, 1]])
+    f = O.Format(O.BITS["UInt2101010"], O.PARTS["RgbA"], O.TRANSFER["Linear"], False)
+    assert np.allclose(O.decode(f, texels, 4, 1).reshape(4, 4), [[1, 255 / 1023, 0, 0], [0, 0, 0, 768 / 1023],
+                                                                  [1, 0, 0, 0], [1, 1, 1, 1]])
+
+
 def test_oracle_int444i_round_trips():
     """UInt444_ (stage.frag's Int444i): R, G, B at bits 4, 8, 12, as mux writes them
     (stage.frag:608).  The demux reads G from bit 8 so that mux and demux invert each other;

@@ -77,9 +77,20 @@ bool same_chroma(const Desc &a, const Desc &b) {
     return true;
 }
 
+// The stage.frag texel code of a SampleBits value (ShaderData::serialize_bits,
+// lib/zosimos/src/shaders/stage.rs:98-118).  It maps UInt1010102 to stage.frag's Int2101010
+// layout (three 10-bit samples from bit 0, 2-bit alpha at bits 30-31) and UInt2101010 to
+// Int1010102 (2-bit first sample at bit 0): the SampleBits names list samples from bit 0,
+// stage.frag's names from the top.  Every other code is the same number.
+static uint8_t stage_bits(uint32_t bits) {
+    if (bits == ZS_BITS_UINT1010102) return 15;
+    if (bits == ZS_BITS_UINT2101010) return 14;
+    return (uint8_t)bits;
+}
+
 ZsFormat format_of(const Desc &d) {
     ZsFormat f{};
-    f.bits = (uint8_t)d.bits;
+    f.bits = stage_bits(d.bits);
     f.parts = (uint8_t)d.parts;
     f.bpp = (uint8_t)texel_bytes(d.bits);
     f.native = 0;
