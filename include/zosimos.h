@@ -335,8 +335,9 @@ typedef struct zs_executable zs_executable;
 int zs_lower(const zs_program *program, const zs_capabilities *caps, zs_executable **out);
 void zs_executable_free(zs_executable *exe);
 /* Executable::query_knob (run.rs:1012-1014) for RegisterKnob { link_idx, register }: the knob
- * id and the byte length of its parameter block.  ZS_ERR_BAD_REGISTER when the register has
- * no knob (link_idx must be 0: the program itself). */
+ * id and the byte length of its parameter block.  link_idx 0 is the linked program's main
+ * buffer, i the i-th function buffer given to zs_link (its first instantiation when it is
+ * invoked more than once).  ZS_ERR_BAD_REGISTER when the register has no knob. */
 int zs_executable_query_knob(const zs_executable *exe, uint32_t link_idx, uint32_t reg, uint32_t *knob,
                              uint64_t *len);
 /* Replaces the parameter block of a knob for every later launch of the executable (the
