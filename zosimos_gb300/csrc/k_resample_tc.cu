@@ -109,12 +109,6 @@ __device__ __forceinline__ void tc_ld4(uint32_t taddr, uint32_t (&r)[4]) {
 
 __device__ __forceinline__ void tc_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-__device__ __forceinline__ float tc_lds(uint32_t addr) {
-    float v;
-    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(addr));
-    return v;
-}
-
 struct TcTile {
     int band, x0, cs0;    // 128-row band, first output column, first staged source column (even)
 };
@@ -276,42 +270,38 @@ __global__ void __launch_bounds__(ZS_TC_THREADS, 1)
             if (!tc_wait(zs_smem_addr(tabfull + ab), (lt / nbuf) & 1u, abort_flag)) break;
             if (!tc_wait(zs_smem_addr(tfull + ab), (lt / nbuf) & 1u, abort_flag)) break;
             tc_fence_after();
-            const uint32_t tw_w = zs_smem_addr(tab + ab * ZS_TC_TAB_BYTES);      // weights [tw][taps]
-            const int *tw_first = (const int *)(tab + ab * ZS_TC_TAB_BYTES + 4 * a.tc_tw * a.taps);
+            const float *tw_w = (const float *)(tab + ab * ZS_TC_TAB_BYTES);
+            const int *tw_first = (const int *)(tw_w + a.tc_tw * a.taps);
+            const int *tw_cnt = tw_first + a.tc_tw;
             const int oy = tt.band * ZS_TC_M + m;
             const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16) + ab * accw;
-            const int *tw_cnt = tw_first + a.tc_tw;
-            // Every column runs the image's full tap count (a kernel parameter, so the loop is
-            // uniform and needs no divergence handling around the warp-collective TMEM loads):
-            // the weight rows are zero past a column's own taps, whose TMEM reads repeat the
-            // column's last tap (so only the window's own values ever enter the sums).
-            const int T = a.taps;
             for (int ox = tt.x0 + part; ox < min(tt.x0 + a.tc_tw, a.width); ox += 4) {
                 const int oxl = ox - tt.x0;
+                const int cnt = tw_cnt[oxl];
                 const uint32_t col = (uint32_t)(tw_first[oxl] - tt.cs0) * 4u;
-                const uint32_t cmax = col + 4u * (uint32_t)max(tw_cnt[oxl] - 1, 0);
-                const uint32_t w = tw_w + 4u * (uint32_t)(oxl * T);
+                const float *w = tw_w + oxl * a.taps;
                 // Two accumulator pairs (even and odd taps) halve the FMA dependency chains.
                 float2 a01 = make_float2(0.f, 0.f), a23 = make_float2(0.f, 0.f);
                 float2 b01 = make_float2(0.f, 0.f), b23 = make_float2(0.f, 0.f);
-                for (int k0 = 0; k0 < T; k0 += 8) {
+                for (int k0 = 0; k0 < cnt; k0 += 8) {
+                    const int n = min(8, cnt - k0);
                     uint32_t r[8][4];
                     float wk[8];
 #pragma unroll
                     for (int j = 0; j < 8; ++j)
-                        if (k0 + j < T) tc_ld4(trow + min(col + 4u * (uint32_t)(k0 + j), cmax), r[j]);
+                        if (j < n) tc_ld4(trow + col + 4u * (uint32_t)(k0 + j), r[j]);
 #pragma unroll
                     for (int j = 0; j < 8; ++j)
-                        if (k0 + j < T) wk[j] = tc_lds(w + 4u * (uint32_t)(k0 + j));
+                        if (j < n) wk[j] = w[k0 + j];
                     tc_wait_ld();
                     // Tie the loaded registers to the wait so that no use moves above it.
 #pragma unroll
                     for (int j = 0; j < 8; ++j)
-                        if (k0 + j < T)
+                        if (j < n)
                             asm volatile("" : "+r"(r[j][0]), "+r"(r[j][1]), "+r"(r[j][2]), "+r"(r[j][3]));
 #pragma unroll
                     for (int j = 0; j < 8; ++j)
-                        if (k0 + j < T) {
+                        if (j < n) {
                             const float2 w2 = make_float2(wk[j], wk[j]);
                             const float2 v01 = make_float2(__uint_as_float(r[j][0]), __uint_as_float(r[j][1]));
                             const float2 v23 = make_float2(__uint_as_float(r[j][2]), __uint_as_float(r[j][3]));
