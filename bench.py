@@ -456,7 +456,7 @@ def workload_resample(args, stream, sh):
     src.upload(img)
     if args.profile:
         # A short, fixed sequence for ncu (4096^2 RGBA16F source, 128 MiB > L2): one fused
-        # launch each of Lanczos-3 /2, Lanczos-3 /8 and box /2.
+        # launch each of Lanczos-3 /2, Lanczos-3 /8 and box /2, then one 17 degree rotation.
         import torch
         for filt, factor in ((zs.Filter.Lanczos3, 2.0), (zs.Filter.Lanczos3, 8.0), (zs.Filter.Box, 2.0)):
             ow = int(round(n / factor))
@@ -466,6 +466,12 @@ def workload_resample(args, stream, sh):
             exe.run_device([src.ptr], [dst.ptr], sh)
             torch.cuda.synchronize()
             dst.free()
+        c, _, _, _ = rotation(n, n, 17.0)
+        exe = zs.Linker.from_included().compile(c).lower_to(zs.Capabilities(mode=zs.Mode.Fused))
+        dst = zs.DeviceBuffer(n * n * 8)
+        exe.run_device([src.ptr], [dst.ptr], sh)
+        torch.cuda.synchronize()
+        dst.free()
         print("profile run done", flush=True)
         return
     steps = max(3, args.steps // 10)
