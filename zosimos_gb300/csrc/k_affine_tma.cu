@@ -7,13 +7,13 @@
 // pixels; for each tile the rectangle of source pixels its taps can touch (the inverse
 // affine of the tile's corner pixel centres, one pixel of margin for rounding, clamped to
 // the image, x rounded down to an even pixel for the 16-byte TMA alignment) arrives by one
-// cp.async.bulk.tensor.2d copy into one of two shared buffers, the copy of the next tile in
-// flight while the current one is computed.  The taps are then shared-memory loads; the
+// cp.async.bulk.tensor.2d copy into one of three shared buffers, the copies of the next two
+// tiles in flight while the current one is computed.  The taps are then shared-memory loads; the
 // arithmetic (map, coverage, clamp-to-edge taps, lerps, pixel program, encode) is that of
 // zs_affine_f16_kernel, in the same order, so the bytes are the same.  A tile whose taps do
 // not fit the box (a transform the host did not size it for) reads global memory instead.
 //
-// Roles: thread 0 issues the copies (tiles 0 and 1 up front, tile i + 2 once every warp has
+// Roles: thread 0 issues the copies (tiles 0..2 up front, tile i + 3 once every warp has
 // released the buffer of tile i); all eight warps compute.  Every mbarrier wait is bounded
 // (one second): a wait that gives up records ZS_DEVSTAT_WAIT_TIMEOUT, the CTA stops taking
 // tiles, and thread 0 waits (bounded) for its copies still in flight before returning.
@@ -30,6 +30,7 @@
 #define ZS_AT_THREADS 256
 #define ZS_AT_TW 64
 #define ZS_AT_TH 32
+#define ZS_AT_NBUF 3          // staging buffers: two tiles in flight while one is computed
 #define ZS_AT_MAX_SMEM (200 * 1024)
 
 struct ZsAffTma {
@@ -94,7 +95,7 @@ __global__ void __launch_bounds__(ZS_AT_THREADS) zs_affine_tma_kernel(const __gr
                                                                       const __grid_constant__ CUtensorMap tm,
                                                                       const __grid_constant__ ZsAffTma p) {
     extern __shared__ __align__(128) uint8_t zs_at_smem[];
-    __shared__ __align__(8) uint64_t full[2], empty[2];
+    __shared__ __align__(8) uint64_t full[ZS_AT_NBUF], empty[ZS_AT_NBUF];
     __shared__ int abort_word;
     volatile int *abort_flag = &abort_word;
     const ZsSource &s0 = a.src[0], &s1 = a.src[1];
@@ -103,7 +104,7 @@ __global__ void __launch_bounds__(ZS_AT_THREADS) zs_affine_tma_kernel(const __gr
     const float fw = (float)W, fh = (float)H;
 
     if (threadIdx.x == 0) {
-        for (int b = 0; b < 2; ++b) {
+        for (int b = 0; b < ZS_AT_NBUF; ++b) {
             zs_mbar_init(zs_smem_addr(full + b), 1);
             zs_mbar_init(zs_smem_addr(empty + b), ZS_AT_THREADS / 32);
         }
@@ -113,15 +114,15 @@ __global__ void __launch_bounds__(ZS_AT_THREADS) zs_affine_tma_kernel(const __gr
     }
     __syncthreads();
 
-    // Thread 0: start the copy of local tile `it` into buffer it & 1 (or complete its
-    // barrier without data when its taps do not fit the box).
+    // Thread 0: start the copy of local tile `it` into buffer it % ZS_AT_NBUF (or complete
+    // its barrier without data when its taps do not fit the box).
     uint32_t issued = 0;
     auto issue = [&](uint32_t it) {
         const int t = (int)(blockIdx.x + it * gridDim.x);
         const int tyi = t / p.tiles_x, txi = t - tyi * p.tiles_x;
         const int x0 = txi * ZS_AT_TW, y0 = tyi * ZS_AT_TH;
         int bx0, by0;
-        const uint32_t b = it & 1u, bar = zs_smem_addr(full + b);
+        const uint32_t b = it % ZS_AT_NBUF, bar = zs_smem_addr(full + b);
         if (zs_at_box(a.aff, W, H, p.bw, p.bh, x0, y0, min(x0 + ZS_AT_TW, a.width), min(y0 + ZS_AT_TH, a.height), bx0,
                       by0)) {
             zs_mbar_expect_tx(bar, (uint32_t)(p.bw * p.bh * 8));
@@ -133,12 +134,12 @@ __global__ void __launch_bounds__(ZS_AT_THREADS) zs_affine_tma_kernel(const __gr
     };
     const uint32_t ntiles = blockIdx.x < (uint32_t)p.tiles ? (p.tiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
     if (threadIdx.x == 0)
-        for (uint32_t it = 0; it < 2 && it < ntiles; ++it) issue(it);
+        for (uint32_t it = 0; it < ZS_AT_NBUF && it < ntiles; ++it) issue(it);
 
     const int cxl = threadIdx.x & (ZS_AT_TW - 1), ryl = threadIdx.x / ZS_AT_TW;   // column, first row
     uint32_t landed = 0;   // tiles whose copy this thread has seen complete
     for (uint32_t it = 0; it < ntiles; ++it) {
-        const uint32_t b = it & 1u, parity = (it >> 1) & 1u;
+        const uint32_t b = it % ZS_AT_NBUF, parity = (it / ZS_AT_NBUF) & 1u;
         if (!zs_at_wait(zs_smem_addr(full + b), parity, abort_flag)) break;
         landed = it + 1;
         const int t = (int)(blockIdx.x + it * gridDim.x);
@@ -191,18 +192,20 @@ __global__ void __launch_bounds__(ZS_AT_THREADS) zs_affine_tma_kernel(const __gr
                 zs_store_raw(dp, a.dst_fmt.bpp, zs_encode_raw(a.dst_fmt, r));
             }
         }
-        // Release the buffer; thread 0 refills it with local tile it + 2 once every warp has.
+        // Release the buffer; thread 0 refills it with local tile it + ZS_AT_NBUF once every
+        // warp has.
         __syncwarp();
         if (lane == 0) zs_mbar_arrive(zs_smem_addr(empty + b));
-        if (threadIdx.x == 0 && it + 2 < ntiles) {
+        if (threadIdx.x == 0 && it + ZS_AT_NBUF < ntiles) {
             if (!zs_at_wait(zs_smem_addr(empty + b), parity, abort_flag)) break;
-            issue(it + 2);
+            issue(it + ZS_AT_NBUF);
         }
     }
     // A CTA that stops early lets thread 0's copies still in flight land before its shared
     // memory goes (bounded).
     if (threadIdx.x == 0 && *abort_flag) {
-        for (uint32_t j = landed; j < issued; ++j) zs_mbar_wait(zs_smem_addr(full + (j & 1u)), (j >> 1) & 1u);
+        for (uint32_t j = landed; j < issued; ++j)
+            zs_mbar_wait(zs_smem_addr(full + j % ZS_AT_NBUF), (j / ZS_AT_NBUF) & 1u);
     }
 }
 
@@ -235,7 +238,7 @@ bool at_box_size(const float *aff, int &bw, int &bh) {
     bw = (int)std::ceil(sx) + 6;
     bw += bw & 1;
     bh = (int)std::ceil(sy) + 5;
-    return bw <= 256 && bh <= 256 && 2 * (((size_t)bw * bh * 8 + 127) & ~(size_t)127) <= ZS_AT_MAX_SMEM;
+    return bw <= 256 && bh <= 256 && ZS_AT_NBUF * (((size_t)bw * bh * 8 + 127) & ~(size_t)127) <= ZS_AT_MAX_SMEM;
 }
 
 }  // namespace
@@ -265,7 +268,7 @@ cudaError_t launch_affine_tma(const ZsRasterArgs &a, int sm_count, cudaStream_t 
     p.tiles = p.tiles_x * ((a.height + ZS_AT_TH - 1) / ZS_AT_TH);
     p.buf_bytes = (uint32_t)(((size_t)bw * bh * 8 + 127) & ~(size_t)127);
     p.pad = 0;
-    const size_t smem = 2 * (size_t)p.buf_bytes;
+    const size_t smem = ZS_AT_NBUF * (size_t)p.buf_bytes;
     cudaError_t e = cudaFuncSetAttribute(zs_affine_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int per_sm = 0;
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, zs_affine_tma_kernel, ZS_AT_THREADS, smem);
