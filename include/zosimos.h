@@ -362,6 +362,10 @@ int zs_env_bind(zs_environment *env, uint32_t reg, uint64_t key);
 /* Environment::knob (run.rs:1292-1306): the parameter block of `knob` for this launch only (len
  * must equal the knob's, else ZS_ERR_INVALID_ARG); launches without one use the static block. */
 int zs_env_knob(zs_environment *env, uint32_t knob, const void *data, uint64_t len);
+/* Environment::recover_buffers (run.rs:1312-1347): an executable keeps its intermediate device
+ * buffers between launches, so there is nothing to take from the pool; *bytes receives the
+ * bytes it already holds (RecoveredBufferStats::mem). */
+int zs_env_recover_buffers(zs_environment *env, uint64_t *bytes);
 /* Environment::bind_output (run.rs:1207): write the output into an existing image. */
 int zs_env_bind_output(zs_environment *env, uint32_t reg, uint64_t key);
 /* Executable::launch (run.rs:1016): consumes `env` (even on failure). */
@@ -370,8 +374,15 @@ int zs_launch(zs_executable *exe, zs_environment *env, zs_execution **out);
 int zs_exec_is_running(const zs_execution *exec);
 /* Execution::step (run.rs:1389): enqueue the next instruction. */
 int zs_exec_step(zs_execution *exec);
+/* Execution::step_to(StepLimits::new().with_steps(max_steps)) (run.rs:1394, 3000-3013):
+ * enqueue up to max_steps instructions (fewer at the end); *steps receives the count. */
+int zs_exec_step_to(zs_execution *exec, uint32_t max_steps, uint32_t *steps);
 /* SyncPoint::block_on (run.rs:3019): wait for everything enqueued so far. */
 int zs_exec_sync(zs_execution *exec);
+/* Retire::input (run.rs:2791): the pool key of the image bound to input `reg` (binding does
+ * not move the image out of the pool here, so it is the key given to zs_env_bind);
+ * ZS_ERR_BAD_REGISTER for a register that is no input (RetireError::NoSuchInput). */
+int zs_retire_input(zs_execution *exec, uint32_t reg, uint64_t *key);
 /* Retire::output (run.rs:2809): the output moves into the pool; returns its key. */
 int zs_retire_output(zs_execution *exec, uint32_t reg, uint64_t *key);
 /* Retire::finish (run.rs:2962): release the execution. */

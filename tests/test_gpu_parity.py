@@ -564,6 +564,38 @@ def test_pool_upload_device_resident_input():
     assert maxdiff(ours, P.oracle_chain(img)) <= LSB
 
 
+def test_step_to_retire_input_and_recover_buffers():
+    """Execution::step_to with StepLimits (run.rs:1394, 3000-3013), Retire::input (run.rs:2791)
+    and Environment::recover_buffers (run.rs:1312-1347) on a two-kernel program (blend +
+    bilinear resize, per-op FP32 so that an intermediate is held)."""
+    a = srgb_gradient_noise(64, 64, seed=23, image=0)
+    b = srgb_gradient_noise(64, 64, seed=23, image=1)
+    from zosimos_gb300.workloads import blend_resize
+    c, ia, ib, o = blend_resize(64, 64, 48, 48)
+    exe = zs.Linker.from_included().compile(c).lower_to(zs.Capabilities(mode=zs.Mode.PerOpF32))
+    pool = zs.Pool()
+    ka, kb = pool.insert_srgb(a), pool.insert_srgb(b)
+    for launch in range(2):
+        env = exe.from_pool(pool)
+        env.bind(ia, ka)
+        env.bind(ib, kb)
+        held = env.recover_buffers()
+        assert (held > 0) == (launch > 0)       # intermediates exist after the first launch
+        ex = exe.launch(env)
+        total = 0
+        while ex.is_running():
+            n = ex.step_to(2)
+            assert 1 <= n <= 2
+            total += n
+        assert ex.step_to(5) == 0 and total >= 2
+        assert ex.retire_input(ia) == ka and ex.retire_input(ib) == kb
+        with pytest.raises(zs.ZosimosError) as e:
+            ex.retire_input(o)
+        assert e.value.code == 3
+        got = pool.read(ex.retire_output(o))
+        assert maxdiff(got, P.oracle_blend_resize(a, b, (48, 48))) <= LSB
+
+
 def test_two_chain_executables_on_the_per_device_path():
     """Two executables whose chains use different kernel specialisations (with and without
     cube roots), lowered for the same device and launched alternately: each launcher sets

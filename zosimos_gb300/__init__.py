@@ -207,6 +207,8 @@ def _lib():
             "zs_tune_cache_save": ([ctypes.c_char_p], I32), "zs_tune_cache_load": ([ctypes.c_char_p], I32),
             "zs_executable_query_knob": ([P, U32, U32, pU32, pU64], I32),
             "zs_executable_set_knob": ([P, U32, P, U64], I32), "zs_env_knob": ([P, U32, P, U64], I32),
+            "zs_exec_step_to": ([P, U32, pU32], I32), "zs_retire_input": ([P, U32, pU64], I32),
+            "zs_env_recover_buffers": ([P, pU64], I32),
             "zs_cmd_generic": ([P, pU32], I32), "zs_cmd_input_generic": ([P, U32, pU32], I32),
             "zs_cmd_derive_descriptor": ([P, U32, U32, U32, pU32], I32),
             "zs_cmd_register_descriptor": ([P, U32, pU32], I32),
@@ -861,6 +863,12 @@ class Environment:
     def bind_output(self, reg: int, key: int) -> None:
         _check(_lib().zs_env_bind_output(self._h, reg, key))
 
+    def recover_buffers(self) -> int:
+        """Environment::recover_buffers: bytes of intermediate buffers the executable holds."""
+        n = ctypes.c_uint64()
+        _check(_lib().zs_env_recover_buffers(self._h, ctypes.byref(n)))
+        return n.value
+
     def knob(self, knob: int, data) -> None:
         """Environment::knob: this launch's parameter block for `knob`."""
         b = bytes(np.ascontiguousarray(data).view(np.uint8).reshape(-1)) if isinstance(data, np.ndarray) else bytes(data)
@@ -885,8 +893,19 @@ class Execution:
     def step(self) -> None:
         _check(_lib().zs_exec_step(self._h))
 
+    def step_to(self, max_steps: int) -> int:
+        """Execution::step_to(StepLimits::new().with_steps(max_steps)): steps enqueued."""
+        n = ctypes.c_uint32()
+        _check(_lib().zs_exec_step_to(self._h, max_steps, ctypes.byref(n)))
+        return n.value
+
     def sync(self) -> None:
         _check(_lib().zs_exec_sync(self._h))
+
+    def retire_input(self, reg: int) -> int:
+        key = ctypes.c_uint64()
+        _check(_lib().zs_retire_input(self._h, reg, ctypes.byref(key)))
+        return key.value
 
     def retire_output(self, reg: int) -> int:
         key = ctypes.c_uint64()

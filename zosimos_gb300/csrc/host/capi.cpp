@@ -830,6 +830,19 @@ int zs_exec_step(zs_execution *exec) {
     });
 }
 
+int zs_exec_step_to(zs_execution *exec, uint32_t max_steps, uint32_t *steps) {
+    return guarded([&] {
+        NEED(exec);
+        uint32_t n = 0;
+        while (n < max_steps && exec->x.cursor < exec->x.total) {
+            const int rc = zs_exec_step(exec);
+            if (rc != ZS_OK) fail(rc, last_error());
+            ++n;
+        }
+        if (steps) *steps = n;
+    });
+}
+
 int zs_exec_sync(zs_execution *exec) {
     return guarded([&] {
         NEED(exec);
@@ -837,6 +850,33 @@ int zs_exec_sync(zs_execution *exec) {
         uint32_t flags = 0;
         check_cuda(read_device_status(exec->x.exe->device, &flags, true), "device status");
         if (flags) fail(ZS_ERR_TIMEOUT, "a kernel's bounded wait on its bulk copies gave up");
+    });
+}
+
+int zs_retire_input(zs_execution *exec, uint32_t reg, uint64_t *key) {
+    return guarded([&] {
+        NEED(exec); NEED(key);
+        Execution &X = exec->x;
+        const Executable &E = *X.exe;
+        reg = flat_reg(E, 0, reg);
+        for (size_t i = 0; i < E.input_regs.size(); ++i)
+            if (E.input_regs[i] == reg) {
+                if (i >= X.input_keys.size() || !X.input_keys[i]) fail(ZS_ERR_MISSING_KEY, "input was not bound");
+                *key = X.input_keys[i];
+                return;
+            }
+        fail(ZS_ERR_BAD_REGISTER, "no such input register (RetireError::NoSuchInput)");
+    });
+}
+
+int zs_env_recover_buffers(zs_environment *env, uint64_t *bytes) {
+    return guarded([&] {
+        NEED(env);
+        const Executable &E = *env->env.exe;
+        uint64_t held = 0;
+        for (size_t i = 0; i < E.slots.size() && i < E.dev_buffers.size(); ++i)
+            if (E.dev_buffers[i] && E.slots[i].kind == SlotKind::Intermediate) held += E.slots[i].bytes;
+        if (bytes) *bytes = held;
     });
 }
 
