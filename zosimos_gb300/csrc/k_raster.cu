@@ -391,9 +391,6 @@ cudaError_t launch_raster(const ZsRasterArgs &args, int sm_count, cudaStream_t s
     if (args.producer == ZS_PR_AFFINE && args.bilinear && !args.raw_copy && !args.virt1 &&
         args.src[1].fmt.fast == ZS_FAST_F16X4 &&
         args.aff[6] == 0.f && args.aff[7] == 0.f && args.aff[8] == 1.f) {
-        // Tile footprints staged by TMA when the transform and the source layout allow.
-        const cudaError_t te = launch_affine_tma(args, sm_count, stream);
-        if (te != cudaErrorNotSupported) return te;
         int64_t blocks = (int64_t)((args.width + 31) / 32) * ((args.height + 15) / 16);
         const int64_t cap = (int64_t)(sm_count > 0 ? sm_count : 148) * 8;
         if (blocks > cap) blocks = cap;

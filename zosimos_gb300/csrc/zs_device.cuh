@@ -27,7 +27,7 @@ static __device__ uint32_t zs_srgb_encode_tab_shifted[ZS_ENCS_ENTRIES];
 static __device__ unsigned int zs_device_status_word;
 
 // The kernel files, one translation unit each (ZS_TU_HOOKS(name) in every one).
-#define ZS_DEVICE_TUS(X) X(raster) X(resample) X(resample_tc) X(chain) X(layers) X(batch) X(noalloc) X(selftest) X(affine_tma)
+#define ZS_DEVICE_TUS(X) X(raster) X(resample) X(resample_tc) X(chain) X(layers) X(batch) X(noalloc) X(selftest)
 
 #define ZS_TU_DECLARE_HOOKS(NAME)                                                                   \
     cudaError_t tu_upload_tables_##NAME(const float *dec, const uint32_t *enc, const uint32_t *encs); \

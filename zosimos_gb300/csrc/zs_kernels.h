@@ -25,9 +25,6 @@ cudaError_t launch_resample2d(const ZsRasterArgs &args, int sm_count, cudaStream
 // the source is RGBA16F with 16-byte aligned rows and the TMA encoder is available.
 bool resample_tc_usable(const ZsRasterArgs &args);
 cudaError_t launch_resample_tc(const ZsRasterArgs &args, int sm_count, cudaStream_t stream);
-// The RGBA16F affine bilinear gather with tile footprints staged by TMA (k_affine_tma.cu);
-// cudaErrorNotSupported when the transform or the source layout does not suit it.
-cudaError_t launch_affine_tma(const ZsRasterArgs &args, int sm_count, cudaStream_t stream);
 
 // Fused colour chain in canonical form, RGBA8 in / RGBA8 out (k_chain.cu).
 // Returns cudaErrorNotSupported when no specialisation exists for the formats or the buffers
