@@ -176,11 +176,12 @@ static cudaError_t launch_chain_t(const ZsChainArgs &args, int sm_count, cudaStr
     const size_t smem = sizeof(ZsChainSmem);
     // The shared-memory opt-in is a per-device attribute of the kernel: set it (and size the
     // grid) once per device and block size, on the device that is current for this launch.
-    // Block sizes: 1024 threads (one block per SM) or 512 (two blocks per SM), chosen by
-    // the autotuner; both run the same arithmetic per pixel.
-    static std::atomic<int> per_sm_of[ZS_MAX_DEVICES][2];
-    const int which = threads == 512 ? 1 : 0;
-    const int block = which ? 512 : ZS_CHAIN_THREADS;
+    // Block sizes: 1024 threads (one block per SM) or 512, chosen by the autotuner, and 256
+    // for the zero-copy host round trip (fewer host reads in flight); all run the same
+    // arithmetic per pixel.
+    static std::atomic<int> per_sm_of[ZS_MAX_DEVICES][3];
+    const int which = threads == 512 ? 1 : (threads == 256 ? 2 : 0);
+    const int block = which == 1 ? 512 : (which == 2 ? 256 : ZS_CHAIN_THREADS);
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
