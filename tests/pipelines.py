@@ -1,4 +1,4 @@
-"""The reference's own test pipelines (lib/zosimos/tests/blend.rs) and the BASELINE
+"""The reference's own test pipelines (lib/zosimos/tests/blend.rs) and the benchmark
 workloads, each expressed twice: through the executor's API (``ours_*``, runs on the
 GPU) and through the CPU oracle (``oracle_*``).  Both return texel bytes as
 (H, row_bytes) uint8 arrays (or float arrays for float outputs)."""
@@ -297,7 +297,7 @@ def oracle_lab_grid(space: str):
     return O.encode(O.SRGB_RGBA8, lab)
 
 
-# ---------------------------------------------------------------- the fused colour chain (config 2)
+# ---------------------------------------------------------------- the fused colour chain
 
 from zosimos_gb300.workloads import OKLAB_SCALE, color_chain as chain_commands  # noqa: E402
 
@@ -335,7 +335,7 @@ def rgb_cube_image() -> np.ndarray:
     return out
 
 
-# ---------------------------------------------------------------- batched uneven thumbnails (config 4)
+# ---------------------------------------------------------------- batched uneven thumbnails
 
 
 def fit_size(w, h, canvas):

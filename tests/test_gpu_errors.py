@@ -49,7 +49,7 @@ def lsb(a, b):
     return int(np.abs(a.astype(np.int16) - b.astype(np.int16)).max())
 
 
-# ---------------------------------------------------------------- config 2: the colour chain, stage by stage
+# ---------------------------------------------------------------- the colour chain, stage by stage
 
 LAB = dict(bits=Bits.Float32x4, parts=Parts.LabA, color=ColorKind.Oklab, transfer=Transfer.Linear)
 
@@ -120,17 +120,17 @@ def test_chain_stage_error(chain_case, stage, name, mode):
     k = pool.insert_srgb(img)
     got = P.run(c, pool, [(i, k)], [o], mode)[0]
     if stage == 7:
-        record("2 colour chain", STAGES[stage - 1], name, lsb(got.reshape(h, w * 4), ref[6].reshape(h, w * 4)), "lsb", 1)
+        record("colour chain (512 x 4096)", STAGES[stage - 1], name, lsb(got.reshape(h, w * 4), ref[6].reshape(h, w * 4)), "lsb", 1)
         return
     got = np.frombuffer(got, np.float32).reshape(h, w, 4).astype(np.float64)
     err = float(np.abs(got[..., :3] - ref[stage - 1][..., :3]).max())
     # A program that ends in an FP32 output stores nothing else in fused mode; the per-op FP16
     # programs store every intermediate as FP16.
     bound = (STAGE_TOL_F16 if mode == zs.Mode.PerOpF16 else STAGE_TOL)[stage - 1]
-    record("2 colour chain", STAGES[stage - 1], name, err, "abs", bound)
+    record("colour chain (512 x 4096)", STAGES[stage - 1], name, err, "abs", bound)
 
 
-# ---------------------------------------------------------------- config 1: decode, blend, bilinear resize
+# ---------------------------------------------------------------- two 512^2 images: decode, blend, bilinear resize
 
 
 @pytest.mark.parametrize("name,mode", MODES)
@@ -138,10 +138,10 @@ def test_blend_resize_error(name, mode):
     a = srgb_gradient_noise(512, 512, seed=1, image=0)
     b = srgb_gradient_noise(512, 512, seed=1, image=1)
     got = P.ours_blend_resize(a, b, mode=mode)
-    record("1 blend + resize", "over + bilinear 512->384 (sRGB8)", name, lsb(got, P.oracle_blend_resize(a, b)), "lsb", 1)
+    record("blend + resize (2 x 512^2)", "over + bilinear 512->384 (sRGB8)", name, lsb(got, P.oracle_blend_resize(a, b)), "lsb", 1)
 
 
-# ---------------------------------------------------------------- config 3: resample sweep and rotation
+# ---------------------------------------------------------------- resample sweep and rotation
 
 
 @pytest.fixture(scope="module")
@@ -162,7 +162,7 @@ def test_resample_error(img2k, filt, fname, factor, name, mode, simt):
     ow = int(round(2048 / factor))
     got = P.ours_resample(img, (ow, ow), filt, mode, simt)
     err = float(np.abs(got - O.resample(img64, ow, ow, filt)).max())
-    record("3 resample (RGBA16F 2048^2)", f"{fname} /{factor:g}", name, err, "abs", F16_TOL)
+    record("resample (RGBA16F 2048^2)", f"{fname} /{factor:g}", name, err, "abs", F16_TOL)
 
 
 @pytest.mark.parametrize("name,mode", MODES)
@@ -170,10 +170,10 @@ def test_rotation_error(img2k, name, mode):
     img, _ = img2k
     got = P.ours_rotation(img, 17.0, mode)
     err = float(np.abs(got - P.oracle_rotation(img, 17.0)).max())
-    record("3 resample (RGBA16F 2048^2)", "17 deg bilinear rotation", name, err, "abs", F16_TOL)
+    record("resample (RGBA16F 2048^2)", "17 deg bilinear rotation", name, err, "abs", F16_TOL)
 
 
-# ---------------------------------------------------------------- config 4: thumbnails
+# ---------------------------------------------------------------- thumbnails
 
 
 def test_thumbnail_batch_error():
@@ -181,7 +181,7 @@ def test_thumbnail_batch_error():
     images = [srgb_gradient_noise(int(w), int(h), seed=4, image=i) for i, (w, h) in enumerate(zip(ws[:64], hs[:64]))]
     got = P.ours_thumbnails(images)
     ref = P.oracle_thumbnails(images)
-    record("4 thumbnails (64 of the 1024)", "chain + box fit + canvas (sRGB8)", "fused batch kernel",
+    record("thumbnails (64 of the 1024)", "chain + box fit + canvas (sRGB8)", "fused batch kernel",
            max(lsb(g, r) for g, r in zip(got, ref)), "lsb", 1)
 
 
@@ -191,10 +191,10 @@ def test_thumbnail_program_error(name, mode):
     images = [srgb_gradient_noise(int(w), int(h), seed=4, image=i) for i, (w, h) in enumerate(zip(ws[:8], hs[:8]))]
     ref = P.oracle_thumbnails(images)
     err = max(lsb(P.ours_thumbnail_program(im, mode=mode), r) for im, r in zip(images, ref))
-    record("4 thumbnails (8 of the 1024)", "one program per image (sRGB8)", name, err, "lsb", 1)
+    record("thumbnails (8 of the 1024)", "one program per image (sRGB8)", name, err, "lsb", 1)
 
 
-# ---------------------------------------------------------------- config 5: layer stack
+# ---------------------------------------------------------------- layer stack
 
 
 @pytest.mark.parametrize("name,mode", MODES)
@@ -204,4 +204,4 @@ def test_layer_stack_error(name, mode):
     transforms = layer_transforms(n, seed=5)
     got = P.ours_layer_stack(layers, transforms, mode)
     err = float(np.abs(got - P.oracle_layer_stack(layers, transforms)).max())
-    record("5 layers (8 x 1024^2)", "affine bilinear + over/multiply/screen/add (RGBA16F)", name, err, "abs", F16_TOL)
+    record("layers (8 x 1024^2)", "affine bilinear + over/multiply/screen/add (RGBA16F)", name, err, "abs", F16_TOL)

@@ -34,7 +34,7 @@ def bands(n, rows=16):
     return [(0, rows), (n // 2 - rows // 2, n // 2 + rows // 2), (n - rows, n)]
 
 
-# ---------------------------------------------------------------- config 2: every RGB triple
+# ---------------------------------------------------------------- colour chain, 4096^2: every RGB triple
 
 
 @pytest.fixture(scope="module")
@@ -79,7 +79,7 @@ def test_chain_every_rgb_triple_per_op(cube, mode):
     _check_cube(img, got, ref)
 
 
-# ---------------------------------------------------------------- config 3: 8192^2 resample sweep
+# ---------------------------------------------------------------- resample sweep of an 8192^2 RGBA16F image
 
 
 @pytest.fixture(scope="module")
@@ -132,7 +132,7 @@ def test_rotation_8192(big16, mode):
         assert np.abs(got[y0:y1] - P.oracle_rotation_rows(img64, 17.0, y0, y1)).max() <= F16_TOL, (y0, y1)
 
 
-# ---------------------------------------------------------------- config 5: 32 distinct layers
+# ---------------------------------------------------------------- layer stack: 32 distinct 4096^2 layers
 
 
 @pytest.mark.parametrize("mode", [zs.Mode.Fused, zs.Mode.PerOpF32])
@@ -158,7 +158,7 @@ def test_layer_stack_32_distinct_4096(mode):
         assert np.abs(got[y0:y1] - exact).max() <= F16_TOL, (y0, y1)
 
 
-# ---------------------------------------------------------------- config 4: 1024 thumbnails
+# ---------------------------------------------------------------- 1024 uneven thumbnails
 
 
 def test_thumbnails_1024_all_images():
