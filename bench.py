@@ -483,6 +483,12 @@ def workload_resample(args, stream, sh):
                     zs.Capabilities(mode=zs.Mode.Fused, simt_resample=True)]
             exes = [zs.Linker.from_included().compile(c).lower_to(cp) for cp in caps]
             dst = zs.DeviceBuffer(ow * ow * 8)
+            tile = None
+            if "tensor cores" in exes[0].describe():
+                # the tile width of the tensor-core kernel, tuned on these buffers (outside the
+                # timed region; every candidate computes the same bytes)
+                exes[0].autotune([src.ptr], [dst.ptr], sh, reps=3)
+                tile = exes[0].get_launch(zs.Tune.ResampleTile)
             ms0, clocks = _clocked(timed, lambda i, e=exes[0]: e.run_device([src.ptr], [dst.ptr], sh), steps,
                                    args.warmup)
             ms = [ms0] + [timed(lambda i, e=e: e.run_device([src.ptr], [dst.ptr], sh), steps, args.warmup)
@@ -491,7 +497,8 @@ def workload_resample(args, stream, sh):
             _line(f"resample {fname} 8192^2 RGBA16F /{factor} -> {ow}^2", n * n, n * n * 8 + ow * ow * 8,
                   ms[0], ms[1], clocks,
                   {"kernel": "tcgen05 band MMA + TMEM epilogue" if tensor else "FP32 SIMT tiled",
-                   "fused_simt_fp32_ms": round(ms[2], 4)})
+                   "fused_simt_fp32_ms": round(ms[2], 4),
+                   "autotune": {"tile_output_columns": tile}})
             dst.free()
     c, _, _, _ = rotation(n, n, 17.0)
     exes = [zs.Linker.from_included().compile(c).lower_to(zs.Capabilities(mode=m))

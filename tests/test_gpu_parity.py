@@ -564,6 +564,30 @@ def test_pool_upload_device_resident_input():
     assert maxdiff(ours, P.oracle_chain(img)) <= LSB
 
 
+def test_resample_tile_widths_give_identical_bytes():
+    """Every tile width the tensor-core resample fits (the autotuner's candidates) computes the
+    same bytes, and the autotuner keeps one of them."""
+    img = P.f16_bytes(np.random.default_rng(31).random((700, 900, 4)).astype(np.float16))
+    from zosimos_gb300.workloads import resample as resample_cmds
+    c, _, _ = resample_cmds(900, 700, 450, 350, zs.Filter.Lanczos3)
+    exe = zs.Linker.from_included().compile(c).lower_to()
+    assert "tensor cores" in exe.describe()
+    src, dst = zs.DeviceBuffer(img.nbytes), zs.DeviceBuffer(450 * 350 * 8)
+    src.upload(img)
+    outs = []
+    for tw in (8, 16, 32):
+        exe.set_launch(zs.Tune.ResampleTile, tw)
+        exe.run_device([src.ptr], [dst.ptr])
+        zs.device_synchronize()
+        outs.append(dst.download(np.empty((350, 450 * 8), np.uint8)))
+    assert all((o == outs[0]).all() for o in outs[1:])
+    exe.autotune([src.ptr], [dst.ptr], reps=3)
+    assert exe.get_launch(zs.Tune.ResampleTile) in (8, 16, 32)
+    exe.run_device([src.ptr], [dst.ptr])
+    zs.device_synchronize()
+    assert (dst.download(np.empty((350, 450 * 8), np.uint8)) == outs[0]).all()
+
+
 def test_step_to_retire_input_and_recover_buffers():
     """Execution::step_to with StepLimits (run.rs:1394, 3000-3013), Retire::input (run.rs:2791)
     and Environment::recover_buffers (run.rs:1312-1347) on a two-kernel program (blend +

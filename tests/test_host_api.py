@@ -318,6 +318,21 @@ def test_tuning_cache_and_keys(tmp_path):
         exe.set_launch(zs.Tune.BatchRows, 17)
     assert e.value.code == 10
     assert exe.tune_key(zs.Tune.BatchThreads, 256).startswith("batch_threads/flags")
+    # the tensor-core resample's tile width: the planned width, candidates only
+    rc, _, _ = resample(1024, 1024, 512, 512, zs.Filter.Lanczos3)
+    rexe = lower(rc)
+    assert "tensor cores" in rexe.describe()
+    assert rexe.get_launch(zs.Tune.ResampleTile) == 16
+    assert rexe.tune_key(zs.Tune.ResampleTile).startswith("resample_tc/taps")
+    for tw in (8, 32, 16):
+        rexe.set_launch(zs.Tune.ResampleTile, tw)
+        assert rexe.get_launch(zs.Tune.ResampleTile) == tw
+    with pytest.raises(ZosimosError) as e:
+        rexe.set_launch(zs.Tune.ResampleTile, 24)
+    assert e.value.code == 10
+    with pytest.raises(ZosimosError) as e:
+        exe.set_launch(zs.Tune.ResampleTile, 16)          # the chain has no resample step
+    assert e.value.code == 2
     exe.set_launch(zs.Tune.BatchThreads, 640)
     assert exe.get_launch(zs.Tune.BatchThreads) == 640
     with pytest.raises(ZosimosError) as e:

@@ -5,6 +5,8 @@
 //
 // Tunables (every candidate runs the same arithmetic per pixel, so results are byte-identical):
 //  * the colour-chain kernel's block size: 1024 threads (one block per SM) or 512 (two);
+//  * the tensor-core resample's tile width (8, 16 or 32 output columns, each with the atoms its
+//    source span needs; the same MMAs and taps per output pixel, so the same bytes);
 //  * the batched-thumbnail kernel's work-item height, 1, 2, 4, 8 or 16 (a streaming item covers
 //    about 16 x that many source rows: taller items share fewer boundary rows between items,
 //    shorter ones balance the warps better), and its block size, 768 or 640 threads (one block
@@ -103,11 +105,37 @@ std::string batch_tune_key(const Executable &E, uint32_t canvas, int device, con
     return os.str();
 }
 
+// Tensor-core resample steps: the horizontal tap count, log2 size classes of the source and
+// output widths, and the device.
+std::string resample_tune_key(const Step &st, int device) {
+    std::ostringstream os;
+    const ZsRasterArgs &a = st.raster;
+    os << "resample_tc/taps" << a.taps << "/src2^" << (int)std::floor(std::log2((double)std::max(a.src[0].width, 1)))
+       << "/dst2^" << (int)std::floor(std::log2((double)std::max(a.width, 1))) << '/' << device_key(device);
+    return os.str();
+}
+
+bool set_resample_tile(Step &st, int tw) {
+    for (const auto &c : st.tc_cands)
+        if (c.first == tw) {
+            st.raster.tc_tw = c.first;
+            st.raster.tc_atoms = c.second;
+            return true;
+        }
+    return false;
+}
+
+static bool is_tc_resample(const Step &st) {
+    return st.kind == StepKind::Raster && st.raster.producer == ZS_PR_RESAMPLE_2D && st.raster.tc_tw > 0 &&
+           !st.tc_cands.empty();
+}
+
 // Tuned values of an executable's steps from the cache (called once its device is known).
 void apply_tuned(Executable &E) {
     for (Step &st : E.steps) {
         int v;
         if (st.kind == StepKind::Chain && !st.tune_threads && tune_get(chain_tune_key(st, E.device), v)) st.tune_threads = v;
+        if (is_tc_resample(st) && tune_get(resample_tune_key(st, E.device), v)) set_resample_tile(st, v);
     }
 }
 
@@ -139,12 +167,30 @@ static float time_step(Executable &E, const std::vector<void *> &ptrs, size_t k,
     return ms[ms.size() / 2];
 }
 
-// Tunes every chain step of E on the given buffers; returns the chosen block size of the
-// last one (0 when E has no chain step).
+// Tunes every chain step (block size) and tensor-core resample step (tile width) of E on the
+// given buffers; returns the chosen block size of the last chain step (0 when E has none).
 int autotune_steps(Executable &E, const std::vector<void *> &ptrs, cudaStream_t s, uint32_t reps) {
     int chosen = 0;
     for (size_t k = 0; k < E.steps.size(); ++k) {
         Step &st = E.steps[k];
+        if (is_tc_resample(st) && st.tc_cands.size() > 1) {
+            int best = st.raster.tc_tw;
+            float best_ms = 0.f;
+            bool first = true;
+            const std::vector<std::pair<int, int>> cands = st.tc_cands;
+            for (const auto &c : cands) {
+                set_resample_tile(st, c.first);
+                const float t = time_step(E, ptrs, k, s, reps);
+                if (first || t < best_ms) {
+                    best = c.first;
+                    best_ms = t;
+                    first = false;
+                }
+            }
+            set_resample_tile(st, best);
+            tune_put(resample_tune_key(st, E.device), best);
+            continue;
+        }
         if (st.kind != StepKind::Chain) continue;
         int best = 1024;
         float best_ms = 0.f;

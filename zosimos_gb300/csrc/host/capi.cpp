@@ -1344,6 +1344,17 @@ int zs_executable_set_launch(zs_executable *exe, uint32_t param, int32_t value) 
         } else if (param == ZS_TUNE_BATCH_THREADS) {
             if (value != 768 && value != 640) fail(ZS_ERR_INVALID_ARG, "batch block size must be 768 or 640");
             E.batch_threads = value;
+        } else if (param == ZS_TUNE_RESAMPLE_TILE) {
+            bool any = false;
+            for (Step &st : E.steps)
+                if (!st.tc_cands.empty()) {
+                    if (!set_resample_tile(st, value)) fail(ZS_ERR_INVALID_ARG, "not a tile width this resample fits");
+                    any = true;
+                }
+            if (!any) fail(ZS_ERR_UNIMPLEMENTED, "the executable has no tensor-core resample step");
+            for (auto &kv : E.graphs) cudaGraphExecDestroy(kv.second);
+            E.graphs.clear();
+            E.graph_order.clear();
         } else {
             fail(ZS_ERR_INVALID_ARG, "unknown launch parameter");
         }
@@ -1362,6 +1373,10 @@ int zs_executable_get_launch(const zs_executable *exe, uint32_t param, int32_t *
             *value = E.batch_rows;
         } else if (param == ZS_TUNE_BATCH_THREADS) {
             *value = E.batch_threads;
+        } else if (param == ZS_TUNE_RESAMPLE_TILE) {
+            *value = 0;
+            for (const Step &st : E.steps)
+                if (!st.tc_cands.empty()) *value = st.raster.tc_tw;
         } else {
             fail(ZS_ERR_INVALID_ARG, "unknown launch parameter");
         }
@@ -1386,6 +1401,10 @@ int zs_executable_tune_key(const zs_executable *exe, uint32_t param, uint32_t ca
             copy_string(batch_tune_key(E, canvas, E.device), buf, len);
         } else if (param == ZS_TUNE_BATCH_THREADS) {
             copy_string(batch_tune_key(E, canvas, E.device, "batch_threads"), buf, len);
+        } else if (param == ZS_TUNE_RESAMPLE_TILE) {
+            for (const Step &st : E.steps)
+                if (!st.tc_cands.empty()) return copy_string(resample_tune_key(st, E.device), buf, len);
+            fail(ZS_ERR_UNIMPLEMENTED, "the executable has no tensor-core resample step");
         } else {
             fail(ZS_ERR_INVALID_ARG, "unknown launch parameter");
         }

@@ -28,6 +28,7 @@ struct Pending {
     int idx_x_slot = -1, idx_y_slot = -1, weight_slot = -1;
     int vfirst_slot = -1, vcount_slot = -1, vweight_slot = -1;
     int vimg_slot = -1, vimg_index_slot = -1;
+    std::vector<std::pair<int, int>> tc_cands;   // tensor-core tiles that fit: (tile width, atoms)
     HProgram prog;
     // virt1: the gathered image's producer sources and program (evaluated per tap)
     int vsrc_slot[2] = {-1, -1};
@@ -249,6 +250,7 @@ struct Planner {
         st.vweight_slot = p.vweight_slot;
         st.vimg_slot = p.vimg_slot;
         st.vimg_index_slot = p.vimg_index_slot;
+        st.tc_cands = p.tc_cands;
         // Pixel program: FP64 host program -> FP32 parameters.
         ZsPixelProgram &pp = st.raster.prog;
         std::memset(&pp, 0, sizeof(pp));
@@ -1051,22 +1053,26 @@ struct Planner {
         // Prefer tiles whose span fits 4 atoms (two accumulators: the epilogue of one tile
         // overlaps the MMAs of the next), else up to 8 atoms (one 512-column accumulator).
         int tw = 0, span = 0;
+        std::vector<std::pair<int, int>> cands;      // every tile width that fits 8 atoms
+        for (int cand : {32, 16, 8}) {
+            int sp = 0;
+            for (int x0 = 0; x0 < dw; x0 += cand) {
+                const int x1 = std::min(x0 + cand, dw) - 1;
+                sp = std::max(sp, hf[x1] + hc[x1] - (hf[x0] & ~1));
+            }
+            if (sp * 4 <= 64 * ZS_TC_MAX_ATOMS) cands.push_back({cand, (sp * 4 + 63) / 64});
+        }
         for (int max_atoms : {4, ZS_TC_MAX_ATOMS}) {
-            for (int cand : {32, 16, 8}) {
-                int sp = 0;
-                for (int x0 = 0; x0 < dw; x0 += cand) {
-                    const int x1 = std::min(x0 + cand, dw) - 1;
-                    sp = std::max(sp, hf[x1] + hc[x1] - (hf[x0] & ~1));
-                }
-                if (sp * 4 <= 64 * max_atoms) {
-                    tw = cand;
-                    span = sp;
+            for (const auto &c : cands)
+                if (c.second <= max_atoms) {
+                    tw = c.first;
+                    span = c.second * 64 / 4;
                     break;
                 }
-            }
             if (tw) break;
         }
         if (!tw) return;
+        p.tc_cands = cands;
         const int bands = (dh + ZS_TC_M - 1) / ZS_TC_M;
         std::vector<int32_t> index(2 * (size_t)bands);
         std::vector<uint16_t> img;
@@ -1093,7 +1099,7 @@ struct Planner {
         p.vimg_slot = table_slot(img.data(), img.size() * 2);
         p.vimg_index_slot = table_slot(index.data(), index.size() * 4);
         p.a.tc_tw = tw;
-        p.a.tc_atoms = (span * 4 + 63) / 64;
+        p.a.tc_atoms = (span * 4 + 63) / 64;   // the candidate's atoms (span rounded to atoms above)
         p.label = "resample 2d [tensor cores: f16 band matrices, FP32 accumulation]";
     }
 

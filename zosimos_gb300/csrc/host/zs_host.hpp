@@ -214,6 +214,9 @@ struct Step {
     uint64_t copy_rows = 0;
     int64_t copy_src_pitch = 0, copy_dst_pitch = 0;
     int tune_threads = 0;        // Chain: block size chosen by the autotuner (0: default)
+    // RESAMPLE_2D on the tensor cores: the tile widths that fit, with their atoms; the
+    // autotuner picks among them (raster.tc_tw / tc_atoms hold the choice).
+    std::vector<std::pair<int, int>> tc_cands;
     uint32_t dyn_op = 0;         // Dynamic: registered op; src_slot[0..1] RGBA32F operands,
     int dyn_uniform_slot = -1;   //   dst_slot an RGBA32F result, uniforms in this table slot
     std::string label;
@@ -305,6 +308,11 @@ std::string device_key(int device);
 std::string chain_tune_key(const Step &st, int device);
 // `family`: "batch" (work-item height) or "batch_threads" (block size).
 std::string batch_tune_key(const Executable &E, uint32_t canvas, int device, const char *family = "batch");
+// Tensor-core resample steps: filter taps, source and output size classes.
+std::string resample_tune_key(const Step &st, int device);
+// Sets the tile width of a tensor-core resample step to one of its candidates; false when
+// the width is not one.
+bool set_resample_tile(Step &st, int tw);
 // Tuned values of the executable's steps from the process-wide cache.
 void apply_tuned(Executable &E);
 // Times the candidates of every tunable step on these buffers and keeps the fastest.
