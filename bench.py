@@ -337,7 +337,9 @@ def run_ours(args, rank, world, dist):
                    "parallelism": f"replicas x{world}",
                    "launch": "one kernel per step, launched directly with programmatic dependent launch "
                              "(multi-kernel executables replay CUDA graphs)",
-                   "autotune": {"chain_threads_per_block": chain_threads, "key": tune_key}},
+                   "autotune": {"chain_threads_per_block": chain_threads,
+                                "chain_vectors_per_iteration": fused.get_launch(zs.Tune.ChainVectors),
+                                "key": tune_key}},
         "plain_per_op_fp32": {"value": round(aggregate_mpix(world, NPX, ms_plain * 1e-3), 1), "unit": "Mpix/s",
                               "ms_per_step": round(ms_plain, 4), "kernels": plain.kernel_count()},
         "per_op_fp16": {"value": round(aggregate_mpix(world, NPX, ms_plain16 * 1e-3), 1), "unit": "Mpix/s",

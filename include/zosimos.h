@@ -470,8 +470,10 @@ enum {
     ZS_TUNE_BATCH_ROWS = 1,      /* batched thumbnails: work-item height, 1..16 (about 16 x value
                                     source rows per item; value output rows for upscaled images) */
     ZS_TUNE_BATCH_THREADS = 2,   /* batched thumbnails: block size, 768 or 640 (one block per SM) */
-    ZS_TUNE_RESAMPLE_TILE = 3    /* tensor-core resample: output columns per tile, 8, 16 or 32 (those
+    ZS_TUNE_RESAMPLE_TILE = 3,   /* tensor-core resample: output columns per tile, 8, 16 or 32 (those
                                     whose source span fits the kernel) */
+    ZS_TUNE_CHAIN_VECTORS = 4    /* colour-chain kernel: 16-byte vectors (4 pixels each) per thread
+                                    and loop iteration, 2 or 1 */
 };
 /* Times the candidates of every tunable launch of `exe` (CUDA events, median of `reps`
  * launches each) on the given device buffers -- which receive the result -- and keeps the

@@ -735,13 +735,15 @@ def test_autotune_candidates_are_byte_identical():
     src.upload(P.rgba_bytes(img))
     outs = []
     for t in (1024, 512):
-        exe.set_launch(zs.Tune.ChainThreads, t)
-        exe.run_device([src.ptr], [dst.ptr])
-        zs.device_synchronize()
-        outs.append(dst.download(np.empty((768, 4096), np.uint8)))
-    assert (outs[0] == outs[1]).all()
+        for vec in (2, 1):
+            exe.set_launch(zs.Tune.ChainThreads, t)
+            exe.set_launch(zs.Tune.ChainVectors, vec)
+            exe.run_device([src.ptr], [dst.ptr])
+            zs.device_synchronize()
+            outs.append(dst.download(np.empty((768, 4096), np.uint8)))
+    assert all((o == outs[0]).all() for o in outs[1:])
     chosen = exe.autotune([src.ptr], [dst.ptr], reps=5)
-    assert chosen in (1024, 512)
+    assert chosen in (1024, 512) and exe.get_launch(zs.Tune.ChainVectors) in (1, 2)
     again = zs.Linker.from_included().compile(c).lower_to()
     again.run_device([src.ptr], [dst.ptr])            # first use reads the cache
     assert again.get_launch(zs.Tune.ChainThreads) == chosen

@@ -309,6 +309,13 @@ def test_tuning_cache_and_keys(tmp_path):
     assert parts[0] == "chain" and parts[1].startswith("flags") and parts[2] == "px2^24"
     assert exe.tune_key(zs.Tune.BatchRows, 256).startswith("batch/flags")
     assert exe.get_launch(zs.Tune.ChainThreads) == 1024          # untuned default
+    assert exe.get_launch(zs.Tune.ChainVectors) == 2
+    assert exe.tune_key(zs.Tune.ChainVectors).startswith("chain_vectors/flags")
+    exe.set_launch(zs.Tune.ChainVectors, 1)
+    assert exe.get_launch(zs.Tune.ChainVectors) == 1
+    with pytest.raises(ZosimosError) as e:
+        exe.set_launch(zs.Tune.ChainVectors, 3)
+    assert e.value.code == 10
     exe.set_launch(zs.Tune.ChainThreads, 512)
     assert exe.get_launch(zs.Tune.ChainThreads) == 512
     with pytest.raises(ZosimosError) as e:

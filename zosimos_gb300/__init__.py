@@ -89,7 +89,7 @@ class Mode:
 
 class Tune:
     """Launch parameters the autotuner chooses (ZS_TUNE_*)."""
-    ChainThreads, BatchRows, BatchThreads, ResampleTile = range(4)
+    ChainThreads, BatchRows, BatchThreads, ResampleTile, ChainVectors = range(5)
 
 
 STATUS = {0: "ok", 1: "type error", 2: "unimplemented", 3: "bad register", 4: "other", 5: "launch error",

@@ -4,7 +4,8 @@
 // a text file so that later processes start tuned.
 //
 // Tunables (every candidate runs the same arithmetic per pixel, so results are byte-identical):
-//  * the colour-chain kernel's block size: 1024 threads (one block per SM) or 512 (two);
+//  * the colour-chain kernel's block size, 1024 threads (one block per SM) or 512, and its
+//    16-byte vectors per thread and loop iteration, 2 or 1;
 //  * the tensor-core resample's tile width (8, 16 or 32 output columns, each with the atoms its
 //    source span needs; the same MMAs and taps per output pixel, so the same bytes);
 //  * the batched-thumbnail kernel's work-item height, 1, 2, 4, 8 or 16 (a streaming item covers
@@ -96,6 +97,8 @@ std::string chain_tune_key(const Step &st, int device) {
     return os.str();
 }
 
+std::string chain_vectors_key(const Step &st, int device) { return "chain_vectors/" + chain_tune_key(st, device).substr(6); }
+
 std::string batch_tune_key(const Executable &E, uint32_t canvas, int device, const char *family) {
     int flags = 0;
     for (const Step &st : E.steps)
@@ -135,6 +138,9 @@ void apply_tuned(Executable &E) {
     for (Step &st : E.steps) {
         int v;
         if (st.kind == StepKind::Chain && !st.tune_threads && tune_get(chain_tune_key(st, E.device), v)) st.tune_threads = v;
+        if (st.kind == StepKind::Chain && !st.tune_vectors && tune_get(chain_vectors_key(st, E.device), v) &&
+            (v == 1 || v == 2))
+            st.tune_vectors = v;
         if (is_tc_resample(st) && tune_get(resample_tune_key(st, E.device), v)) set_resample_tile(st, v);
     }
 }
@@ -192,18 +198,25 @@ int autotune_steps(Executable &E, const std::vector<void *> &ptrs, cudaStream_t 
             continue;
         }
         if (st.kind != StepKind::Chain) continue;
-        int best = 1024;
+        int best = 1024, best_vec = 2;
         float best_ms = 0.f;
-        for (int cand : {1024, 512}) {
-            st.tune_threads = cand;
-            const float t = time_step(E, ptrs, k, s, reps);
-            if (cand == 1024 || t < best_ms) {
-                best = cand;
-                best_ms = t;
+        bool first = true;
+        for (int cand : {1024, 512})
+            for (int vec : {2, 1}) {
+                st.tune_threads = cand;
+                st.tune_vectors = vec;
+                const float t = time_step(E, ptrs, k, s, reps);
+                if (first || t < best_ms) {
+                    best = cand;
+                    best_vec = vec;
+                    best_ms = t;
+                    first = false;
+                }
             }
-        }
         st.tune_threads = best;
+        st.tune_vectors = best_vec;
         tune_put(chain_tune_key(st, E.device), best);
+        tune_put(chain_vectors_key(st, E.device), best_vec);
         chosen = best;
     }
     // Captured graphs hold the old launch parameters.

@@ -991,7 +991,7 @@ static bool run_host_striped(zs_executable *exe, const void *const *inputs, void
         c.dst = dout + p0 * 4;
         c.npx = n;
         check_cuda(launch_chain(c, st.chain_src_fast, st.chain_dst_fast, E.sm_count, t,
-                                st.tune_threads ? st.tune_threads : 1024),
+                                st.tune_threads ? st.tune_threads : 1024, st.tune_vectors ? st.tune_vectors : 2),
                    st.label.c_str());
         check_cuda(cudaMemcpyAsync(hout + p0 * 4, dout + p0 * 4, n * 4, cudaMemcpyDeviceToHost, t), "d2h");
     }
@@ -1344,6 +1344,13 @@ int zs_executable_set_launch(zs_executable *exe, uint32_t param, int32_t value) 
         } else if (param == ZS_TUNE_BATCH_THREADS) {
             if (value != 768 && value != 640) fail(ZS_ERR_INVALID_ARG, "batch block size must be 768 or 640");
             E.batch_threads = value;
+        } else if (param == ZS_TUNE_CHAIN_VECTORS) {
+            if (value != 1 && value != 2) fail(ZS_ERR_INVALID_ARG, "chain vectors per iteration must be 1 or 2");
+            for (Step &st : E.steps)
+                if (st.kind == StepKind::Chain) st.tune_vectors = value;
+            for (auto &kv : E.graphs) cudaGraphExecDestroy(kv.second);
+            E.graphs.clear();
+            E.graph_order.clear();
         } else if (param == ZS_TUNE_RESAMPLE_TILE) {
             bool any = false;
             for (Step &st : E.steps)
@@ -1373,6 +1380,10 @@ int zs_executable_get_launch(const zs_executable *exe, uint32_t param, int32_t *
             *value = E.batch_rows;
         } else if (param == ZS_TUNE_BATCH_THREADS) {
             *value = E.batch_threads;
+        } else if (param == ZS_TUNE_CHAIN_VECTORS) {
+            *value = 0;
+            for (const Step &st : E.steps)
+                if (st.kind == StepKind::Chain) *value = st.tune_vectors ? st.tune_vectors : 2;
         } else if (param == ZS_TUNE_RESAMPLE_TILE) {
             *value = 0;
             for (const Step &st : E.steps)
@@ -1401,6 +1412,10 @@ int zs_executable_tune_key(const zs_executable *exe, uint32_t param, uint32_t ca
             copy_string(batch_tune_key(E, canvas, E.device), buf, len);
         } else if (param == ZS_TUNE_BATCH_THREADS) {
             copy_string(batch_tune_key(E, canvas, E.device, "batch_threads"), buf, len);
+        } else if (param == ZS_TUNE_CHAIN_VECTORS) {
+            for (const Step &st : E.steps)
+                if (st.kind == StepKind::Chain) return copy_string(chain_vectors_key(st, E.device), buf, len);
+            fail(ZS_ERR_UNIMPLEMENTED, "the executable has no chain step");
         } else if (param == ZS_TUNE_RESAMPLE_TILE) {
             for (const Step &st : E.steps)
                 if (!st.tc_cands.empty()) return copy_string(resample_tune_key(st, E.device), buf, len);

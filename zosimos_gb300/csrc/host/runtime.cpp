@@ -160,7 +160,8 @@ void Executable::record_range(cudaStream_t stream, const std::vector<void *> &pt
             c.src = (const uint8_t *)ptrs[st.src_slot[0]];
             c.dst = (uint8_t *)ptrs[st.dst_slot];
             const cudaError_t e =
-                launch_chain(c, st.chain_src_fast, st.chain_dst_fast, sm_count, stream, st.tune_threads ? st.tune_threads : 1024);
+                launch_chain(c, st.chain_src_fast, st.chain_dst_fast, sm_count, stream, st.tune_threads ? st.tune_threads : 1024,
+                             st.tune_vectors ? st.tune_vectors : 2);
             if (e != cudaErrorNotSupported) {
                 check_cuda(e, st.label.c_str());
                 break;

@@ -214,6 +214,7 @@ struct Step {
     uint64_t copy_rows = 0;
     int64_t copy_src_pitch = 0, copy_dst_pitch = 0;
     int tune_threads = 0;        // Chain: block size chosen by the autotuner (0: default)
+    int tune_vectors = 0;        // Chain: 16-byte vectors per thread and iteration (0: default 2)
     // RESAMPLE_2D on the tensor cores: the tile widths that fit, with their atoms; the
     // autotuner picks among them (raster.tc_tw / tc_atoms hold the choice).
     std::vector<std::pair<int, int>> tc_cands;
@@ -308,6 +309,8 @@ std::string device_key(int device);
 std::string chain_tune_key(const Step &st, int device);
 // `family`: "batch" (work-item height) or "batch_threads" (block size).
 std::string batch_tune_key(const Executable &E, uint32_t canvas, int device, const char *family = "batch");
+// Chain steps: the key of the vectors-per-iteration choice.
+std::string chain_vectors_key(const Step &st, int device);
 // Tensor-core resample steps: filter taps, source and output size classes.
 std::string resample_tune_key(const Step &st, int device);
 // Sets the tile width of a tensor-core resample step to one of its candidates; false when

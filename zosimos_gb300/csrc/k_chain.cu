@@ -89,7 +89,9 @@ __device__ __forceinline__ void zs_chain_pair(uint32_t &wp, uint32_t &wq, const 
     wq = __byte_perm(__byte_perm(rq, gq, 0x0073), __byte_perm(bq, wq, 0x0073), 0x5410);
 }
 
-template <bool CBRT, bool CUBE, bool CLAMP, bool NONNEG, bool RANK1>
+// VEC: 16-byte vectors per thread and loop iteration (2: two computed while the next two are
+// in flight; 1: one computed while the next one is in flight), chosen by the autotuner.
+template <bool CBRT, bool CUBE, bool CLAMP, bool NONNEG, bool RANK1, int VEC>
 __global__ void __launch_bounds__(ZS_CHAIN_THREADS, 1) zs_chain_srgb8_kernel(const __grid_constant__ ZsChainArgs a) {
     extern __shared__ __align__(16) unsigned char zs_smem_raw[];
     ZsChainSmem &sm = *reinterpret_cast<ZsChainSmem *>(zs_smem_raw);
@@ -115,6 +117,33 @@ __global__ void __launch_bounds__(ZS_CHAIN_THREADS, 1) zs_chain_srgb8_kernel(con
     // visible (a no-op without programmatic dependent launch); the first two vectors are
     // requested before the barrier that publishes the tables.
     asm volatile("griddepcontrol.wait;" ::: "memory");
+    if (VEC == 1) {
+        uint4 w = make_uint4(0, 0, 0, 0);
+        if (v < nvec) w = __ldcs(in + v);
+        __syncthreads();
+        const int lane = threadIdx.x & 31;
+        const unsigned char *lut = reinterpret_cast<const unsigned char *>(sm.lut);
+        const uint32_t lane4 = (uint32_t)lane << 2;
+        const uint32_t ebase = zs_enc_base(sm.enc, lane);
+        for (; v < nvec; v += stride) {
+            // The next vector is in flight while this one is computed.
+            const uint4 n = v + stride < nvec ? __ldcs(in + v + stride) : w;
+            zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG, RANK1>(w.x, w.y, lut, lane4, ebase, a);
+            zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG, RANK1>(w.z, w.w, lut, lane4, ebase, a);
+            __stcs(out + v, w);
+            w = n;
+        }
+        const int64_t tail0 = nvec << 2;
+        const int64_t t = tail0 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+        if (t < a.npx && t < tail0 + 4) {
+            const uint32_t *in32 = reinterpret_cast<const uint32_t *>(a.src);
+            uint32_t *out32 = reinterpret_cast<uint32_t *>(a.dst);
+            uint32_t p = in32[t], q = p;
+            zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG, RANK1>(p, q, lut, lane4, ebase, a);
+            out32[t] = p;
+        }
+        return;
+    }
     const bool piped = v + stride < nvec;
     uint4 w0 = make_uint4(0, 0, 0, 0), w1 = w0;
     if (piped) {
@@ -171,29 +200,31 @@ __global__ void __launch_bounds__(ZS_CHAIN_THREADS, 1) zs_chain_srgb8_kernel(con
 namespace zs {
 
 template <bool CBRT, bool CUBE, bool CLAMP, bool NONNEG, bool RANK1 = false>
-static cudaError_t launch_chain_t(const ZsChainArgs &args, int sm_count, cudaStream_t stream, int threads) {
-    auto kernel = zs_chain_srgb8_kernel<CBRT, CUBE, CLAMP, NONNEG, RANK1>;
+static cudaError_t launch_chain_t(const ZsChainArgs &args, int sm_count, cudaStream_t stream, int threads,
+                                  int vectors) {
+    auto kernel = vectors == 1 ? zs_chain_srgb8_kernel<CBRT, CUBE, CLAMP, NONNEG, RANK1, 1>
+                               : zs_chain_srgb8_kernel<CBRT, CUBE, CLAMP, NONNEG, RANK1, 2>;
     const size_t smem = sizeof(ZsChainSmem);
     // The shared-memory opt-in is a per-device attribute of the kernel: set it (and size the
     // grid) once per device and block size, on the device that is current for this launch.
     // Block sizes: 1024 threads (one block per SM) or 512, chosen by the autotuner, and 256
     // for the zero-copy host round trip (fewer host reads in flight); all run the same
     // arithmetic per pixel.
-    static std::atomic<int> per_sm_of[ZS_MAX_DEVICES][3];
-    const int which = threads == 512 ? 1 : (threads == 256 ? 2 : 0);
+    static std::atomic<int> per_sm_of[ZS_MAX_DEVICES][3][2];
+    const int which = threads == 512 ? 1 : (threads == 256 ? 2 : 0), vi = vectors == 1 ? 1 : 0;
     const int block = which == 1 ? 512 : (which == 2 ? 256 : ZS_CHAIN_THREADS);
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= ZS_MAX_DEVICES) return cudaErrorInvalidDevice;
-    int per_sm = per_sm_of[dev][which].load();
+    int per_sm = per_sm_of[dev][which][vi].load();
     if (per_sm == 0) {
         e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem);
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
-        per_sm_of[dev][which].store(per_sm);
+        per_sm_of[dev][which][vi].store(per_sm);
     }
     const int64_t nvec = (args.npx + 3) / 4;
     int64_t blocks = (nvec + block - 1) / block;
@@ -220,32 +251,33 @@ static cudaError_t launch_chain_t(const ZsChainArgs &args, int sm_count, cudaStr
 }
 
 template <bool NONNEG>
-static cudaError_t launch_chain_n(const ZsChainArgs &args, int sm_count, cudaStream_t stream, int threads) {
+static cudaError_t launch_chain_n(const ZsChainArgs &args, int sm_count, cudaStream_t stream, int threads,
+                                  int vectors) {
     const bool cb = args.flags & ZS_CHAIN_CBRT, cu = args.flags & ZS_CHAIN_CUBE, cl = args.flags & ZS_CHAIN_CLAMP;
     // The Oklab form (cube root, L/C scaling, cube) with the rank-1 middle matrix.
     if (cb && cu && (args.flags & ZS_CHAIN_MB_RANK1)) {
-        if (cl) return launch_chain_t<true, true, true, NONNEG, true>(args, sm_count, stream, threads);
-        return launch_chain_t<true, true, false, NONNEG, true>(args, sm_count, stream, threads);
+        if (cl) return launch_chain_t<true, true, true, NONNEG, true>(args, sm_count, stream, threads, vectors);
+        return launch_chain_t<true, true, false, NONNEG, true>(args, sm_count, stream, threads, vectors);
     }
-    if (cb && cu && cl) return launch_chain_t<true, true, true, NONNEG>(args, sm_count, stream, threads);
-    if (cb && cu && !cl) return launch_chain_t<true, true, false, NONNEG>(args, sm_count, stream, threads);
-    if (cb && !cu && cl) return launch_chain_t<true, false, true, NONNEG>(args, sm_count, stream, threads);
-    if (cb && !cu && !cl) return launch_chain_t<true, false, false, NONNEG>(args, sm_count, stream, threads);
-    if (!cb && cu && cl) return launch_chain_t<false, true, true, NONNEG>(args, sm_count, stream, threads);
-    if (!cb && cu && !cl) return launch_chain_t<false, true, false, NONNEG>(args, sm_count, stream, threads);
-    if (!cb && !cu && cl) return launch_chain_t<false, false, true, NONNEG>(args, sm_count, stream, threads);
-    return launch_chain_t<false, false, false, NONNEG>(args, sm_count, stream, threads);
+    if (cb && cu && cl) return launch_chain_t<true, true, true, NONNEG>(args, sm_count, stream, threads, vectors);
+    if (cb && cu && !cl) return launch_chain_t<true, true, false, NONNEG>(args, sm_count, stream, threads, vectors);
+    if (cb && !cu && cl) return launch_chain_t<true, false, true, NONNEG>(args, sm_count, stream, threads, vectors);
+    if (cb && !cu && !cl) return launch_chain_t<true, false, false, NONNEG>(args, sm_count, stream, threads, vectors);
+    if (!cb && cu && cl) return launch_chain_t<false, true, true, NONNEG>(args, sm_count, stream, threads, vectors);
+    if (!cb && cu && !cl) return launch_chain_t<false, true, false, NONNEG>(args, sm_count, stream, threads, vectors);
+    if (!cb && !cu && cl) return launch_chain_t<false, false, true, NONNEG>(args, sm_count, stream, threads, vectors);
+    return launch_chain_t<false, false, false, NONNEG>(args, sm_count, stream, threads, vectors);
 }
 
 cudaError_t launch_chain(const ZsChainArgs &args, uint8_t src_fast, uint8_t dst_fast, int sm_count,
-                         cudaStream_t stream, int threads) {
+                         cudaStream_t stream, int threads, int vectors) {
     if (src_fast != ZS_FAST_RGBA8_SRGB || dst_fast != ZS_FAST_RGBA8_SRGB) return cudaErrorNotSupported;
     if (args.npx <= 0) return cudaSuccess;
     // 16-byte vector loads and stores: other pointers take the generic raster kernel.
     if (((uintptr_t)args.src | (uintptr_t)args.dst) & 15u) return cudaErrorNotSupported;
     if ((args.flags & ZS_CHAIN_CBRT_NONNEG) || !(args.flags & ZS_CHAIN_CBRT))
-        return launch_chain_n<true>(args, sm_count, stream, threads);
-    return launch_chain_n<false>(args, sm_count, stream, threads);
+        return launch_chain_n<true>(args, sm_count, stream, threads, vectors);
+    return launch_chain_n<false>(args, sm_count, stream, threads, vectors);
 }
 
 }  // namespace zs

@@ -28,9 +28,10 @@ cudaError_t launch_resample_tc(const ZsRasterArgs &args, int sm_count, cudaStrea
 
 // Fused colour chain in canonical form, RGBA8 in / RGBA8 out (k_chain.cu).
 // Returns cudaErrorNotSupported when no specialisation exists for the formats or the buffers
-// are not 16-byte aligned.  threads: 1024 (default, one block per SM) or 512 (two).
+// are not 16-byte aligned.  threads: 1024 (default, one block per SM), 512 or 256; vectors:
+// 16-byte vectors per thread and loop iteration, 2 (default) or 1.
 cudaError_t launch_chain(const ZsChainArgs &args, uint8_t src_fast, uint8_t dst_fast, int sm_count,
-                         cudaStream_t stream, int threads = 1024);
+                         cudaStream_t stream, int threads = 1024, int vectors = 2);
 
 // A stack of affine-transformed layers blended in one pass (k_layers.cu).
 cudaError_t launch_layers(const ZsLayersArgs &args, int sm_count, cudaStream_t stream);
