@@ -116,3 +116,35 @@ def test_set_knob_on_the_one_call_path():
         got = dst.download(np.empty((32, 256), np.uint8))
         want = O.encode(O.SRGB_RGBA8, np.broadcast_to(np.array(color, np.float64), (32, 64, 4)).copy())
         assert (got == want).all(), color
+
+
+def test_knob_inside_a_linked_function(goldens):
+    """tests/knobs.rs's knob, recorded inside a function that main invokes (two levels: main ->
+    outer -> inner) and reached through its link index (RegisterKnob { link_idx, register })."""
+    inner = zs.CommandBuffer()
+    g = inner.generic()
+    x = inner.input_generic(g)
+    r = inner.with_knob().bilinear(zs.Descriptor.srgb_rgba8(512, 512), **BASE)
+    inner.output(r)
+    outer = zs.CommandBuffer()
+    h = outer.generic()
+    y = outer.input_generic(h)
+    fi = outer.function(inner)
+    (res,) = outer.invoke(fi, generics=[h], arguments=[y])
+    outer.output(res)
+    main = zs.CommandBuffer()
+    fo = main.function(outer)
+    pool = zs.Pool()
+    ks = pool.insert(zs.Descriptor.srgb_rgba8(8, 8), np.zeros((8, 32), np.uint8))
+    m = main.input(pool.descriptor(ks))
+    (out,) = main.invoke(fo, generics=[main.register_descriptor(m)], arguments=[m])
+    o, _ = main.output(out)
+    exe = zs.Linker.from_included().link(main, [], [outer, inner], [[1], [2], []]).lower_to()
+    knob, nbytes = exe.query_knob(r, link_idx=2)
+    assert nbytes == 96
+    for idx, (u_min, u_max, v_min, v_max) in enumerate(KNOBS[:3]):
+        block = std430(u_min, u_max, v_min, v_max)
+        (key,) = zs.run_executable(exe, pool, [(m, ks)], [(knob, block)], [o])
+        got = pool.read(key)
+        assert (got == oracle_bilinear_srgb8(512, 512, block)).all(), idx
+        assert blockhash256(got.reshape(512, 512, 4)) in goldens[f"bilinear-knob-{idx}"]
