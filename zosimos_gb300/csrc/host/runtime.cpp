@@ -59,13 +59,15 @@ PoolImage &Pool::get(uint64_t key) {
 
 Executable::~Executable() {
     for (auto &kv : graphs) cudaGraphExecDestroy(kv.second);
-    if (batch_graph) cudaGraphExecDestroy(batch_graph);
-    if (batch_done) {
-        cudaEventSynchronize(batch_done);
-        cudaEventDestroy(batch_done);
+    for (BatchSet &b : batch_sets) {
+        if (b.graph) cudaGraphExecDestroy(b.graph);
+        if (b.done) {
+            cudaEventSynchronize(b.done);
+            cudaEventDestroy(b.done);
+        }
+        if (b.scratch) cudaFree(b.scratch);
+        if (b.staging) cudaFreeHost(b.staging);
     }
-    if (batch_scratch) cudaFree(batch_scratch);
-    if (batch_staging) cudaFreeHost(batch_staging);
     if (graph_stream) cudaStreamDestroy(graph_stream);
     for (void *p : dev_buffers)
         if (p) cudaFree(p);

@@ -256,14 +256,19 @@ struct Executable {
     std::map<std::pair<uint32_t, uint32_t>, uint32_t> alias;   // Program::alias
     std::vector<int> input_slot, output_slot;
     std::vector<void *> dev_buffers;                   // device allocation per slot (owned ones)
-    // zs_batch_thumbnails: device image/prefix tables, their pinned staging copy, the event of
-    // the last batch and its captured graph (memset + kernel) with the key it was captured for
-    void *batch_scratch = nullptr;
-    void *batch_staging = nullptr;
-    size_t batch_bytes = 0;
-    cudaEvent_t batch_done = nullptr;
-    cudaGraphExec_t batch_graph = nullptr;
-    std::vector<uint64_t> batch_key;
+    // zs_batch_thumbnails: two sets (alternate batches) of device image/prefix tables, their
+    // pinned staging copy, the event of the batch that last used them, and that set's captured
+    // graph with its key, so that the tables of one batch are built while the previous runs.
+    struct BatchSet {
+        void *scratch = nullptr;
+        void *staging = nullptr;
+        size_t bytes = 0;
+        cudaEvent_t done = nullptr;
+        cudaGraphExec_t graph = nullptr;
+        std::vector<uint64_t> key;
+    };
+    BatchSet batch_sets[2];
+    int batch_next = 0;
     int batch_rows = 0;                                // batch work-item height (0: tuned or default)
     int batch_threads = 0;                             // batch kernel block size (0: tuned or default)
     std::string plan_text;

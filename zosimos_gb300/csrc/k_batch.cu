@@ -461,9 +461,10 @@ int batch_thumbnails(Executable *chain, const void *const *images, const uint32_
         }
         prefix[k + 1] = prefix[k] + (int32_t)items;
     }
-    // Scratch: image table + item prefix table, kept with the executable, uploaded from a
-    // pinned staging copy.  The previous batch of this executable must have finished with
-    // both before they are rewritten.
+    // Scratch: image table + item prefix table, kept with the executable in two sets used by
+    // alternate batches, uploaded from a pinned staging copy: the batch two calls back (the
+    // last user of this set) must have finished with it before it is rewritten, while the
+    // previous batch may still run.
     const size_t table_bytes = (sizeof(ZsBatchImage) * n + 255) & ~(size_t)255;
     const size_t prefix_bytes = (sizeof(int32_t) * (n + 1) + 15) & ~(size_t)15;
     const size_t bytes = table_bytes + prefix_bytes + 16;   // + the queue counter
@@ -472,19 +473,21 @@ int batch_thumbnails(Executable *chain, const void *const *images, const uint32_
         return e == cudaErrorMemoryAllocation ? ZS_ERR_OUT_OF_MEMORY : ZS_ERR_DEVICE;
     };
     cudaError_t e = cudaSuccess;
-    if (chain->batch_done && (e = cudaEventSynchronize(chain->batch_done)) != cudaSuccess) return device_error(e);
-    if (chain->batch_bytes < bytes) {
-        if (chain->batch_scratch) cudaFree(chain->batch_scratch);
-        if (chain->batch_staging) cudaFreeHost(chain->batch_staging);
-        chain->batch_scratch = chain->batch_staging = nullptr;
-        chain->batch_bytes = 0;
-        if ((e = cudaMalloc(&chain->batch_scratch, bytes)) != cudaSuccess) return device_error(e);
-        if ((e = cudaMallocHost(&chain->batch_staging, bytes)) != cudaSuccess) return device_error(e);
-        chain->batch_bytes = bytes;
+    Executable::BatchSet &bs = chain->batch_sets[chain->batch_next];
+    chain->batch_next ^= 1;
+    if (bs.done && (e = cudaEventSynchronize(bs.done)) != cudaSuccess) return device_error(e);
+    if (bs.bytes < bytes) {
+        if (bs.scratch) cudaFree(bs.scratch);
+        if (bs.staging) cudaFreeHost(bs.staging);
+        bs.scratch = bs.staging = nullptr;
+        bs.bytes = 0;
+        if ((e = cudaMalloc(&bs.scratch, bytes)) != cudaSuccess) return device_error(e);
+        if ((e = cudaMallocHost(&bs.staging, bytes)) != cudaSuccess) return device_error(e);
+        bs.bytes = bytes;
     }
-    if (!chain->batch_done && (e = cudaEventCreateWithFlags(&chain->batch_done, cudaEventDisableTiming)) != cudaSuccess)
+    if (!bs.done && (e = cudaEventCreateWithFlags(&bs.done, cudaEventDisableTiming)) != cudaSuccess)
         return device_error(e);
-    uint8_t *scratch = (uint8_t *)chain->batch_scratch, *staging = (uint8_t *)chain->batch_staging;
+    uint8_t *scratch = (uint8_t *)bs.scratch, *staging = (uint8_t *)bs.staging;
     std::memcpy(staging, sorted.data(), sizeof(ZsBatchImage) * n);
     std::memcpy(staging + table_bytes, prefix.data(), sizeof(int32_t) * (n + 1));
     if ((e = cudaMemcpyAsync(scratch, staging, table_bytes + prefix_bytes, cudaMemcpyHostToDevice, stream)) !=
@@ -556,15 +559,15 @@ int batch_thumbnails(Executable *chain, const void *const *images, const uint32_
         }
         return ce;
     };
-    if (!chain->batch_graph || chain->batch_key != key) {
-        if (chain->batch_graph) cudaGraphExecDestroy(chain->batch_graph);
-        chain->batch_graph = nullptr;
-        chain->batch_key.clear();
+    if (!bs.graph || bs.key != key) {
+        if (bs.graph) cudaGraphExecDestroy(bs.graph);
+        bs.graph = nullptr;
+        bs.key.clear();
         if (cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
             // A stream that cannot be captured (the legacy default stream): launch directly.
             cudaGetLastError();
             if ((e = enqueue()) != cudaSuccess) return device_error(e);
-            if ((e = cudaEventRecord(chain->batch_done, stream)) != cudaSuccess) return device_error(e);
+            if ((e = cudaEventRecord(bs.done, stream)) != cudaSuccess) return device_error(e);
             g_kernel_launches.fetch_add(1);
             return ZS_OK;
         }
@@ -579,11 +582,11 @@ int batch_thumbnails(Executable *chain, const void *const *images, const uint32_
         e = cudaGraphInstantiate(&ge, g, 0);
         cudaGraphDestroy(g);
         if (e != cudaSuccess) return device_error(e);
-        chain->batch_graph = ge;
-        chain->batch_key = key;
+        bs.graph = ge;
+        bs.key = key;
     }
-    if ((e = cudaGraphLaunch(chain->batch_graph, stream)) != cudaSuccess) return device_error(e);
-    if ((e = cudaEventRecord(chain->batch_done, stream)) != cudaSuccess) return device_error(e);
+    if ((e = cudaGraphLaunch(bs.graph, stream)) != cudaSuccess) return device_error(e);
+    if ((e = cudaEventRecord(bs.done, stream)) != cudaSuccess) return device_error(e);
     g_kernel_launches.fetch_add(1);
     return ZS_OK;
 }
