@@ -503,8 +503,10 @@ int zs_tune_cache_load(const char *path);
 uint64_t zs_kernel_launch_count(void);
 
 /* Device status word of `device` (ZS_DEVSTAT_* bits of zs_shared.h; bit 0: a bounded wait of
- * a kernel on its own bulk copies gave up, and that launch's output is incomplete), read
- * after synchronising and cleared.  zs_exec_sync reports a set bit as ZS_ERR_TIMEOUT.
+ * a kernel on its own bulk copies gave up, and that launch's output is incomplete; bit 1: a
+ * kernel found its shared-memory window laid out other than the host checked and wrote
+ * nothing), read after synchronising and cleared.  zs_exec_sync reports bit 0 as
+ * ZS_ERR_TIMEOUT and bit 1 as ZS_ERR_DEVICE.
  * No counterpart in the reference (wgpu reports device loss through its own callbacks). */
 int zs_device_status(int device, uint32_t *flags);
 

@@ -849,7 +849,8 @@ int zs_exec_sync(zs_execution *exec) {
         check_cuda(cudaStreamSynchronize(exec->x.stream), "synchronize");
         uint32_t flags = 0;
         check_cuda(read_device_status(exec->x.exe->device, &flags, true), "device status");
-        if (flags) fail(ZS_ERR_TIMEOUT, "a kernel's bounded wait on its bulk copies gave up");
+        if (flags & ZS_DEVSTAT_WAIT_TIMEOUT) fail(ZS_ERR_TIMEOUT, "a kernel's bounded wait on its bulk copies gave up");
+        if (flags) fail(ZS_ERR_DEVICE, "a kernel's shared-memory layout did not fit its window");
     });
 }
 

@@ -39,6 +39,7 @@
 #include "zs_kernels.h"
 
 #define ZS_BATCH_SPAN 128         // source columns of a streaming item: 4 per lane
+#define ZS_BATCH_SMEM (2 * ZS_DEC_ABS)   // dynamic shared memory per block
 #define ZS_BATCH_ROWS_DEFAULT 4   // work-item height until the autotuner chose (see batch_thumbnails)
 
 struct ZsBatchImage {
@@ -100,19 +101,20 @@ __device__ __forceinline__ void zs_cbrt_pair(float2 &x) {
 }
 
 // The canonical chain on four texels (two FP32x2 pairs: (w0, w1) and (w2, w3)), linear
-// result in v[pair][channel]: decode through the lane-replicated shared table, matrix
-// products, MUFU cube roots.
+// result in v[pair][channel]: decode through the lane-replicated shared table at shared
+// address ZS_DEC_ABS (lane4 = ZS_DEC_ABS | lane << 2), matrix products, MUFU cube roots.
 template <int SPEC>
 __device__ __forceinline__ void zs_batch_chain4(uint32_t w0, uint32_t w1, uint32_t w2, uint32_t w3,
                                                 const unsigned char *lut, uint32_t lane4, const ZsBatchArgs &a,
                                                 float2 (&v)[2][3]) {
     using S = ZsBatchSpec<SPEC>;
-    v[0][0] = make_float2(zs_dec<0>(lut, w0, lane4), zs_dec<0>(lut, w1, lane4));
-    v[0][1] = make_float2(zs_dec<1>(lut, w0, lane4), zs_dec<1>(lut, w1, lane4));
-    v[0][2] = make_float2(zs_dec<2>(lut, w0, lane4), zs_dec<2>(lut, w1, lane4));
-    v[1][0] = make_float2(zs_dec<0>(lut, w2, lane4), zs_dec<0>(lut, w3, lane4));
-    v[1][1] = make_float2(zs_dec<1>(lut, w2, lane4), zs_dec<1>(lut, w3, lane4));
-    v[1][2] = make_float2(zs_dec<2>(lut, w2, lane4), zs_dec<2>(lut, w3, lane4));
+    (void)lut;
+    v[0][0] = make_float2(zs_dec_abs<0>(w0, lane4), zs_dec_abs<0>(w1, lane4));
+    v[0][1] = make_float2(zs_dec_abs<1>(w0, lane4), zs_dec_abs<1>(w1, lane4));
+    v[0][2] = make_float2(zs_dec_abs<2>(w0, lane4), zs_dec_abs<2>(w1, lane4));
+    v[1][0] = make_float2(zs_dec_abs<0>(w2, lane4), zs_dec_abs<0>(w3, lane4));
+    v[1][1] = make_float2(zs_dec_abs<1>(w2, lane4), zs_dec_abs<1>(w3, lane4));
+    v[1][2] = make_float2(zs_dec_abs<2>(w2, lane4), zs_dec_abs<2>(w3, lane4));
     zs_m3x2x2<false>(a.m2[0], v);
     const bool cbrt = S::generic ? (a.flags & ZS_CHAIN_CBRT) != 0 : true;
     if (cbrt) {
@@ -341,18 +343,30 @@ __device__ __forceinline__ void zs_batch_direct(const ZsBatchImage &I, int band,
 // 24 warps with a few spilled registers or 20 warps without).
 template <int THREADS, int SPEC>
 __global__ void __launch_bounds__(THREADS, 1) zs_batch_kernel(const __grid_constant__ ZsBatchArgs a) {
-    // [0, 64 KiB): decode table, [code][64] floats (lanes 32..63 unused);
-    // then one 128-column slice of float4 column sums per warp.
+    // From the start of the dynamic window: one 128-column slice of float4 column sums per
+    // warp; at shared address ZS_DEC_ABS .. 2 * ZS_DEC_ABS: the decode table, [code][64] floats
+    // (lanes 32..63 unused), so that one PRMT forms each decode's load address.  The host
+    // launches with ZS_BATCH_SMEM bytes after checking that the slices fit below ZS_DEC_ABS;
+    // should the window start higher, the block flags it and does nothing.
     extern __shared__ __align__(16) float zs_batch_smem[];
+    const uint32_t s0 = (uint32_t)__cvta_generic_to_shared(zs_batch_smem);
+    uint32_t dyn;
+    asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
+    if (s0 + (uint32_t)(THREADS / 32 * ZS_BATCH_SPAN * sizeof(float4)) > ZS_DEC_ABS ||
+        ZS_DEC_ABS + 256u * 64u * 4u > s0 + dyn) {
+        if (threadIdx.x == 0) atomicOr(&zs_device_status_word, ZS_DEVSTAT_LAYOUT);
+        return;
+    }
+    float *table = reinterpret_cast<float *>(reinterpret_cast<unsigned char *>(zs_batch_smem) + (ZS_DEC_ABS - s0));
     for (int i = threadIdx.x; i < 256 * 8; i += blockDim.x) {
         const float d = zs_srgb_decode_lut[i >> 3];
-        reinterpret_cast<float4 *>(zs_batch_smem)[(i >> 3) * 16 + (i & 7)] = make_float4(d, d, d, d);
+        reinterpret_cast<float4 *>(table)[(i >> 3) * 16 + (i & 7)] = make_float4(d, d, d, d);
     }
     __syncthreads();
-    const unsigned char *lut = reinterpret_cast<const unsigned char *>(zs_batch_smem);
-    float4 *hb = reinterpret_cast<float4 *>(zs_batch_smem + 256 * 64) + (threadIdx.x >> 5) * ZS_BATCH_SPAN;
+    const unsigned char *lut = reinterpret_cast<const unsigned char *>(table);
+    float4 *hb = reinterpret_cast<float4 *>(zs_batch_smem) + (threadIdx.x >> 5) * ZS_BATCH_SPAN;
     const int lane = threadIdx.x & 31;
-    const uint32_t lane4 = (uint32_t)lane << 2;
+    const uint32_t lane4 = ZS_DEC_ABS | ((uint32_t)lane << 2);
     const int total = a.prefix[a.n];
     int img = 0;   // entry of the current item: a warp's items only move forward, so scan on
     for (;;) {
@@ -524,7 +538,16 @@ int batch_thumbnails(Executable *chain, const void *const *images, const uint32_
         {zs_batch_kernel<640, 0>, zs_batch_kernel<640, 1>, zs_batch_kernel<640, 2>, zs_batch_kernel<640, 3>,
          zs_batch_kernel<640, 4>}};
     void (*kernel)(ZsBatchArgs) = kernels[threads == 640 ? 1 : 0][spec];
-    const size_t smem = 256 * 64 * sizeof(float) + (size_t)(threads / 32) * ZS_BATCH_SPAN * sizeof(float4);
+    // The column-sum slices below ZS_DEC_ABS, after the driver's reserved shared memory (the
+    // kernel has no static shared memory), the decode table above it.
+    const size_t smem = ZS_BATCH_SMEM;
+    {
+        int reserved = 0;
+        e = cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, chain->device);
+        if (e != cudaSuccess) return device_error(e);
+        if ((size_t)reserved + (size_t)(threads / 32) * ZS_BATCH_SPAN * sizeof(float4) > ZS_DEC_ABS)
+            return device_error(cudaErrorNotSupported);
+    }
     e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int per_sm = 0;
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, smem);

@@ -15,7 +15,8 @@
 //    next two are in flight (software pipeline); one 1024-thread block per SM, so the
 //    replicated tables fit beside each other;
 //  * sRGB decode from a lane-replicated shared table (lane l reads column l: no bank
-//    conflicts whatever the data);
+//    conflicts whatever the data) at shared address 0x10000, so one PRMT of the texel forms
+//    the load address; 32-bit vector indices;
 //  * pixels processed in pairs with packed FP32x2 FMA (one instruction, two pixels),
 //    the matrix coefficients read as 64-bit constant operands;
 //  * cube roots as ex2(lg2(x)/3) on the MUFU pipe (the sign fix-up is dropped when the
@@ -29,6 +30,8 @@
 //    shift-add, one shared load and one add per channel, packed with PRMT;
 //  * alpha bytes passed through (unorm8 alpha decode + encode is the identity).
 #include <atomic>
+#include <cstdint>
+#include <type_traits>
 
 #include "zs_chain.cuh"
 #include "zs_device.cuh"
@@ -43,12 +46,20 @@ struct ZsChainSmem {
     uint32_t enc[ZS_ENCS_ENTRIES * ZS_ENC_REP];   // [bucket][lane & 7], shifted domain
 };
 
-template <bool CBRT, bool CUBE, bool CLAMP, bool NONNEG, bool RANK1>
+// Decode of byte K: from the table at `lut` (lane4 = lane << 2), or with ABS from the table
+// at shared address ZS_DEC_ABS (lane4 = ZS_DEC_ABS | lane << 2).
+template <int K, bool ABS>
+__device__ __forceinline__ float zs_dec_at(const unsigned char *lut, uint32_t w, uint32_t lane4) {
+    if (ABS) return zs_dec_abs<K>(w, lane4);
+    return zs_dec<K>(lut, w, lane4);
+}
+
+template <bool CBRT, bool CUBE, bool CLAMP, bool NONNEG, bool RANK1, bool ABS = false>
 __device__ __forceinline__ void zs_chain_pair(uint32_t &wp, uint32_t &wq, const unsigned char *lut,
                                               uint32_t lane4, uint32_t ebase, const ZsChainArgs &a) {
-    float2 r = make_float2(zs_dec<0>(lut, wp, lane4), zs_dec<0>(lut, wq, lane4));
-    float2 g = make_float2(zs_dec<1>(lut, wp, lane4), zs_dec<1>(lut, wq, lane4));
-    float2 b = make_float2(zs_dec<2>(lut, wp, lane4), zs_dec<2>(lut, wq, lane4));
+    float2 r = make_float2(zs_dec_at<0, ABS>(lut, wp, lane4), zs_dec_at<0, ABS>(lut, wq, lane4));
+    float2 g = make_float2(zs_dec_at<1, ABS>(lut, wp, lane4), zs_dec_at<1, ABS>(lut, wq, lane4));
+    float2 b = make_float2(zs_dec_at<2, ABS>(lut, wp, lane4), zs_dec_at<2, ABS>(lut, wq, lane4));
     zs_m3x2<false>(a.m2[0], r, g, b);
     if (CBRT) {
         if (NONNEG) {
@@ -89,17 +100,43 @@ __device__ __forceinline__ void zs_chain_pair(uint32_t &wp, uint32_t &wq, const 
     wq = __byte_perm(__byte_perm(rq, gq, 0x0073), __byte_perm(bq, wq, 0x0073), 0x5410);
 }
 
+// Dynamic shared memory of the FAST form: the encode table at the start of the block's
+// dynamic window, the decode table at shared address ZS_DEC_ABS .. 2 * ZS_DEC_ABS.
+#define ZS_CHAIN_FAST_SMEM (2 * ZS_DEC_ABS)
+
 // VEC: 16-byte vectors per thread and loop iteration (2: two computed while the next two are
 // in flight; 1: one computed while the next one is in flight), chosen by the autotuner.
-template <bool CBRT, bool CUBE, bool CLAMP, bool NONNEG, bool RANK1, int VEC>
+// FAST (VEC 2, one block per SM, fewer than 2^31 vectors plus three grid strides): the decode
+// table at a fixed 64 KiB-aligned shared address, so each decode is a PRMT and a load with
+// no address add, and 32-bit vector indices; about 5 fewer instructions per pixel.
+template <bool CBRT, bool CUBE, bool CLAMP, bool NONNEG, bool RANK1, int VEC, bool FAST>
 __global__ void __launch_bounds__(ZS_CHAIN_THREADS, 1) zs_chain_srgb8_kernel(const __grid_constant__ ZsChainArgs a) {
     extern __shared__ __align__(16) unsigned char zs_smem_raw[];
-    ZsChainSmem &sm = *reinterpret_cast<ZsChainSmem *>(zs_smem_raw);
+    struct { float *lut; uint32_t *enc; } sm;
+    if (FAST) {
+        // The host launches this form with ZS_CHAIN_FAST_SMEM bytes when the block's shared
+        // window starts below ZS_DEC_ABS - sizeof(enc); should the window start higher, the
+        // block flags it and does nothing.
+        const uint32_t s0 = (uint32_t)__cvta_generic_to_shared(zs_smem_raw);
+        uint32_t dyn;
+        asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(dyn));
+        if (s0 + (uint32_t)sizeof(ZsChainSmem::enc) > ZS_DEC_ABS || ZS_DEC_ABS + (uint32_t)sizeof(ZsChainSmem::lut) > s0 + dyn) {
+            if (threadIdx.x == 0) atomicOr(&zs_device_status_word, ZS_DEVSTAT_LAYOUT);
+            return;
+        }
+        sm.enc = reinterpret_cast<uint32_t *>(zs_smem_raw);
+        sm.lut = reinterpret_cast<float *>(zs_smem_raw + (ZS_DEC_ABS - s0));
+    } else {
+        ZsChainSmem &t = *reinterpret_cast<ZsChainSmem *>(zs_smem_raw);
+        sm.enc = t.enc;
+        sm.lut = t.lut;
+    }
+    using IX = typename std::conditional<FAST, int, int64_t>::type;
     const uint4 *in = reinterpret_cast<const uint4 *>(a.src);
     uint4 *out = reinterpret_cast<uint4 *>(a.dst);
-    const int64_t nvec = a.npx >> 2;
-    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const IX nvec = (IX)(a.npx >> 2);
+    const IX stride = (IX)gridDim.x * blockDim.x;
+    IX v = (IX)blockIdx.x * blockDim.x + threadIdx.x;
     // Programmatic dependent launch: the next launch in the stream may start as soon as this
     // one runs; its CTAs stage their tables while this grid drains, then wait below.
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
@@ -153,25 +190,25 @@ __global__ void __launch_bounds__(ZS_CHAIN_THREADS, 1) zs_chain_srgb8_kernel(con
     __syncthreads();
     const int lane = threadIdx.x & 31;
     const unsigned char *lut = reinterpret_cast<const unsigned char *>(sm.lut);
-    const uint32_t lane4 = (uint32_t)lane << 2;
+    const uint32_t lane4 = ((uint32_t)lane << 2) | (FAST ? ZS_DEC_ABS : 0u);
     const uint32_t ebase = zs_enc_base(sm.enc, lane);
 
     if (piped) {
         // Software pipeline: the next two vectors are in flight while the current two are
         // computed, so each thread keeps 32 bytes of reads outstanding at all times.
         for (;;) {
-            const int64_t nx = v + 2 * stride;
+            const IX nx = v + 2 * stride;
             const bool more = nx + stride < nvec;
             uint4 n0 = w0, n1 = w1;
             if (more) {
                 n0 = __ldcs(in + nx);
                 n1 = __ldcs(in + nx + stride);
             }
-            zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG, RANK1>(w0.x, w0.y, lut, lane4, ebase, a);
-            zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG, RANK1>(w0.z, w0.w, lut, lane4, ebase, a);
+            zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG, RANK1, FAST>(w0.x, w0.y, lut, lane4, ebase, a);
+            zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG, RANK1, FAST>(w0.z, w0.w, lut, lane4, ebase, a);
             __stcs(out + v, w0);
-            zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG, RANK1>(w1.x, w1.y, lut, lane4, ebase, a);
-            zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG, RANK1>(w1.z, w1.w, lut, lane4, ebase, a);
+            zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG, RANK1, FAST>(w1.x, w1.y, lut, lane4, ebase, a);
+            zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG, RANK1, FAST>(w1.z, w1.w, lut, lane4, ebase, a);
             __stcs(out + v + stride, w1);
             v = nx;
             if (!more) break;
@@ -181,8 +218,8 @@ __global__ void __launch_bounds__(ZS_CHAIN_THREADS, 1) zs_chain_srgb8_kernel(con
     }
     if (v < nvec) {
         uint4 w = __ldcs(in + v);
-        zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG, RANK1>(w.x, w.y, lut, lane4, ebase, a);
-        zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG, RANK1>(w.z, w.w, lut, lane4, ebase, a);
+        zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG, RANK1, FAST>(w.x, w.y, lut, lane4, ebase, a);
+        zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG, RANK1, FAST>(w.z, w.w, lut, lane4, ebase, a);
         __stcs(out + v, w);
     }
     // Tail pixels (npx not a multiple of 4): block 0, threads 0..3.
@@ -192,43 +229,70 @@ __global__ void __launch_bounds__(ZS_CHAIN_THREADS, 1) zs_chain_srgb8_kernel(con
         const uint32_t *in32 = reinterpret_cast<const uint32_t *>(a.src);
         uint32_t *out32 = reinterpret_cast<uint32_t *>(a.dst);
         uint32_t p = in32[t], q = p;
-        zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG, RANK1>(p, q, lut, lane4, ebase, a);
+        zs_chain_pair<CBRT, CUBE, CLAMP, NONNEG, RANK1, FAST>(p, q, lut, lane4, ebase, a);
         out32[t] = p;
     }
 }
 
 namespace zs {
 
+// Whether the FAST form's layout fits on `dev`: the block's dynamic shared window starts after
+// the driver's reserved shared memory, which must leave room for the encode table below
+// ZS_DEC_ABS (the kernel has no static shared memory).
+static bool fast_layout_fits(int dev) {
+    static std::atomic<int> fits_of[ZS_MAX_DEVICES];
+    int f = fits_of[dev].load();
+    if (f == 0) {
+        int reserved = 0, optin = 0;
+        if (cudaDeviceGetAttribute(&reserved, cudaDevAttrReservedSharedMemoryPerBlock, dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess) {
+            (void)cudaGetLastError();
+            reserved = 1 << 30;
+        }
+        const bool ok = (size_t)reserved + sizeof(ZsChainSmem::enc) <= ZS_DEC_ABS && optin >= (int)ZS_CHAIN_FAST_SMEM;
+        f = ok ? 1 : 2;
+        fits_of[dev].store(f);
+    }
+    return f == 1;
+}
+
 template <bool CBRT, bool CUBE, bool CLAMP, bool NONNEG, bool RANK1 = false>
 static cudaError_t launch_chain_t(const ZsChainArgs &args, int sm_count, cudaStream_t stream, int threads,
                                   int vectors) {
-    auto kernel = vectors == 1 ? zs_chain_srgb8_kernel<CBRT, CUBE, CLAMP, NONNEG, RANK1, 1>
-                               : zs_chain_srgb8_kernel<CBRT, CUBE, CLAMP, NONNEG, RANK1, 2>;
-    const size_t smem = sizeof(ZsChainSmem);
     // The shared-memory opt-in is a per-device attribute of the kernel: set it (and size the
     // grid) once per device and block size, on the device that is current for this launch.
     // Block sizes: 1024 threads (one block per SM) or 512, chosen by the autotuner, and 256
     // for the zero-copy host round trip (fewer host reads in flight); all run the same
     // arithmetic per pixel.
-    static std::atomic<int> per_sm_of[ZS_MAX_DEVICES][3][2];
-    const int which = threads == 512 ? 1 : (threads == 256 ? 2 : 0), vi = vectors == 1 ? 1 : 0;
+    static std::atomic<int> per_sm_of[ZS_MAX_DEVICES][3][3];
+    const int which = threads == 512 ? 1 : (threads == 256 ? 2 : 0);
     const int block = which == 1 ? 512 : (which == 2 ? 256 : ZS_CHAIN_THREADS);
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e != cudaSuccess) return e;
     if (dev < 0 || dev >= ZS_MAX_DEVICES) return cudaErrorInvalidDevice;
-    int per_sm = per_sm_of[dev][which][vi].load();
+    // The grid is at most one wave (sm_count x blocks per SM, at most 2048 threads per SM); the
+    // FAST form needs vector indices that stay below 2^31 over three grid strides.
+    const int64_t nvec = (args.npx + 3) / 4;
+    const int64_t sms = sm_count > 0 ? sm_count : 148;
+    const bool fast = vectors != 1 && block == ZS_CHAIN_THREADS && (args.npx >> 2) + 3 * 2 * sms * block < INT32_MAX &&
+                      fast_layout_fits(dev);
+    const int form = vectors == 1 ? 1 : (fast ? 2 : 0);
+    auto kernel = form == 1 ? zs_chain_srgb8_kernel<CBRT, CUBE, CLAMP, NONNEG, RANK1, 1, false>
+                            : (form == 2 ? zs_chain_srgb8_kernel<CBRT, CUBE, CLAMP, NONNEG, RANK1, 2, true>
+                                         : zs_chain_srgb8_kernel<CBRT, CUBE, CLAMP, NONNEG, RANK1, 2, false>);
+    const size_t smem = form == 2 ? (size_t)ZS_CHAIN_FAST_SMEM : sizeof(ZsChainSmem);
+    int per_sm = per_sm_of[dev][which][form].load();
     if (per_sm == 0) {
         e = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem);
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
-        per_sm_of[dev][which][vi].store(per_sm);
+        per_sm_of[dev][which][form].store(per_sm);
     }
-    const int64_t nvec = (args.npx + 3) / 4;
     int64_t blocks = (nvec + block - 1) / block;
-    const int64_t cap = (int64_t)(sm_count > 0 ? sm_count : 148) * per_sm;
+    const int64_t cap = sms * per_sm;
     if (blocks > cap) blocks = cap;
     if (blocks < 1) blocks = 1;
     // Launched with programmatic stream serialization: the table staging of this launch

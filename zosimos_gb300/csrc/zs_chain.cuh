@@ -91,6 +91,18 @@ __device__ __forceinline__ float zs_dec(const unsigned char *lut, uint32_t w, ui
     return *reinterpret_cast<const float *>(lut + off);
 }
 
+// The same lookup when the table sits at shared address ZS_DEC_ABS (64 KiB aligned): the
+// PRMT also copies the table's address bits (bytes 2 and 3 of lane4abs = ZS_DEC_ABS | lane
+// << 2), so its result is the shared address itself and the load needs no add.
+#define ZS_DEC_ABS 0x10000u
+template <int K>
+__device__ __forceinline__ float zs_dec_abs(uint32_t w, uint32_t lane4abs) {
+    const uint32_t addr = __byte_perm(w, lane4abs, 0x7604u | (K << 4));
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(addr));
+    return v;
+}
+
 __device__ __forceinline__ void zs_cbrt2(float2 &v) {
     // NONNEG: both arguments are >= 0 (the MUFU log of 0 is -inf, its exp2 is 0).
     float2 l = make_float2(zs_lg2(v.x), zs_lg2(v.y));

@@ -170,6 +170,7 @@ struct ZsRasterArgs {
 
 // Bits of the device status word.
 #define ZS_DEVSTAT_WAIT_TIMEOUT 1u   // an mbarrier wait on a bulk copy exceeded its limit
+#define ZS_DEVSTAT_LAYOUT 2u         // a kernel's shared-memory layout did not fit its window; it did nothing
 
 // A stack of layers composited in one pass: for every output pixel, start from the
 // base (a constant or a buffer) and for each layer sample it through its inverse affine
