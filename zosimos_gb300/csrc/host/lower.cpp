@@ -27,7 +27,7 @@ struct Pending {
     int src_slot[ZS_MAX_SRCS] = {-1, -1, -1};
     int idx_x_slot = -1, idx_y_slot = -1, weight_slot = -1;
     int vfirst_slot = -1, vcount_slot = -1, vweight_slot = -1;
-    int vimg_slot = -1, vimg_index_slot = -1;
+    int vimg_slot = -1, vimg_index_slot = -1, tc_weight_slot = -1;
     std::vector<std::pair<int, int>> tc_cands;   // tensor-core tiles that fit: (tile width, atoms)
     HProgram prog;
     // virt1: the gathered image's producer sources and program (evaluated per tap)
@@ -250,6 +250,7 @@ struct Planner {
         st.vweight_slot = p.vweight_slot;
         st.vimg_slot = p.vimg_slot;
         st.vimg_index_slot = p.vimg_index_slot;
+        st.tc_weight_slot = p.tc_weight_slot;
         st.tc_cands = p.tc_cands;
         // Pixel program: FP64 host program -> FP32 parameters.
         ZsPixelProgram &pp = st.raster.prog;
@@ -1012,7 +1013,7 @@ struct Planner {
         const Slot &ss = E.slots[vals[op.a].slot];
         if (!(E.flags & ZS_CAP_SIMT_RESAMPLE) && vals[op.a].fmt.fast == ZS_FAST_F16X4 && ss.stride % 16 == 0 &&
             htaps <= 64)
-            plan_resample_tc(*p, hf, hc, vf, vc, vw, vtaps, d);
+            plan_resample_tc(*p, hf, hc, hw, htaps, vf, vc, vw, vtaps, d);
         set_pending(r, std::move(p));
         return true;
     }
@@ -1047,8 +1048,8 @@ struct Planner {
     // 128 x 64 chunk per 64 source rows, laid out as the MMA reads them (K-major rows of
     // 128 bytes, 16-byte chunk c of row m stored at chunk c ^ (m % 8)).
     void plan_resample_tc(Pending &p, const std::vector<int32_t> &hf, const std::vector<int32_t> &hc,
-                          const std::vector<int32_t> &vf, const std::vector<int32_t> &vc, const std::vector<float> &vw,
-                          int vtaps, const Desc &d) {
+                          const std::vector<float> &hw, int htaps, const std::vector<int32_t> &vf,
+                          const std::vector<int32_t> &vc, const std::vector<float> &vw, int vtaps, const Desc &d) {
         const int dw = (int)d.width, dh = (int)d.height;
         // Prefer tiles whose span fits 4 atoms (two accumulators: the epilogue of one tile
         // overlaps the MMAs of the next), else up to 8 atoms (one 512-column accumulator).
@@ -1098,6 +1099,16 @@ struct Planner {
         }
         p.vimg_slot = table_slot(img.data(), img.size() * 2);
         p.vimg_index_slot = table_slot(index.data(), index.size() * 4);
+        // Horizontal weights with rows of a multiple of 4 taps (zeros after each output's
+        // count), so that the epilogue reads four weights per 16-byte shared load; padded with
+        // zero rows to a multiple of 32 output columns like the tap windows.
+        const int taps4 = (htaps + 3) & ~3;
+        const size_t padded = ((size_t)dw + 31) / 32 * 32;
+        std::vector<float> hw4(padded * (size_t)taps4, 0.f);
+        for (int x = 0; x < dw; ++x)
+            for (int t = 0; t < htaps; ++t) hw4[(size_t)x * taps4 + t] = hw[(size_t)x * htaps + t];
+        p.tc_weight_slot = table_slot(hw4.data(), hw4.size() * 4);
+        p.a.tc_taps = taps4;
         p.a.tc_tw = tw;
         p.a.tc_atoms = (span * 4 + 63) / 64;   // the candidate's atoms (span rounded to atoms above)
         p.label = "resample 2d [tensor cores: f16 band matrices, FP32 accumulation]";

@@ -110,6 +110,7 @@ static ZsRasterArgs raster_args(const Step &st, const std::vector<void *> &ptrs)
     a.vweights = st.vweight_slot >= 0 ? (const float *)ptrs[st.vweight_slot] : nullptr;
     a.vimg = st.vimg_slot >= 0 ? (const uint8_t *)ptrs[st.vimg_slot] : nullptr;
     a.vimg_index = st.vimg_index_slot >= 0 ? (const int32_t *)ptrs[st.vimg_index_slot] : nullptr;
+    a.tc_weights = st.tc_weight_slot >= 0 ? (const float *)ptrs[st.tc_weight_slot] : nullptr;
     for (int i = 0; i < 2; ++i)
         a.vsrc[i].ptr = st.vsrc_slot[i] >= 0 ? (const uint8_t *)ptrs[st.vsrc_slot[i]] : nullptr;
     return a;

@@ -208,6 +208,7 @@ struct Step {
     int idx_x_slot = -1, idx_y_slot = -1, weight_slot = -1;
     int vfirst_slot = -1, vcount_slot = -1, vweight_slot = -1;   // RESAMPLE_2D vertical tables
     int vimg_slot = -1, vimg_index_slot = -1;                   // RESAMPLE_2D tensor-core band images
+    int tc_weight_slot = -1;                                    // and its 16-byte-row horizontal weights
     int vsrc_slot[2] = {-1, -1};                                // AFFINE virt1: the gathered producer's sources
     uint64_t copy_bytes = 0;
     // Copy of rows between different row strides (copy_rows > 0): copy_bytes per row.

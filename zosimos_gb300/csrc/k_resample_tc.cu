@@ -38,6 +38,9 @@
 
 #define ZS_TC_STAGES 4                                                     // ring slots (narrow tiles)
 #define ZS_TC_EPI_WARPS 16
+#ifndef ZS_TC_TAPB
+#define ZS_TC_TAPB 8                                                       // taps per TMEM-load batch
+#endif
 #define ZS_TC_THREADS (64 + 32 * ZS_TC_EPI_WARPS)
 #define ZS_TC_ATOM_BYTES (ZS_TC_K * 128)                                   // 64 rows x 128 B
 // Narrow tiles (<= 4 atoms): 4 stages of {A, 4 atoms}, two 256-column accumulators.
@@ -46,8 +49,8 @@
 #define ZS_TC_STAGE_BYTES (ZS_TC_CHUNK_BYTES + 4 * ZS_TC_ATOM_BYTES)
 #define ZS_TC_WIDE_STAGE_BYTES (ZS_TC_CHUNK_BYTES + 8 * ZS_TC_ATOM_BYTES)
 #define ZS_TC_TMEM_COLS 512
-// Per-tile horizontal tables (weights [tw][taps], first tap [tw], tap count [tw]) for tw <= 32,
-// taps <= 64, one per accumulator buffer.
+// Per-tile horizontal tables (weights [tw][tc_taps], first tap [tw], tap count [tw]) for
+// tw <= 32, tc_taps <= 64, one per accumulator buffer.
 #define ZS_TC_TAB_BYTES ((32 * 64 + 2 * 32) * 4)
 #define ZS_TC_SMEM (ZS_TC_STAGES * ZS_TC_STAGE_BYTES + 2 * ZS_TC_TAB_BYTES + 1024 + 256)
 
@@ -207,7 +210,7 @@ __global__ void __launch_bounds__(ZS_TC_THREADS, 1)
         // ---------------------------------------------------------------- MMAs
         uint32_t it = 0, lt = 0, tabs = 0;
         const uint32_t idesc0 = tc_idesc(64 * (wide ? 4 : atoms)), idesc1 = tc_idesc(64 * (wide ? atoms - 4 : 4));
-        const uint32_t wbytes = (uint32_t)(a.tc_tw * a.taps * 4), ibytes = (uint32_t)(a.tc_tw * 4);
+        const uint32_t wbytes = (uint32_t)(a.tc_tw * a.tc_taps * 4), ibytes = (uint32_t)(a.tc_tw * 4);
         for (int t = blockIdx.x; t < tiles && !*abort_flag; t += gridDim.x, ++lt) {
             const TcTile tt = tc_tile(a, t, tiles_x);
             const int nk = a.vimg_index[2 * tt.band + 1];
@@ -220,7 +223,7 @@ __global__ void __launch_bounds__(ZS_TC_THREADS, 1)
                 const uint32_t bar = zs_smem_addr(tabfull + ab);
                 const uint32_t tb = zs_smem_addr(tab + ab * ZS_TC_TAB_BYTES);
                 zs_mbar_expect_tx(bar, wbytes + 2 * ibytes);
-                zs_bulk_g2s(tb, a.weights + (int64_t)tt.x0 * a.taps, wbytes, bar);
+                zs_bulk_g2s(tb, a.tc_weights + (int64_t)tt.x0 * a.tc_taps, wbytes, bar);
                 zs_bulk_g2s(tb + wbytes, a.index_x + tt.x0, ibytes, bar);
                 zs_bulk_g2s(tb + wbytes + ibytes, a.index_y + tt.x0, ibytes, bar);
                 ++tabs;
@@ -271,7 +274,7 @@ __global__ void __launch_bounds__(ZS_TC_THREADS, 1)
             if (!tc_wait(zs_smem_addr(tfull + ab), (lt / nbuf) & 1u, abort_flag)) break;
             tc_fence_after();
             const float *tw_w = (const float *)(tab + ab * ZS_TC_TAB_BYTES);
-            const int *tw_first = (const int *)(tw_w + a.tc_tw * a.taps);
+            const int *tw_first = (const int *)(tw_w + a.tc_tw * a.tc_taps);
             const int *tw_cnt = tw_first + a.tc_tw;
             const int oy = tt.band * ZS_TC_M + m;
             const uint32_t trow = tmem + ((uint32_t)(quarter * 32) << 16) + ab * accw;
@@ -279,28 +282,35 @@ __global__ void __launch_bounds__(ZS_TC_THREADS, 1)
                 const int oxl = ox - tt.x0;
                 const int cnt = tw_cnt[oxl];
                 const uint32_t col = (uint32_t)(tw_first[oxl] - tt.cs0) * 4u;
-                const float *w = tw_w + oxl * a.taps;
+                const float *w = tw_w + oxl * a.tc_taps;   // 16-byte rows
                 // Two accumulator pairs (even and odd taps) halve the FMA dependency chains.
                 float2 a01 = make_float2(0.f, 0.f), a23 = make_float2(0.f, 0.f);
                 float2 b01 = make_float2(0.f, 0.f), b23 = make_float2(0.f, 0.f);
-                for (int k0 = 0; k0 < cnt; k0 += 8) {
-                    const int n = min(8, cnt - k0);
-                    uint32_t r[8][4];
-                    float wk[8];
+                for (int k0 = 0; k0 < cnt; k0 += ZS_TC_TAPB) {
+                    const int n = min(ZS_TC_TAPB, cnt - k0);
+                    uint32_t r[ZS_TC_TAPB][4];
+                    float wk[ZS_TC_TAPB];
 #pragma unroll
-                    for (int j = 0; j < 8; ++j)
+                    for (int j = 0; j < ZS_TC_TAPB; ++j)
                         if (j < n) tc_ld4(trow + col + 4u * (uint32_t)(k0 + j), r[j]);
 #pragma unroll
-                    for (int j = 0; j < 8; ++j)
-                        if (j < n) wk[j] = w[k0 + j];
+                    for (int j = 0; j < ZS_TC_TAPB; j += 4)
+                        if (j < n) {
+                            // k0 + j < cnt <= tc_taps, both multiples of 4: inside the row.
+                            const float4 q = *reinterpret_cast<const float4 *>(w + k0 + j);
+                            wk[j] = q.x;
+                            wk[j + 1] = q.y;
+                            wk[j + 2] = q.z;
+                            wk[j + 3] = q.w;
+                        }
                     tc_wait_ld();
                     // Tie the loaded registers to the wait so that no use moves above it.
 #pragma unroll
-                    for (int j = 0; j < 8; ++j)
+                    for (int j = 0; j < ZS_TC_TAPB; ++j)
                         if (j < n)
                             asm volatile("" : "+r"(r[j][0]), "+r"(r[j][1]), "+r"(r[j][2]), "+r"(r[j][3]));
 #pragma unroll
-                    for (int j = 0; j < 8; ++j)
+                    for (int j = 0; j < ZS_TC_TAPB; ++j)
                         if (j < n) {
                             const float2 w2 = make_float2(wk[j], wk[j]);
                             const float2 v01 = make_float2(__uint_as_float(r[j][0]), __uint_as_float(r[j][1]));
@@ -360,7 +370,8 @@ PFN_cuTensorMapEncodeTiled_v12000 encode_tiled() {
 
 bool resample_tc_usable(const ZsRasterArgs &a) {
     const ZsSource &s = a.src[0];
-    return a.tc_tw > 0 && a.vimg && a.vimg_index && s.fmt.fast == ZS_FAST_F16X4 && ((uintptr_t)s.ptr & 15) == 0 &&
+    return a.tc_tw > 0 && a.vimg && a.vimg_index && a.tc_weights && a.tc_taps % 4 == 0 && a.tc_taps <= 64 &&
+           s.fmt.fast == ZS_FAST_F16X4 && ((uintptr_t)s.ptr & 15) == 0 &&
            (s.stride & 15) == 0 && a.tc_atoms >= 1 && a.tc_atoms <= ZS_TC_MAX_ATOMS && encode_tiled() != nullptr;
 }
 

@@ -131,6 +131,9 @@ struct ZsRasterArgs {
     const int32_t *vimg_index;    // per band of 128 output rows: first chunk, chunk count
     int32_t tc_tw;                // output columns per tile
     int32_t tc_atoms;             // 64-element column blocks of source staged per tile (N = 64 * atoms)
+    const float *tc_weights;      // horizontal weights [padded width][tc_taps], rows zero-padded
+    int32_t tc_taps;              // taps rounded up to a multiple of 4 (16-byte weight rows)
+    int32_t tc_pad;
     // destination
     uint8_t *dst;
     int64_t dst_stride;
