@@ -105,8 +105,9 @@ __global__ void __launch_bounds__(256) zs_layers_f16_kernel(const __grid_constan
                     const float fx0 = floorf(txf), fy0 = floorf(tyf);
                     const float fx = txf - fx0, fy = tyf - fy0;
                     const int x0 = (int)fx0, y0i = (int)fy0;
-                    const int xa = zs_clampi(x0, 0, L.width - 1), xb = zs_clampi(x0 + 1, 0, L.width - 1);
-                    const int ya = zs_clampi(y0i, 0, L.height - 1), yb = zs_clampi(y0i + 1, 0, L.height - 1);
+                    // 0 <= q < size puts the first tap in [-1, size - 1]: one bound per tap.
+                    const int xa = max(x0, 0), xb = min(x0 + 1, L.width - 1);
+                    const int ya = max(y0i, 0), yb = min(y0i + 1, L.height - 1);
                     const uint8_t *ra = base + (int64_t)ya * stride, *rb = base + (int64_t)yb * stride;
                     const float4 t00 = zs_h4(__ldg((const uint2 *)(ra + (int64_t)xa * 8)));
                     const float4 t01 = zs_h4(__ldg((const uint2 *)(ra + (int64_t)xb * 8)));
@@ -125,9 +126,13 @@ __global__ void __launch_bounds__(256) zs_layers_f16_kernel(const __grid_constan
         for (int p = 0; p < 2; ++p) {
             if (p == 1 && !two) break;
             const int y = y0 + 4 * p;
+            uint8_t *dp = a.dst + (int64_t)y * a.dst_stride + (int64_t)x * a.dst_fmt.bpp;
+            if (zs_plain_f16_out(a.prog, a.dst_fmt)) {
+                zs_store_f16x4(dp, acc[p]);
+                continue;
+            }
             float4 r = acc[p], r2 = make_float4(0.f, 0.f, 0.f, 0.f);
             zs_run_program(a.prog, a.fmts, r, r2);
-            uint8_t *dp = a.dst + (int64_t)y * a.dst_stride + (int64_t)x * a.dst_fmt.bpp;
             zs_store_raw(dp, a.dst_fmt.bpp, zs_encode_raw(a.dst_fmt, r));
         }
     }

@@ -336,6 +336,7 @@ __global__ void __launch_bounds__(256) zs_affine_f16_kernel(const __grid_constan
     const int64_t n = (int64_t)tiles_x * ((a.height + 15) >> 4) * 256;
     const int64_t step = (int64_t)gridDim.x * blockDim.x;
     const float fw = (float)s1.width, fh = (float)s1.height;
+    const bool plain = zs_plain_f16_out(a.prog, a.dst_fmt);
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += step) {
         const int64_t tile = i >> 8;
         const int t = (int)(i & 255), w = t >> 5, l = t & 31;
@@ -356,8 +357,9 @@ __global__ void __launch_bounds__(256) zs_affine_f16_kernel(const __grid_constan
                 const float fx0 = floorf(txf), fy0 = floorf(tyf);
                 const float fx = txf - fx0, fy = tyf - fy0;
                 const int x0 = (int)fx0, y0i = (int)fy0;
-                const int xa = zs_clampi(x0, 0, s1.width - 1), xb = zs_clampi(x0 + 1, 0, s1.width - 1);
-                const int ya = zs_clampi(y0i, 0, s1.height - 1), yb = zs_clampi(y0i + 1, 0, s1.height - 1);
+                // 0 <= q < size puts the first tap in [-1, size - 1]: one bound per tap is enough.
+                const int xa = max(x0, 0), xb = min(x0 + 1, s1.width - 1);
+                const int ya = max(y0i, 0), yb = min(y0i + 1, s1.height - 1);
                 const uint8_t *ra = s1.ptr + (int64_t)ya * s1.stride, *rb = s1.ptr + (int64_t)yb * s1.stride;
                 const float4 t00 = zs_h4(__ldg((const uint2 *)(ra + (int64_t)xa * 8)));
                 const float4 t01 = zs_h4(__ldg((const uint2 *)(ra + (int64_t)xb * 8)));
@@ -374,9 +376,13 @@ __global__ void __launch_bounds__(256) zs_affine_f16_kernel(const __grid_constan
         for (int p = 0; p < 2; ++p) {
             const int y = y0 + 4 * p;
             if (y >= a.height) break;
+            uint8_t *dp = a.dst + (int64_t)y * a.dst_stride + (int64_t)x * a.dst_fmt.bpp;
+            if (plain) {
+                zs_store_f16x4(dp, r[p]);
+                continue;
+            }
             float4 v = r[p], r2 = make_float4(0.f, 0.f, 0.f, 0.f);
             zs_run_program(a.prog, a.fmts, v, r2);
-            uint8_t *dp = a.dst + (int64_t)y * a.dst_stride + (int64_t)x * a.dst_fmt.bpp;
             zs_store_raw(dp, a.dst_fmt.bpp, zs_encode_raw(a.dst_fmt, v));
         }
     }

@@ -266,6 +266,7 @@ __global__ void __launch_bounds__(ZS_TC_THREADS, 1)
         const int quarter = warp & 3;      // TMEM lanes this warp may read
         const int part = e >> 2;           // this warp's outputs: x0 + part + 4 i
         const int m = quarter * 32 + lane;
+        const bool plain = zs_plain_f16_out(a.prog, a.dst_fmt);
         uint32_t lt = 0;
         for (int t = blockIdx.x; t < tiles; t += gridDim.x, ++lt) {
             const TcTile tt = tc_tile(a, t, tiles_x);
@@ -326,10 +327,14 @@ __global__ void __launch_bounds__(ZS_TC_THREADS, 1)
                 }
                 if (oy < a.height) {
                     float4 acc = make_float4(a01.x + b01.x, a01.y + b01.y, a23.x + b23.x, a23.y + b23.y);
-                    float4 r2 = make_float4(0.f, 0.f, 0.f, 0.f);
-                    zs_run_program(a.prog, a.fmts, acc, r2);
                     uint8_t *dp = a.dst + (int64_t)oy * a.dst_stride + (int64_t)ox * a.dst_fmt.bpp;
-                    zs_store_raw(dp, a.dst_fmt.bpp, zs_encode_raw(a.dst_fmt, acc));
+                    if (plain) {
+                        zs_store_f16x4(dp, acc);
+                    } else {
+                        float4 r2 = make_float4(0.f, 0.f, 0.f, 0.f);
+                        zs_run_program(a.prog, a.fmts, acc, r2);
+                        zs_store_raw(dp, a.dst_fmt.bpp, zs_encode_raw(a.dst_fmt, acc));
+                    }
                 }
             }
             tc_fence_before();

@@ -529,6 +529,17 @@ __device__ __forceinline__ void zs_tile_pixel(int64_t i, int tiles_x, int &x, in
 
 __device__ __forceinline__ int zs_clampi(int v, int lo, int hi) { return v < lo ? lo : (v > hi ? hi : v); }
 
+// The common ending of the RGBA16F kernels: no pixel program after the producer and an RGBA16F
+// destination, stored as one 8-byte texel with two packing conversions (the bits zs_encode_raw
+// gives for ZS_FAST_F16X4, without its format dispatch).
+__device__ __forceinline__ bool zs_plain_f16_out(const ZsPixelProgram &P, const ZsFormat &f) {
+    return P.n == 0 && f.fast == ZS_FAST_F16X4;
+}
+__device__ __forceinline__ void zs_store_f16x4(uint8_t *p, float4 c) {
+    const __half2 lo = __floats2half2_rn(c.x, c.y), hi = __floats2half2_rn(c.z, c.w);
+    *(uint2 *)p = make_uint2(*reinterpret_cast<const uint32_t *>(&lo), *reinterpret_cast<const uint32_t *>(&hi));
+}
+
 __device__ __forceinline__ float4 zs_lerp4(float4 a, float4 b, float t) {
     return make_float4(a.x + (b.x - a.x) * t, a.y + (b.y - a.y) * t, a.z + (b.z - a.z) * t,
                        a.w + (b.w - a.w) * t);
