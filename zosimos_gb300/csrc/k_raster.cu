@@ -332,15 +332,16 @@ __global__ void __launch_bounds__(256) zs_raster_kernel(const __grid_constant__ 
 // thread takes two pixels four rows apart (two samples in flight).
 __global__ void __launch_bounds__(256) zs_affine_f16_kernel(const __grid_constant__ ZsRasterArgs a) {
     const ZsSource &s0 = a.src[0], &s1 = a.src[1];
+    // 32-bit tile arithmetic: the launcher takes this kernel below 2^31 threads' worth of tiles.
     const int tiles_x = (a.width + 31) >> 5;
-    const int64_t n = (int64_t)tiles_x * ((a.height + 15) >> 4) * 256;
-    const int64_t step = (int64_t)gridDim.x * blockDim.x;
+    const int n = tiles_x * ((a.height + 15) >> 4) * 256;
+    const int step = gridDim.x * blockDim.x;
     const float fw = (float)s1.width, fh = (float)s1.height;
     const bool plain = zs_plain_f16_out(a.prog, a.dst_fmt);
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += step) {
-        const int64_t tile = i >> 8;
-        const int t = (int)(i & 255), w = t >> 5, l = t & 31;
-        const int ty = (int)(tile / tiles_x), tx = (int)(tile - (int64_t)ty * tiles_x);
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += step) {
+        const int tile = i >> 8;
+        const int t = i & 255, w = t >> 5, l = t & 31;
+        const int ty = tile / tiles_x, tx = tile - ty * tiles_x;
         const int x = (tx << 5) + ((w & 3) << 3) + (l & 7);
         const int y0 = (ty << 4) + ((w >> 2) << 3) + (l >> 3);
         if (x >= a.width || y0 >= a.height) continue;
@@ -396,7 +397,8 @@ cudaError_t launch_raster(const ZsRasterArgs &args, int sm_count, cudaStream_t s
     if (args.producer == ZS_PR_RESAMPLE_2D) return launch_resample2d(args, sm_count, stream);
     if (args.producer == ZS_PR_AFFINE && args.bilinear && !args.raw_copy && !args.virt1 &&
         args.src[1].fmt.fast == ZS_FAST_F16X4 &&
-        args.aff[6] == 0.f && args.aff[7] == 0.f && args.aff[8] == 1.f) {
+        args.aff[6] == 0.f && args.aff[7] == 0.f && args.aff[8] == 1.f &&
+        (int64_t)((args.width + 31) / 32) * ((args.height + 15) / 16) * 256 + (int64_t)(sm_count > 0 ? sm_count : 148) * 8 * 256 < INT32_MAX) {
         int64_t blocks = (int64_t)((args.width + 31) / 32) * ((args.height + 15) / 16);
         const int64_t cap = (int64_t)(sm_count > 0 ? sm_count : 148) * 8;
         if (blocks > cap) blocks = cap;
