@@ -328,13 +328,14 @@ __global__ void __launch_bounds__(256) zs_raster_kernel(const __grid_constant__ 
 
 // AFFINE with bilinear sampling of an RGBA16F image under an affine (not projective)
 // inverse: the same arithmetic, in the same order, as the generic kernel's AFFINE case
-// without the per-tap format dispatch.  Tiles of 32 x 16 pixels (8 x 8 per warp); each
-// thread takes two pixels four rows apart (two samples in flight).
+// without the per-tap format dispatch.  Tiles of 32 x 32 pixels (8 x 16 per warp); each
+// thread takes four pixels four rows apart (four samples in flight).
+#define ZS_AFF_PX 4
 __global__ void __launch_bounds__(256) zs_affine_f16_kernel(const __grid_constant__ ZsRasterArgs a) {
     const ZsSource &s0 = a.src[0], &s1 = a.src[1];
     // 32-bit tile arithmetic: the launcher takes this kernel below 2^31 threads' worth of tiles.
     const int tiles_x = (a.width + 31) >> 5;
-    const int n = tiles_x * ((a.height + 15) >> 4) * 256;
+    const int n = tiles_x * ((a.height + 8 * ZS_AFF_PX - 1) / (8 * ZS_AFF_PX)) * 256;
     const int step = gridDim.x * blockDim.x;
     const float fw = (float)s1.width, fh = (float)s1.height;
     const bool plain = zs_plain_f16_out(a.prog, a.dst_fmt);
@@ -343,12 +344,12 @@ __global__ void __launch_bounds__(256) zs_affine_f16_kernel(const __grid_constan
         const int t = i & 255, w = t >> 5, l = t & 31;
         const int ty = tile / tiles_x, tx = tile - ty * tiles_x;
         const int x = (tx << 5) + ((w & 3) << 3) + (l & 7);
-        const int y0 = (ty << 4) + ((w >> 2) << 3) + (l >> 3);
+        const int y0 = ty * (8 * ZS_AFF_PX) + (w >> 2) * (4 * ZS_AFF_PX) + (l >> 3);
         if (x >= a.width || y0 >= a.height) continue;
         const float cx = (float)x + 0.5f;
-        float4 r[2];
+        float4 r[ZS_AFF_PX];
 #pragma unroll
-        for (int p = 0; p < 2; ++p) {
+        for (int p = 0; p < ZS_AFF_PX; ++p) {
             const int y = min(y0 + 4 * p, a.height - 1);
             const float cy = (float)y + 0.5f;
             const float qx = fmaf(a.aff[0], cx, fmaf(a.aff[1], cy, a.aff[2]));
@@ -374,7 +375,7 @@ __global__ void __launch_bounds__(256) zs_affine_f16_kernel(const __grid_constan
             }
         }
 #pragma unroll
-        for (int p = 0; p < 2; ++p) {
+        for (int p = 0; p < ZS_AFF_PX; ++p) {
             const int y = y0 + 4 * p;
             if (y >= a.height) break;
             uint8_t *dp = a.dst + (int64_t)y * a.dst_stride + (int64_t)x * a.dst_fmt.bpp;
@@ -398,8 +399,9 @@ cudaError_t launch_raster(const ZsRasterArgs &args, int sm_count, cudaStream_t s
     if (args.producer == ZS_PR_AFFINE && args.bilinear && !args.raw_copy && !args.virt1 &&
         args.src[1].fmt.fast == ZS_FAST_F16X4 &&
         args.aff[6] == 0.f && args.aff[7] == 0.f && args.aff[8] == 1.f &&
-        (int64_t)((args.width + 31) / 32) * ((args.height + 15) / 16) * 256 + (int64_t)(sm_count > 0 ? sm_count : 148) * 8 * 256 < INT32_MAX) {
-        int64_t blocks = (int64_t)((args.width + 31) / 32) * ((args.height + 15) / 16);
+        (int64_t)((args.width + 31) / 32) * ((args.height + 8 * ZS_AFF_PX - 1) / (8 * ZS_AFF_PX)) * 256 +
+                (int64_t)(sm_count > 0 ? sm_count : 148) * 8 * 256 < INT32_MAX) {
+        int64_t blocks = (int64_t)((args.width + 31) / 32) * ((args.height + 8 * ZS_AFF_PX - 1) / (8 * ZS_AFF_PX));
         const int64_t cap = (int64_t)(sm_count > 0 ? sm_count : 148) * 8;
         if (blocks > cap) blocks = cap;
         zs_affine_f16_kernel<<<(unsigned)blocks, 256, 0, stream>>>(args);
