@@ -68,23 +68,23 @@ __global__ void __launch_bounds__(256) zs_layers_kernel(const __grid_constant__ 
 // The common stack: RGBA16F layers sampled bilinearly through affine inverses, premultiplied
 // operands, no lossy quantisation (FP32 quantisation is the identity).  Same arithmetic, in
 // the same order, as zs_layer_sample + zs_blend_px, without the per-tap format dispatch; each
-// thread takes two pixels four rows apart so that a layer's parameters are read once per
-// pair and two samples are in flight.  Tiles of 32 x 16 pixels, 8 x 8 per warp.
+// thread takes four pixels four rows apart so that a layer's parameters are read once per
+// four pixels and four samples are in flight.  Tiles of 32 x 32 pixels, 8 x 16 per warp.
+#define ZS_LAY_PX 4   // pixels per thread, four rows apart
 __global__ void __launch_bounds__(256) zs_layers_f16_kernel(const __grid_constant__ ZsLayersArgs a) {
     const int tiles_x = (a.width + 31) >> 5;
-    const int64_t n = (int64_t)tiles_x * ((a.height + 15) >> 4) * 256;
+    const int64_t n = (int64_t)tiles_x * ((a.height + 8 * ZS_LAY_PX - 1) / (8 * ZS_LAY_PX)) * 256;
     const int64_t step = (int64_t)gridDim.x * blockDim.x;
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += step) {
         const int64_t tile = i >> 8;
         const int t = (int)(i & 255), w = t >> 5, l = t & 31;
         const int ty = (int)(tile / tiles_x), tx = (int)(tile - (int64_t)ty * tiles_x);
         const int x = (tx << 5) + ((w & 3) << 3) + (l & 7);
-        const int y0 = (ty << 4) + ((w >> 2) << 3) + (l >> 3);
+        const int y0 = ty * (8 * ZS_LAY_PX) + (w >> 2) * (4 * ZS_LAY_PX) + (l >> 3);
         if (x >= a.width || y0 >= a.height) continue;
-        const bool two = y0 + 4 < a.height;
-        float4 acc[2];
+        float4 acc[ZS_LAY_PX];
 #pragma unroll
-        for (int p = 0; p < 2; ++p)
+        for (int p = 0; p < ZS_LAY_PX; ++p)
             acc[p] = a.has_base ? zs_load_px(a.base, x, min(y0 + 4 * p, a.height - 1))
                                 : make_float4(a.base_color[0], a.base_color[1], a.base_color[2], a.base_color[3]);
         const float cx = (float)x + 0.5f;
@@ -94,9 +94,9 @@ __global__ void __launch_bounds__(256) zs_layers_f16_kernel(const __grid_constan
             const float fw = (float)L.width, fh = (float)L.height;
             const uint8_t *base = L.ptr;
             const int64_t stride = L.stride;
-            float4 s[2];
+            float4 s[ZS_LAY_PX];
 #pragma unroll
-            for (int p = 0; p < 2; ++p) {
+            for (int p = 0; p < ZS_LAY_PX; ++p) {
                 const float cy = (float)(y0 + 4 * p) + 0.5f;
                 const float qx = fmaf(i0, cx, fmaf(i1, cy, i2));
                 const float qy = fmaf(i3, cx, fmaf(i4, cy, i5));
@@ -119,13 +119,13 @@ __global__ void __launch_bounds__(256) zs_layers_f16_kernel(const __grid_constan
                 }
             }
             const uint32_t mode = L.mode;
-            zs_blend_px(acc[0], s[0], mode, 0);
-            zs_blend_px(acc[1], s[1], mode, 0);
+#pragma unroll
+            for (int p = 0; p < ZS_LAY_PX; ++p) zs_blend_px(acc[p], s[p], mode, 0);
         }
 #pragma unroll
-        for (int p = 0; p < 2; ++p) {
-            if (p == 1 && !two) break;
+        for (int p = 0; p < ZS_LAY_PX; ++p) {
             const int y = y0 + 4 * p;
+            if (y >= a.height) break;
             uint8_t *dp = a.dst + (int64_t)y * a.dst_stride + (int64_t)x * a.dst_fmt.bpp;
             if (zs_plain_f16_out(a.prog, a.dst_fmt)) {
                 zs_store_f16x4(dp, acc[p]);
@@ -143,7 +143,7 @@ namespace zs {
 cudaError_t launch_layers(const ZsLayersArgs &args, int sm_count, cudaStream_t stream) {
     if (args.width <= 0 || args.height <= 0) return cudaSuccess;
     if (args.f16_bilinear) {
-        int64_t blocks = (int64_t)((args.width + 31) / 32) * ((args.height + 15) / 16);
+        int64_t blocks = (int64_t)((args.width + 31) / 32) * ((args.height + 8 * ZS_LAY_PX - 1) / (8 * ZS_LAY_PX));
         const int64_t cap = (int64_t)(sm_count > 0 ? sm_count : 148) * 8;
         if (blocks > cap) blocks = cap;
         zs_layers_f16_kernel<<<(unsigned)blocks, 256, 0, stream>>>(args);
